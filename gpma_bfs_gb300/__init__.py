@@ -1,0 +1,349 @@
+"""GB300-native GPMA+ (dynamic graph in a GPU packed memory array) and BFS.
+
+Python mirror of the reference's C++ interface (recolic/gpma_bfs), over the
+C ABI in ``include/gpma_gb300.h`` (``libgpma_gb300.so``, built in-tree for
+sm_103a by ``gpma_bfs_gb300/build.py``):
+
+* ``GPMA(row_num)``                      - ``GPMA<GPU>::GPMA`` (gpma.cuh:79-82)
+* ``update_gpma(gpma, keys, values)``    - ``update_gpma`` (gpma.cuh:968-1050)
+* ``gpma_bfs(gpma, node_size, edge_size, start_node, results)``
+                                         - ``gpma_bfs`` (gpma_bfs.cuh:511-533)
+
+Arrays may be numpy arrays (host) or torch tensors (host or CUDA). There is
+no CPU fallback: every compute call goes to the CUDA library, and importing
+fails loudly if the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+__all__ = [
+    "GPMA", "GPMAError", "update_gpma", "gpma_bfs", "gpma_bfs_multi", "lib", "library_path",
+    "KEY_NONE", "KEY_MAX", "COL_IDX_NONE", "VALUE_NONE", "gen_rmat", "gen_chung_lu", "edges_to_keys",
+    "read_edges_text", "write_edges_text",
+]
+
+KEY_NONE = 0xFFFFFFFFFFFFFFFF  # gpma.cuh:15
+KEY_MAX = KEY_NONE - 1         # gpma.cuh:16
+COL_IDX_NONE = 0xFFFFFFFF      # gpma.cuh:19
+VALUE_NONE = 0                 # gpma.cuh:18
+
+_PKG = Path(__file__).resolve().parent
+library_path = _PKG / "libgpma_gb300.so"
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "out of memory", 4: "capacity exceeded",
+          5: "device wait timed out", 6: "I/O error", 7: "device-side check failed"}
+
+
+class GPMAError(RuntimeError):
+    """A C-ABI call returned a non-zero gpma_status."""
+
+    def __init__(self, status: int, where: str, detail: str):
+        super().__init__(f"{where}: {STATUS.get(status, status)}: {detail}")
+        self.status = status
+
+
+class _Geometry(ctypes.Structure):
+    _fields_ = [("size", ctypes.c_uint32), ("segment_length", ctypes.c_uint32),
+                ("tree_height", ctypes.c_uint32), ("row_num", ctypes.c_uint32)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "updates", "submitted", "last_inserts", "levels_visited", "accepted_windows", "accepted_slots",
+        "root_resizes", "root_drops", "significant")]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded C-ABI library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = Path(os.environ.get("GPMA_GB300_LIB", library_path))
+    if not path.exists():
+        raise ImportError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = ctypes.CDLL(str(path))
+    P, u32, u64, st = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+    sig = {
+        "gpma_create": (st, [u32, P, ctypes.POINTER(P)]),
+        "gpma_destroy": (st, [P]),
+        "gpma_update": (st, [P, P, P, u64, P]),
+        "gpma_bfs": (st, [P, u32, P, ctypes.POINTER(u64), P]),
+        "gpma_bfs_multi": (st, [P, P, u32, P, P, P]),
+        "gpma_get_geometry": (st, [P, ctypes.POINTER(_Geometry)]),
+        "gpma_get_thresholds": (st, [P, P, P]),
+        "gpma_export_layout": (st, [P, P, P, P, P]),
+        "gpma_export_compact": (st, [P, P, u64, ctypes.POINTER(u64), P]),
+        "gpma_device_arrays": (st, [P, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P)]),
+        "gpma_get_stats": (st, [P, ctypes.POINTER(_Stats)]),
+        "gpma_status_string": (ctypes.c_char_p, [st]),
+        "gpma_last_error": (ctypes.c_char_p, []),
+        "gpma_version": (ctypes.c_char_p, []),
+        "gpma_gen_rmat": (st, [u32, u32, ctypes.c_double, ctypes.c_double, ctypes.c_double, u64, P, P, u64,
+                               ctypes.POINTER(u64)]),
+        "gpma_gen_chung_lu": (st, [u32, u64, ctypes.c_double, u32, u64, P, P]),
+        "gpma_edges_to_keys": (st, [P, P, u64, P]),
+        "gpma_read_edges_text": (st, [ctypes.c_char_p, ctypes.POINTER(u32), ctypes.POINTER(u64), P, P, u64]),
+        "gpma_write_edges_text": (st, [ctypes.c_char_p, u32, P, P, u64]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(status: int, where: str) -> None:
+    if status != 0:
+        raise GPMAError(status, where, lib().gpma_last_error().decode(errors="replace"))
+
+
+def _ptr(a) -> tuple[int, object]:
+    """(address, keep-alive) of a contiguous numpy array or torch tensor."""
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            a = np.ascontiguousarray(a)
+        return a.ctypes.data, a
+    data_ptr = getattr(a, "data_ptr", None)
+    if data_ptr is not None:
+        if not a.is_contiguous():
+            a = a.contiguous()
+        return a.data_ptr(), a
+    raise TypeError(f"expected a numpy array or torch tensor, got {type(a).__name__}")
+
+
+def _stream_ptr(stream) -> int | None:
+    if stream is None:
+        return None
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+def _is_cuda(a) -> bool:
+    return getattr(a, "is_cuda", False)
+
+
+class GPMA:
+    """A dynamic directed graph of ``row_num`` nodes on the current GPU.
+
+    Mirrors ``GPMA<GPU>`` (gpma.cuh:31-102): the constructor inserts one guard
+    key per row; ``keys``, ``values`` and ``row_offset`` are exported copies of
+    the device arrays; ``segment_length``, ``tree_height``, ``lower_element``
+    and ``upper_element`` are the current geometry and density thresholds.
+    """
+
+    def __init__(self, row_num: int, stream=None):
+        if row_num < 0 or row_num >= 0xFFFFFFFF:
+            raise ValueError(f"row_num {row_num} out of range")
+        h = ctypes.c_void_p()
+        _check(lib().gpma_create(int(row_num), _stream_ptr(stream), ctypes.byref(h)), "gpma_create")
+        self._h = h
+        self.row_num = int(row_num)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().gpma_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        if not self._h:
+            raise ValueError("GPMA handle is closed")
+        return self._h
+
+    def geometry(self) -> dict:
+        g = _Geometry()
+        _check(lib().gpma_get_geometry(self.handle, ctypes.byref(g)), "gpma_get_geometry")
+        return {"size": g.size, "segment_length": g.segment_length, "tree_height": g.tree_height,
+                "row_num": g.row_num}
+
+    def get_size(self) -> int:
+        return self.geometry()["size"]
+
+    @property
+    def segment_length(self) -> int:
+        return self.geometry()["segment_length"]
+
+    @property
+    def tree_height(self) -> int:
+        return self.geometry()["tree_height"]
+
+    def thresholds(self) -> tuple[np.ndarray, np.ndarray]:
+        h = self.tree_height
+        lo = np.zeros(h + 1, np.uint32)
+        hi = np.zeros(h + 1, np.uint32)
+        _check(lib().gpma_get_thresholds(self.handle, lo.ctypes.data, hi.ctypes.data), "gpma_get_thresholds")
+        return lo, hi
+
+    @property
+    def lower_element(self) -> np.ndarray:
+        return self.thresholds()[0]
+
+    @property
+    def upper_element(self) -> np.ndarray:
+        return self.thresholds()[1]
+
+    def export_layout(self, stream=None) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """(keys, masked values, row_offset) as host arrays."""
+        size = self.get_size()
+        keys = np.empty(size, np.uint64)
+        vals = np.empty(size, np.uint8)
+        ro = np.empty(self.row_num + 1, np.uint32)
+        _check(lib().gpma_export_layout(self.handle, keys.ctypes.data, vals.ctypes.data, ro.ctypes.data,
+                                        _stream_ptr(stream)), "gpma_export_layout")
+        return keys, vals, ro
+
+    @property
+    def keys(self) -> np.ndarray:
+        return self.export_layout()[0]
+
+    @property
+    def values(self) -> np.ndarray:
+        return self.export_layout()[1]
+
+    @property
+    def row_offset(self) -> np.ndarray:
+        return self.export_layout()[2]
+
+    def compact_keys(self, stream=None) -> np.ndarray:
+        n = ctypes.c_uint64()
+        _check(lib().gpma_export_compact(self.handle, None, 0, ctypes.byref(n), _stream_ptr(stream)),
+               "gpma_export_compact")
+        out = np.empty(n.value, np.uint64)
+        _check(lib().gpma_export_compact(self.handle, out.ctypes.data, n.value, ctypes.byref(n),
+                                         _stream_ptr(stream)), "gpma_export_compact")
+        return out
+
+    def stats(self) -> dict:
+        s = _Stats()
+        _check(lib().gpma_get_stats(self.handle, ctypes.byref(s)), "gpma_get_stats")
+        return {name: getattr(s, name) for name, _ in _Stats._fields_}
+
+    def device_arrays(self) -> tuple[int, int, int]:
+        k, v, r = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        _check(lib().gpma_device_arrays(self.handle, ctypes.byref(k), ctypes.byref(v), ctypes.byref(r)),
+               "gpma_device_arrays")
+        return k.value, v.value, r.value
+
+
+def update_gpma(gpma: GPMA, update_keys, update_values, stream=None) -> None:
+    """Applies one batch: value 0 deletes a key, non-zero inserts or modifies.
+
+    Raises ValueError when the key and value counts differ, as the
+    reference's batch entry throws std::invalid_argument (multidev.cuh:107-108).
+    The inputs are left unmodified.
+    """
+    if len(update_keys) != len(update_values):
+        raise ValueError("Inconsistant kv size.")
+    n = len(update_keys)
+    if isinstance(update_keys, np.ndarray):
+        update_keys = np.ascontiguousarray(update_keys, dtype=np.uint64)
+    if isinstance(update_values, np.ndarray):
+        update_values = np.ascontiguousarray(update_values).view(np.uint8) \
+            if update_values.dtype.itemsize == 1 else np.ascontiguousarray(update_values, dtype=np.uint8)
+    kp, kk = _ptr(update_keys)
+    vp, vk = _ptr(update_values)
+    _check(lib().gpma_update(gpma.handle, kp, vp, n, _stream_ptr(stream)), "gpma_update")
+    del kk, vk
+
+
+def gpma_bfs(gpma: GPMA, node_size: int, edge_size: int, start_node: int, results=None, stream=None):
+    """BFS levels from start_node (1 = start, 0 = unreached) into results.
+
+    ``results`` (numpy uint32 array, or torch int32/uint32 tensor on host or
+    GPU, ``node_size`` entries) is allocated when omitted. edge_size is
+    accepted for signature parity (the reference sized its queues with it).
+    Returns (results, reachable node count).
+    """
+    del edge_size
+    if node_size != gpma.row_num:
+        raise ValueError(f"node_size {node_size} != row_num {gpma.row_num}")
+    if results is None:
+        results = np.zeros(node_size, np.uint32)
+    if len(results) < node_size:
+        raise ValueError("results holds fewer than node_size entries")
+    rp, keep = _ptr(results)
+    reached = ctypes.c_uint64()
+    _check(lib().gpma_bfs(gpma.handle, int(start_node), rp, ctypes.byref(reached), _stream_ptr(stream)), "gpma_bfs")
+    del keep
+    return results, reached.value
+
+
+def gpma_bfs_multi(gpma: GPMA, sources, results=None, stream=None):
+    """Up to 64 BFS at once; results is [k][row_num] uint32. Returns (results, reached[k])."""
+    src = np.ascontiguousarray(np.asarray(sources, dtype=np.uint32))
+    k = len(src)
+    if results is None:
+        results = np.zeros((k, gpma.row_num), np.uint32)
+    rp, keep = _ptr(results)
+    reached = np.zeros(k, np.uint64)
+    _check(lib().gpma_bfs_multi(gpma.handle, src.ctypes.data, k, rp, reached.ctypes.data, _stream_ptr(stream)),
+           "gpma_bfs_multi")
+    del keep
+    return results, reached
+
+
+# ---- synthetic graphs and the reference's text format -------------------------
+
+def gen_rmat(scale: int, edge_factor: int, a: float = 0.57, b: float = 0.19, c: float = 0.19, seed: int = 1):
+    """R-MAT edge list (src, dst uint32), self-loops and duplicates removed, shuffled."""
+    cap = edge_factor << scale
+    src = np.empty(cap, np.uint32)
+    dst = np.empty(cap, np.uint32)
+    m = ctypes.c_uint64()
+    _check(lib().gpma_gen_rmat(scale, edge_factor, a, b, c, seed, src.ctypes.data, dst.ctypes.data, cap,
+                               ctypes.byref(m)), "gpma_gen_rmat")
+    return src[: m.value].copy(), dst[: m.value].copy()
+
+
+def gen_chung_lu(n: int, m: int, exponent: float = 2.3, max_degree: int = 9000, seed: int = 2):
+    """Power-law edge list with exactly m distinct non-loop edges, shuffled."""
+    src = np.empty(m, np.uint32)
+    dst = np.empty(m, np.uint32)
+    _check(lib().gpma_gen_chung_lu(n, m, exponent, max_degree, seed, src.ctypes.data, dst.ctypes.data),
+           "gpma_gen_chung_lu")
+    return src, dst
+
+
+def edges_to_keys(src: np.ndarray, dst: np.ndarray) -> np.ndarray:
+    """keys = (src << 32) + dst (gpma_bfs_demo.cu:53)."""
+    return (src.astype(np.uint64) << np.uint64(32)) + dst.astype(np.uint64)
+
+
+def write_edges_text(path: str, n: int, src: np.ndarray, dst: np.ndarray) -> None:
+    src = np.ascontiguousarray(src, np.uint32)
+    dst = np.ascontiguousarray(dst, np.uint32)
+    _check(lib().gpma_write_edges_text(str(path).encode(), n, src.ctypes.data, dst.ctypes.data, len(src)),
+           "gpma_write_edges_text")
+
+
+def read_edges_text(path: str):
+    """(n, src, dst) from a text edge list in the reference's format."""
+    n = ctypes.c_uint32()
+    m = ctypes.c_uint64()
+    _check(lib().gpma_read_edges_text(str(path).encode(), ctypes.byref(n), ctypes.byref(m), None, None, 0),
+           "gpma_read_edges_text")
+    src = np.empty(m.value, np.uint32)
+    dst = np.empty(m.value, np.uint32)
+    _check(lib().gpma_read_edges_text(str(path).encode(), ctypes.byref(n), ctypes.byref(m), src.ctypes.data,
+                                      dst.ctypes.data, m.value), "gpma_read_edges_text")
+    return n.value, src, dst

@@ -1,0 +1,453 @@
+// capi.cu - the extern "C" boundary of the library (include/gpma_gb300.h).
+#include "gpma_internal.cuh"
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+namespace gpma {
+
+static thread_local char g_last_error[512] = "";
+
+void set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+}
+
+gpma_status cuda_fail(cudaError_t e, const char *what) {
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? GPMA_ERR_NOMEM : GPMA_ERR_CUDA;
+}
+
+bool is_device_pointer(const void *p) {
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+gpma_status copy_any(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+    if (bytes == 0)
+        return GPMA_OK;
+    GPMA_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, s));
+    return GPMA_OK;
+}
+
+namespace {
+
+// Stage a pageable host copy through a pinned buffer so the transfer is a
+// true async DMA; device and pinned pointers are copied directly.
+gpma_status copy_in(gpma_graph *g, void *dst_dev, const void *src, size_t bytes, cudaStream_t s) {
+    if (bytes == 0)
+        return GPMA_OK;
+    cudaPointerAttributes attr;
+    bool known = cudaPointerGetAttributes(&attr, src) == cudaSuccess;
+    if (!known)
+        cudaGetLastError();
+    if (known && attr.type != cudaMemoryTypeUnregistered)
+        return copy_any(dst_dev, src, bytes, s);
+    (void)g;
+    GPMA_CUDA(cudaMemcpyAsync(dst_dev, src, bytes, cudaMemcpyHostToDevice, s));
+    return GPMA_OK;
+}
+
+void release(gpma_graph *g) {
+    dev_free(g->keys);
+    dev_free(g->values);
+    dev_free(g->row_offset);
+    dev_free(g->d_lower);
+    dev_free(g->d_upper);
+    dev_free(g->skeys);
+    dev_free(g->svals);
+    dev_free(g->chunk_cnt);
+    for (int i = 0; i < 2; ++i) {
+        dev_free(g->bkeys[i]);
+        dev_free(g->bvals[i]);
+        dev_free(g->wnode[i]);
+        dev_free(g->wa[i]);
+        dev_free(g->wb[i]);
+    }
+    dev_free(g->leaf);
+    dev_free(g->ikeys);
+    dev_free(g->ivals);
+    dev_free(g->ileaf);
+    dev_free(g->wflag);
+    dev_free(g->wlive);
+    dev_free(g->sort_hist);
+    dev_free(g->sort_base);
+    dev_free(g->sort_plan);
+    dev_free(g->sort_tiles);
+    dev_free(g->sort_status);
+    dev_free(g->cta_cnt);
+    dev_free(g->status);
+    if (g->h_status)
+        cudaFreeHost(g->h_status);
+    g->h_status = nullptr;
+    free_bfs(g);
+    if (g->h_bfs_ctl)
+        cudaFreeHost(g->h_bfs_ctl);
+    g->h_bfs_ctl = nullptr;
+}
+
+__global__ void init_layout_kernel(uint64_t *keys, uint8_t *vals) {
+    // init_gpma_members (gpma.cuh:54-69): 4 slots, KEY_MAX at 0 and 2
+    int t = threadIdx.x;
+    if (t < 4) {
+        keys[t] = (t == 0 || t == 2) ? KEY_MAX : KEY_NONE;
+        vals[t] = (t == 0 || t == 2) ? 1 : 0;
+    }
+}
+
+__global__ void guard_keys_kernel(uint64_t *keys, uint8_t *vals, uint32_t row_num) {
+    // init_gpma_insertions (gpma.cuh:70-78): (r << 32) | 0xFFFFFFFF, value 1
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < row_num; r += gridDim.x * blockDim.x) {
+        keys[r] = ((uint64_t)r << 32) + COL_NONE;
+        vals[r] = 1;
+    }
+}
+
+__global__ void mask_values_kernel(const uint64_t *keys, const uint8_t *vals, uint8_t *out, uint32_t size) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < size; t += gridDim.x * blockDim.x)
+        out[t] = keys[t] == KEY_NONE ? 0 : vals[t];
+}
+
+__global__ void live_flags_kernel(const uint64_t *keys, const uint8_t *vals, uint32_t size, uint32_t *chunk_cnt) {
+    __shared__ uint32_t tmp[BLOCK / 32 + 1];
+    uint32_t chunks = (size + CHUNK - 1) / CHUNK;
+    for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {
+        uint32_t cl = 0;
+        for (uint32_t t = c * CHUNK + threadIdx.x; t < min(size, (c + 1) * CHUNK); t += BLOCK)
+            cl += (keys[t] != KEY_NONE && vals[t] != 0);
+        uint32_t s = block_sum(cl, tmp);
+        if (threadIdx.x == 0)
+            chunk_cnt[c] = s;
+    }
+}
+
+__global__ void scan_chunks_kernel(uint32_t *chunk_cnt, uint32_t chunks, uint32_t *total) {
+    __shared__ uint32_t tmp[BLOCK / 32 + 1];
+    uint32_t run = 0;
+    for (uint32_t k0 = 0; k0 < chunks; k0 += BLOCK) {
+        uint32_t k = k0 + threadIdx.x;
+        uint32_t v = k < chunks ? chunk_cnt[k] : 0;
+        uint32_t tot;
+        uint32_t ex = block_excl_scan(v, &tot, tmp);
+        if (k < chunks)
+            chunk_cnt[k] = run + ex;
+        run += tot;
+    }
+    if (threadIdx.x == 0)
+        *total = run;
+}
+
+__global__ void gather_live_kernel(const uint64_t *keys, const uint8_t *vals, uint32_t size, const uint32_t *off,
+                                   uint64_t *out) {
+    __shared__ uint32_t tmp[BLOCK / 32 + 1];
+    constexpr uint32_t K = CHUNK / BLOCK;
+    uint32_t chunks = (size + CHUNK - 1) / CHUNK;
+    for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {
+        uint32_t base = c * CHUNK + threadIdx.x * K;
+        uint32_t cl = 0;
+        for (uint32_t j = 0; j < K; ++j) {
+            uint32_t t = base + j;
+            cl += (t < size && keys[t] != KEY_NONE && vals[t] != 0);
+        }
+        uint32_t tot;
+        uint32_t o = off[c] + block_excl_scan(cl, &tot, tmp);
+        for (uint32_t j = 0; j < K; ++j) {
+            uint32_t t = base + j;
+            if (t < size && keys[t] != KEY_NONE && vals[t] != 0)
+                out[o++] = keys[t];
+        }
+    }
+}
+
+int small_grid(uint64_t work, int sms) {
+    uint64_t g = (work + BLOCK - 1) / BLOCK;
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, (uint64_t)sms * 8));
+}
+
+}  // namespace
+}  // namespace gpma
+
+using namespace gpma;
+
+extern "C" {
+
+const char *gpma_version(void) { return "gpma_gb300 0.1 (sm_103a)"; }
+
+const char *gpma_last_error(void) { return g_last_error; }
+
+const char *gpma_status_string(gpma_status s) {
+    switch (s) {
+    case GPMA_OK: return "ok";
+    case GPMA_ERR_INVALID: return "invalid argument";
+    case GPMA_ERR_CUDA: return "CUDA runtime error";
+    case GPMA_ERR_NOMEM: return "out of memory";
+    case GPMA_ERR_CAPACITY: return "capacity exceeded";
+    case GPMA_ERR_TIMEOUT: return "device wait timed out";
+    case GPMA_ERR_IO: return "I/O error";
+    case GPMA_ERR_DEVICE: return "device-side check failed";
+    }
+    return "unknown status";
+}
+
+gpma_status gpma_create(uint32_t row_num, void *stream, gpma_graph **out) {
+    if (!out) {
+        set_error("gpma_create: out is NULL");
+        return GPMA_ERR_INVALID;
+    }
+    *out = nullptr;
+    if (row_num >= 0xFFFFFFFFu) {
+        set_error("gpma_create: row_num %u leaves no room for the reserved column", row_num);
+        return GPMA_ERR_INVALID;
+    }
+    gpma_graph *g = new (std::nothrow) gpma_graph();
+    if (!g) {
+        set_error("gpma_create: host allocation failed");
+        return GPMA_ERR_NOMEM;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    gpma_status st = [&]() -> gpma_status {
+        GPMA_CUDA(cudaGetDevice(&g->device));
+        GPMA_CUDA(cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, g->device));
+        g->row_num = row_num;
+        g->cap = 4;
+        GPMA_TRY(dev_alloc(&g->keys, 4));
+        GPMA_TRY(dev_alloc(&g->values, 4));
+        GPMA_TRY(dev_alloc(&g->row_offset, (uint64_t)row_num + 1));
+        GPMA_TRY(dev_alloc(&g->d_lower, 32));
+        GPMA_TRY(dev_alloc(&g->d_upper, 32));
+        GPMA_TRY(dev_alloc(&g->sort_hist, 8 * 256));
+        GPMA_TRY(dev_alloc(&g->sort_base, 8 * 256));
+        GPMA_TRY(dev_alloc(&g->sort_plan, 1));
+        GPMA_TRY(dev_alloc(&g->sort_tiles, 8));
+        GPMA_TRY(dev_alloc(&g->status, 1));
+        cudaError_t e = cudaMallocHost((void **)&g->h_status, sizeof(DeviceStatus));
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaMallocHost(status)");
+        GPMA_TRY(ensure_scratch(g, 4));
+        GPMA_CUDA(cudaMemsetAsync(g->row_offset, 0, sizeof(uint32_t) * ((uint64_t)row_num + 1), s));
+        init_layout_kernel<<<1, 32, 0, s>>>(g->keys, g->values);
+        GPMA_CUDA(cudaGetLastError());
+        g->geo.size = 4;
+        g->geo.seg = 2;
+        g->geo.height = 1;
+        recalculate_density(g->geo);
+        GPMA_TRY(upload_geometry(g, s));
+        if (row_num == 0)
+            return GPMA_OK;
+        GPMA_TRY(ensure_batch(g, row_num));
+        guard_keys_kernel<<<small_grid(row_num, g->sms), BLOCK, 0, s>>>(g->bkeys[0], g->bvals[0], row_num);
+        GPMA_CUDA(cudaGetLastError());
+        return update_device(g, row_num, s);
+    }();
+    if (st != GPMA_OK) {
+        release(g);
+        delete g;
+        return st;
+    }
+    g->stats = gpma_stats{};
+    *out = g;
+    return GPMA_OK;
+}
+
+gpma_status gpma_destroy(gpma_graph *g) {
+    if (!g)
+        return GPMA_OK;
+    cudaDeviceSynchronize();
+    release(g);
+    delete g;
+    return GPMA_OK;
+}
+
+gpma_status gpma_update(gpma_graph *g, const uint64_t *keys, const uint8_t *values, uint64_t n, void *stream) {
+    if (!g || (n && (!keys || !values))) {
+        set_error("gpma_update: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    if (n >= (1ull << 30)) {
+        set_error("gpma_update: batch of %llu keys exceeds 2^30", (unsigned long long)n);
+        return GPMA_ERR_CAPACITY;
+    }
+    g->stats.updates++;
+    g->stats.submitted += n;
+    if (n == 0)
+        return GPMA_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    GPMA_TRY(ensure_batch(g, n));
+    GPMA_TRY(copy_in(g, g->bkeys[0], keys, n * sizeof(uint64_t), s));
+    GPMA_TRY(copy_in(g, g->bvals[0], values, n, s));
+    return update_device(g, n, s);
+}
+
+gpma_status gpma_bfs(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached, void *stream) {
+    if (!g || !levels) {
+        set_error("gpma_bfs: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    if (src >= g->row_num) {
+        set_error("gpma_bfs: start node %u out of range (row_num %u)", src, g->row_num);
+        return GPMA_ERR_INVALID;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    GPMA_TRY(bfs_run(g, src, s, reached));
+    GPMA_TRY(copy_any(levels, g->bfs_levels, sizeof(uint32_t) * g->row_num, s));
+    GPMA_CUDA(cudaStreamSynchronize(s));
+    return GPMA_OK;
+}
+
+gpma_status gpma_bfs_multi(gpma_graph *g, const uint32_t *srcs, uint32_t k, uint32_t *levels, uint64_t *reached,
+                           void *stream) {
+    if (!g || !srcs || !levels || k == 0 || k > 64) {
+        set_error("gpma_bfs_multi: bad arguments (k must be 1..64)");
+        return GPMA_ERR_INVALID;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    uint32_t hs[64];
+    GPMA_TRY(copy_any(hs, srcs, sizeof(uint32_t) * k, s));
+    GPMA_CUDA(cudaStreamSynchronize(s));
+    for (uint32_t i = 0; i < k; ++i) {
+        if (hs[i] >= g->row_num) {
+            set_error("gpma_bfs_multi: source %u out of range (row_num %u)", hs[i], g->row_num);
+            return GPMA_ERR_INVALID;
+        }
+    }
+    if (!g->msbfs_src)
+        GPMA_TRY(dev_alloc(&g->msbfs_src, 64));
+    GPMA_CUDA(cudaMemcpyAsync(g->msbfs_src, hs, sizeof(uint32_t) * k, cudaMemcpyHostToDevice, s));
+    GPMA_TRY(bfs_multi_run(g, g->msbfs_src, k, s));
+    GPMA_TRY(copy_any(levels, g->msbfs_levels, sizeof(uint32_t) * (uint64_t)k * g->row_num, s));
+    GPMA_CUDA(cudaStreamSynchronize(s));
+    if (reached) {
+        const unsigned long long *r = reinterpret_cast<const unsigned long long *>(g->h_bfs_ctl + 16);
+        for (uint32_t i = 0; i < k; ++i)
+            reached[i] = r[i];
+    }
+    return GPMA_OK;
+}
+
+gpma_status gpma_get_geometry(const gpma_graph *g, gpma_geometry *out) {
+    if (!g || !out) {
+        set_error("gpma_get_geometry: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    out->size = g->geo.size;
+    out->segment_length = g->geo.seg;
+    out->tree_height = g->geo.height;
+    out->row_num = g->row_num;
+    return GPMA_OK;
+}
+
+gpma_status gpma_get_thresholds(const gpma_graph *g, uint32_t *lower, uint32_t *upper) {
+    if (!g) {
+        set_error("gpma_get_thresholds: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    for (uint32_t i = 0; i <= g->geo.height; ++i) {
+        if (lower)
+            lower[i] = g->geo.lower[i];
+        if (upper)
+            upper[i] = g->geo.upper[i];
+    }
+    return GPMA_OK;
+}
+
+gpma_status gpma_export_layout(gpma_graph *g, uint64_t *keys, uint8_t *masked_values, uint32_t *row_offset,
+                               void *stream) {
+    if (!g) {
+        set_error("gpma_export_layout: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t size = g->geo.size;
+    if (keys)
+        GPMA_TRY(copy_any(keys, g->keys, sizeof(uint64_t) * size, s));
+    if (masked_values) {
+        uint8_t *tmp = nullptr;
+        GPMA_TRY(dev_alloc(&tmp, size));
+        mask_values_kernel<<<small_grid(size, g->sms), BLOCK, 0, s>>>(g->keys, g->values, tmp, size);
+        gpma_status st = copy_any(masked_values, tmp, size, s);
+        cudaStreamSynchronize(s);
+        dev_free(tmp);
+        GPMA_TRY(st);
+    }
+    if (row_offset)
+        GPMA_TRY(copy_any(row_offset, g->row_offset, sizeof(uint32_t) * ((uint64_t)g->row_num + 1), s));
+    GPMA_CUDA(cudaStreamSynchronize(s));
+    return GPMA_OK;
+}
+
+gpma_status gpma_export_compact(gpma_graph *g, uint64_t *keys, uint64_t capacity, uint64_t *count, void *stream) {
+    if (!g || !count) {
+        set_error("gpma_export_compact: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t size = g->geo.size;
+    const uint32_t chunks = (size + CHUNK - 1) / CHUNK;
+    uint32_t *off = nullptr;
+    GPMA_TRY(dev_alloc(&off, chunks + 1));
+    live_flags_kernel<<<small_grid((uint64_t)chunks * BLOCK, g->sms), BLOCK, 0, s>>>(g->keys, g->values, size, off);
+    scan_chunks_kernel<<<1, BLOCK, 0, s>>>(off, chunks, off + chunks);
+    uint32_t total = 0;
+    cudaMemcpyAsync(&total, off + chunks, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        dev_free(off);
+        return cuda_fail(e, "gpma_export_compact");
+    }
+    *count = total;
+    gpma_status st = GPMA_OK;
+    if (keys) {
+        if (capacity < total) {
+            set_error("gpma_export_compact: capacity %llu < %u live keys", (unsigned long long)capacity, total);
+            st = GPMA_ERR_INVALID;
+        } else {
+            uint64_t *tmp = nullptr;
+            st = dev_alloc(&tmp, total);
+            if (st == GPMA_OK) {
+                gather_live_kernel<<<small_grid((uint64_t)chunks * BLOCK, g->sms), BLOCK, 0, s>>>(g->keys, g->values,
+                                                                                                 size, off, tmp);
+                st = copy_any(keys, tmp, sizeof(uint64_t) * total, s);
+                cudaStreamSynchronize(s);
+                dev_free(tmp);
+            }
+        }
+    }
+    dev_free(off);
+    return st;
+}
+
+gpma_status gpma_device_arrays(gpma_graph *g, const uint64_t **keys, const uint8_t **values,
+                               const uint32_t **row_offset) {
+    if (!g) {
+        set_error("gpma_device_arrays: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    if (keys)
+        *keys = g->keys;
+    if (values)
+        *values = g->values;
+    if (row_offset)
+        *row_offset = g->row_offset;
+    return GPMA_OK;
+}
+
+gpma_status gpma_get_stats(const gpma_graph *g, gpma_stats *out) {
+    if (!g || !out) {
+        set_error("gpma_get_stats: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    *out = g->stats;
+    return GPMA_OK;
+}
+
+}  // extern "C"

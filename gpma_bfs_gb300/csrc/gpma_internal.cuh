@@ -1,0 +1,343 @@
+// gpma_internal.cuh - shared definitions of the GB300 GPMA+ library.
+//
+// Data layout in HBM (structure of arrays, one allocation each):
+//   keys[cap]    u64  slot keys, KEY_NONE in empty slots
+//   values[cap]  u8   1 = live (or any non-zero value), 0 = tombstone
+//   row_offset[row_num+1] u32, row_offset[r+1] = slot of row r's guard
+//   scratch keys/values [cap] for windows wider than one CTA and resizes
+// plus per-batch buffers sized by the largest batch seen.
+#pragma once
+
+#include "../../include/gpma_gb300.h"
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace gpma {
+
+// Reference constants (gpma.cuh:15-19, 40-43, 1003).
+constexpr uint64_t KEY_NONE = 0xFFFFFFFFFFFFFFFFull;
+constexpr uint64_t KEY_MAX = KEY_NONE - 1;
+constexpr uint32_t SIZE_NONE = 0xFFFFFFFFu;
+constexpr uint64_t COL_NONE = 0xFFFFFFFFull;
+constexpr double LOWER_LEAF = 0.08, LOWER_ROOT = 0.42, UPPER_LEAF = 0.92, UPPER_ROOT = 0.84;
+constexpr uint64_t SIGNIFICANT_INSERTS = 5000000ull;
+constexpr uint32_t MAX_SLOTS = 1u << 31;
+
+// Launch shapes.
+constexpr int BLOCK = 256;                 // threads of every persistent kernel
+constexpr uint32_t WARP_WINDOW_MAX = 256;  // widest window handled by one warp group
+constexpr uint32_t CTA_WINDOW_MAX = 2048;  // widest window handled by one CTA in shared memory
+constexpr uint32_t CHUNK = 2048;           // slots per CTA step for wider windows
+// Shared memory of the update kernel: three staging arrays (keys + values)
+// of CTA_WINDOW_MAX slots.
+constexpr size_t UPDATE_SMEM = 3ull * CTA_WINDOW_MAX * 9ull + 64;
+
+// Device error codes (DeviceStatus::err).
+enum : uint32_t {
+    DERR_NONE = 0,
+    DERR_BARRIER_TIMEOUT = 1,
+    DERR_LOOKBACK_TIMEOUT = 2,
+    DERR_BOUNDS = 3,
+    DERR_INVALID_KEY = 4,
+};
+
+// Bounded waits give up after this long (ns of %globaltimer).
+constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;
+
+struct GridBarrier {
+    unsigned int count;
+    unsigned int gen;
+};
+
+// Written by the update kernel, read back once per update.
+struct DeviceStatus {
+    uint32_t err;
+    uint32_t invalid_keys;  // keys whose column is the reserved 0xFFFFFFFF
+    uint32_t significant;   // >= SIGNIFICANT_INSERTS insertions: host rebuild
+    uint32_t inserts;       // insertions after delete/modify
+    uint32_t remaining;     // insertions still pending after the level loop
+    uint32_t rem_a;         // their start in the insertion arrays
+    uint32_t levels;        // level iterations executed
+    uint32_t pad;
+    unsigned long long accepted_windows;
+    unsigned long long accepted_slots;
+    GridBarrier bar;
+};
+
+// Sort plan for one batch: which digit passes are trivial and where each
+// pass reads from.
+struct SortPlan {
+    uint32_t trivial[8];
+    uint32_t in_sel[8];   // ping-pong buffer read by pass p
+    uint32_t final_sel;   // buffer holding the sorted batch
+    uint32_t pad[7];
+};
+
+struct Geometry {
+    uint32_t size = 0, seg = 0, height = 0;
+    std::vector<uint32_t> lower, upper;
+};
+
+// Recomputes the density thresholds exactly as recalculate_density
+// (gpma.cuh:147-168): same double expressions and evaluation order, then the
+// integer clamps against the previous level.
+void recalculate_density(Geometry &geo);
+uint32_t fls32(uint32_t x);
+
+}  // namespace gpma
+
+// Opaque handle of the C ABI.
+struct gpma_graph {
+    int device = 0;
+    int sms = 0;
+    uint32_t row_num = 0;
+    gpma::Geometry geo;
+    uint32_t cap = 0;                 // allocated slots of keys/values
+    uint64_t *keys = nullptr;
+    uint8_t *values = nullptr;
+    uint32_t *row_offset = nullptr;
+    uint32_t *d_lower = nullptr;      // 33 entries (height <= 31)
+    uint32_t *d_upper = nullptr;
+    uint32_t scratch_cap = 0;
+    uint64_t *skeys = nullptr;        // scratch for wide windows and resizes
+    uint8_t *svals = nullptr;
+    uint32_t *chunk_cnt = nullptr;    // scratch_cap / CHUNK + 1 entries
+    // per-batch buffers
+    uint64_t batch_cap = 0;
+    uint64_t *bkeys[2] = {nullptr, nullptr};
+    uint8_t *bvals[2] = {nullptr, nullptr};
+    uint32_t *leaf = nullptr;
+    uint64_t *ikeys = nullptr;
+    uint8_t *ivals = nullptr;
+    uint32_t *ileaf = nullptr;
+    uint32_t *wnode[2] = {nullptr, nullptr};
+    uint32_t *wa[2] = {nullptr, nullptr};
+    uint32_t *wb[2] = {nullptr, nullptr};
+    uint32_t *wflag = nullptr;
+    uint32_t *wlive = nullptr;
+    // sort scratch
+    uint32_t *sort_hist = nullptr;     // 8 * 256
+    uint32_t *sort_base = nullptr;     // 8 * 256
+    gpma::SortPlan *sort_plan = nullptr;
+    uint32_t *sort_tiles = nullptr;    // 8 tile counters
+    uint32_t *sort_status = nullptr;   // 8 * tiles * 256 look-back words
+    uint64_t sort_status_cap = 0;
+    // persistent-kernel scratch
+    uint32_t *cta_cnt = nullptr;       // 2 * grid
+    int update_grid = 0;
+    gpma::DeviceStatus *status = nullptr;
+    gpma::DeviceStatus *h_status = nullptr;  // pinned
+    // BFS state
+    uint32_t bfs_cap = 0;
+    uint32_t *bfs_visited = nullptr;   // row_num/32 + 1 words
+    uint32_t *bfs_queue[2] = {nullptr, nullptr};
+    uint32_t *bfs_levels = nullptr;
+    uint32_t *bfs_ctl = nullptr;       // counters + status
+    uint32_t *h_bfs_ctl = nullptr;     // pinned
+    int bfs_grid = 0;
+    uint64_t *msbfs_mask[3] = {nullptr, nullptr, nullptr};
+    uint32_t *msbfs_levels = nullptr;
+    uint64_t msbfs_levels_cap = 0;
+    uint32_t *msbfs_src = nullptr;
+    // staging for host pointers
+    void *h_stage = nullptr;
+    size_t h_stage_cap = 0;
+    gpma_stats stats{};
+};
+
+namespace gpma {
+
+// ---- host error handling -------------------------------------------------
+void set_error(const char *fmt, ...);
+gpma_status cuda_fail(cudaError_t e, const char *what);
+#define GPMA_CUDA(expr)                                                                                                \
+    do {                                                                                                               \
+        cudaError_t _e = (expr);                                                                                       \
+        if (_e != cudaSuccess)                                                                                         \
+            return ::gpma::cuda_fail(_e, #expr);                                                                       \
+    } while (0)
+#define GPMA_TRY(expr)                                                                                                 \
+    do {                                                                                                               \
+        gpma_status _s = (expr);                                                                                       \
+        if (_s != GPMA_OK)                                                                                             \
+            return _s;                                                                                                 \
+    } while (0)
+
+// true if p is device-accessible memory of the current device
+bool is_device_pointer(const void *p);
+// copies between host or device pointers on a stream (kind inferred)
+gpma_status copy_any(void *dst, const void *src, size_t bytes, cudaStream_t s);
+template <typename T>
+gpma_status dev_alloc(T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0)
+        count = 1;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        set_error("cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+        return GPMA_ERR_NOMEM;
+    }
+    return GPMA_OK;
+}
+template <typename T>
+void dev_free(T *&p) {
+    if (p)
+        cudaFree((void *)p);
+    p = nullptr;
+}
+
+// ---- host entry points implemented per translation unit -------------------
+gpma_status ensure_batch(gpma_graph *g, uint64_t n);
+gpma_status ensure_scratch(gpma_graph *g, uint32_t slots);
+gpma_status upload_geometry(gpma_graph *g, cudaStream_t s);
+gpma_status sort_batch(gpma_graph *g, uint64_t n, cudaStream_t s);
+gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s);
+gpma_status bfs_run(gpma_graph *g, uint32_t src, cudaStream_t s, uint64_t *reached);
+gpma_status bfs_multi_run(gpma_graph *g, const uint32_t *d_src, uint32_t k, cudaStream_t s);
+void free_bfs(gpma_graph *g);
+
+}  // namespace gpma
+
+// ---- device helpers --------------------------------------------------------
+#ifdef __CUDACC__
+namespace gpma {
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) { return *(const volatile uint32_t *)p; }
+
+// Sense-free generation barrier across the CTAs of a cooperative launch.
+// Every wait is bounded: after WAIT_LIMIT_NS the CTA records
+// DERR_BARRIER_TIMEOUT and returns false; CTAs that see an error stop waiting.
+__device__ __forceinline__ bool grid_barrier(GridBarrier *bar, uint32_t *err) {
+    __syncthreads();
+    __shared__ uint32_t s_ok;
+    if (threadIdx.x == 0) {
+        volatile unsigned int *vgen = &bar->gen;
+        unsigned int g0 = *vgen;
+        __threadfence();
+        unsigned int prev = atomicAdd(&bar->count, 1u);
+        if (prev == gridDim.x - 1) {
+            atomicExch(&bar->count, 0u);
+            __threadfence();
+            atomicAdd(&bar->gen, 1u);
+        } else {
+            uint64_t t0 = globaltimer_ns();
+            unsigned ns = 32;
+            while (*vgen == g0) {
+                if (ld_volatile(err) != 0)
+                    break;
+                __nanosleep(ns);
+                if (ns < 512)
+                    ns <<= 1;
+                if (globaltimer_ns() - t0 > WAIT_LIMIT_NS) {
+                    atomicCAS(err, 0u, DERR_BARRIER_TIMEOUT);
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        s_ok = ld_volatile(err) == 0;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Inclusive warp scan over `width` lanes (power of two <= 32).
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x, int width = 32) {
+    int lane = threadIdx.x & (width - 1);
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        if (d >= width)
+            break;
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, d, width);
+        if (lane >= d)
+            x += y;
+    }
+    return x;
+}
+
+// Exclusive scan over the CTA (blockDim.x == BLOCK); returns the exclusive
+// prefix and writes the CTA total. `tmp` holds BLOCK/32 + 1 words.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t *total, uint32_t *tmp) {
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t inc = warp_incl_scan(x);
+    if (lane == 31)
+        tmp[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t v = lane < BLOCK / 32 ? tmp[lane] : 0;
+        uint32_t vi = warp_incl_scan(v);
+        if (lane < BLOCK / 32)
+            tmp[lane] = vi - v;
+        if (lane == BLOCK / 32 - 1)
+            tmp[BLOCK / 32] = vi;
+    }
+    __syncthreads();
+    uint32_t res = tmp[warp] + inc - x;
+    *total = tmp[BLOCK / 32];
+    __syncthreads();
+    return res;
+}
+
+__device__ __forceinline__ uint32_t block_sum(uint32_t x, uint32_t *tmp) {
+    uint32_t total;
+    block_excl_scan(x, &total, tmp);
+    return total;
+}
+
+// Number of elements of sorted a[0..n) that are < key (lower) or <= key (upper).
+template <typename P>
+__device__ __forceinline__ uint32_t lower_bound_u64(P a, uint32_t n, uint64_t key) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] < key)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+template <typename P>
+__device__ __forceinline__ uint32_t upper_bound_u64(P a, uint32_t n, uint64_t key) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] <= key)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// First merged index of segment s when M elements are spread over F segments
+// (F a power of two, log2F its log): ceil(s*M/F). Element i of the merge
+// lands in segment floor(F*i/M) at lane (F*i mod M)/F (gpma.cuh:636-654);
+// inverting that, segment s holds elements [first(s), first(s+1)) packed from
+// lane 0.
+__device__ __forceinline__ uint64_t seg_first(uint64_t s, uint64_t M, uint32_t log2F) {
+    return (s * M + ((1ull << log2F) - 1)) >> log2F;
+}
+
+__device__ __forceinline__ bool is_guard(uint64_t k) { return (k & COL_NONE) == COL_NONE && k != KEY_NONE; }
+
+}  // namespace gpma
+#endif

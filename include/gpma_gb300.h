@@ -1,0 +1,164 @@
+/*
+ * gpma_gb300.h - C ABI of the GB300-native GPMA+ (dynamic graph in a GPU
+ * packed memory array) and its BFS.
+ *
+ * The reference (recolic/gpma_bfs) is a header-only C++/CUDA template library
+ * with no C ABI; these entry points are what its update/BFS path would export
+ * through an FFI. Types follow the reference: keys are uint64_t
+ * (src << 32 | dst, utils.cuh:11,19), values are one byte (utils.cuh:20;
+ * 1 = live/insert, 0 = delete/tombstone, gpma.cuh:18), slot indices and node
+ * ids are uint32_t (utils.cuh:21).
+ *
+ * Every call returns a status and never aborts. Pointer arguments documented
+ * as "host or device" may point to pageable host memory, pinned host memory
+ * or device memory of the graph's GPU; the library detects which. A graph
+ * handle is single-writer: concurrent calls on one handle must be serialised
+ * by the caller. `stream` is a cudaStream_t (NULL = legacy default stream).
+ */
+#ifndef GPMA_GB300_H
+#define GPMA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define GPMA_API __attribute__((visibility("default")))
+#else
+#define GPMA_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gpma_status {
+    GPMA_OK = 0,
+    GPMA_ERR_INVALID = 1,  /* bad argument: null pointer, out-of-range node, ... */
+    GPMA_ERR_CUDA = 2,     /* a CUDA runtime call failed (see gpma_last_error) */
+    GPMA_ERR_NOMEM = 3,    /* device or host allocation failed */
+    GPMA_ERR_CAPACITY = 4, /* the structure would exceed 2^31 slots (32-bit slot ids) */
+    GPMA_ERR_TIMEOUT = 5,  /* a bounded device-side wait gave up; the context stays usable */
+    GPMA_ERR_IO = 6,       /* file could not be read or written */
+    GPMA_ERR_DEVICE = 7    /* a device-side consistency check failed */
+} gpma_status;
+
+typedef struct gpma_graph gpma_graph;
+
+typedef struct gpma_geometry {
+    uint32_t size;           /* slots in the array (power of two), GPMA::keys.size() */
+    uint32_t segment_length; /* GPMA::segment_length (gpma.cuh:37) */
+    uint32_t tree_height;    /* GPMA::tree_height (gpma.cuh:38) */
+    uint32_t row_num;        /* GPMA::row_num (gpma.cuh:49) */
+} gpma_geometry;
+
+typedef struct gpma_stats {
+    uint64_t updates;          /* gpma_update calls */
+    uint64_t submitted;        /* keys submitted over all calls */
+    uint64_t last_inserts;     /* insertions left after delete/modify in the last call */
+    uint64_t levels_visited;   /* level-loop iterations executed */
+    uint64_t accepted_windows; /* windows redispatched */
+    uint64_t accepted_slots;   /* sum of the widths of redispatched windows */
+    uint64_t root_resizes;     /* root resizes (gpma.cuh:1034-1044) */
+    uint64_t root_drops;       /* root rebalances that failed their density check */
+    uint64_t significant;      /* bulk rebuilds for >= 5,000,000 insertions (gpma.cuh:1003) */
+} gpma_stats;
+
+/* ---- lifetime ------------------------------------------------------------
+ * Replaces the reference constructor GPMA<GPU>::GPMA(SIZE_TYPE row_num)
+ * (gpma.cuh:79-82): an empty structure plus one guard key (r<<32)|0xFFFFFFFF
+ * per row, inserted through the update path (gpma.cuh:70-78). Uses the
+ * current CUDA device. */
+GPMA_API gpma_status gpma_create(uint32_t row_num, void *stream, gpma_graph **out);
+
+/* Releases every device and host buffer of the graph (reference: ~GPMA). */
+GPMA_API gpma_status gpma_destroy(gpma_graph *g);
+
+/* ---- update --------------------------------------------------------------
+ * Replaces update_gpma<GPU>(GPMA&, NATIVE_VEC_KEY&, NATIVE_VEC_VALUE&)
+ * (gpma.cuh:27,968-1050). keys/values (host or device, n entries each) are a
+ * batch of edge keys; value 0 deletes the key, a non-zero value inserts it or
+ * overwrites the value of an existing key. Unlike the reference, the inputs
+ * are not modified. Returns after the structure is updated (the stream is
+ * synchronised). Keys that occur more than once in one batch with different
+ * values are applied in an unspecified order, as in the reference. */
+GPMA_API gpma_status gpma_update(gpma_graph *g, const uint64_t *keys, const uint8_t *values, uint64_t n, void *stream);
+
+/* ---- BFS -----------------------------------------------------------------
+ * Replaces gpma_bfs(const GPMA_multidev&, node_size, edge_size, start_node,
+ * SIZE_TYPE *results) (gpma_bfs.cuh:517-533) and the single-device
+ * gpma_bfs<DEV>(keys, values, row_offsets, node_size, edge_size, start_node,
+ * results) (gpma_bfs.cuh:511-515). levels (host or device, row_num entries)
+ * receives the BFS level of every node: 1 for src, L+1 for a neighbour of a
+ * level-L node, 0 for unreached. reached (optional, host) receives the
+ * number of non-zero levels. */
+GPMA_API gpma_status gpma_bfs(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached, void *stream);
+
+/* Multi-source BFS: k (1..64) independent searches in one traversal, one bit
+ * lane per source. levels (host or device) is [k][row_num]; reached
+ * (optional, host) has k entries. Each row equals gpma_bfs from that source.
+ * No reference counterpart (the reference BFS takes one source). */
+GPMA_API gpma_status gpma_bfs_multi(gpma_graph *g, const uint32_t *srcs, uint32_t k, uint32_t *levels, uint64_t *reached,
+                           void *stream);
+
+/* ---- views ---------------------------------------------------------------
+ * GPMA's public members (gpma.cuh:31-52) as read-only views. */
+GPMA_API gpma_status gpma_get_geometry(const gpma_graph *g, gpma_geometry *out);
+
+/* Density thresholds lower_element/upper_element (gpma.cuh:45-46,147-168):
+ * tree_height + 1 entries each (host arrays). */
+GPMA_API gpma_status gpma_get_thresholds(const gpma_graph *g, uint32_t *lower, uint32_t *upper);
+
+/* Copies the raw layout (GPMA::keys, values and row_offset). keys has `size`
+ * entries, masked_values has `size` entries (the slot's value, or 0 where the
+ * key is empty), row_offset has row_num + 1 entries. Any of them may be NULL;
+ * each may be host or device. */
+GPMA_API gpma_status gpma_export_layout(gpma_graph *g, uint64_t *keys, uint8_t *masked_values, uint32_t *row_offset,
+                               void *stream);
+
+/* Live keys (non-empty, value != 0) in slot order, i.e. the sorted key set
+ * including the row guards and the two KEY_MAX sentinels. With keys == NULL
+ * only *count is written. keys (host or device) holds `capacity` entries. */
+GPMA_API gpma_status gpma_export_compact(gpma_graph *g, uint64_t *keys, uint64_t capacity, uint64_t *count, void *stream);
+
+/* Raw device pointers to the live arrays (valid until the next update). */
+GPMA_API gpma_status gpma_device_arrays(gpma_graph *g, const uint64_t **keys, const uint8_t **values,
+                               const uint32_t **row_offset);
+
+GPMA_API gpma_status gpma_get_stats(const gpma_graph *g, gpma_stats *out);
+
+/* ---- diagnostics ---------------------------------------------------------- */
+GPMA_API const char *gpma_status_string(gpma_status s);
+/* Detail text of the last failing call on this host thread ("" if none). */
+GPMA_API const char *gpma_last_error(void);
+GPMA_API const char *gpma_version(void);
+
+/* ---- synthetic streams and the reference's text format ---------------------
+ * Host-only helpers (no GPU needed). The reference's demo loads "n m" then m
+ * "src dst" lines (gpma_bfs_demo.cu:6-30; dataset/prepare_dataset.sh:23-37). */
+
+/* R-MAT with quadrant probabilities a, b, c (d = 1-a-b-c): edge_factor << scale
+ * samples, then self-loops and duplicates removed and the list shuffled.
+ * src/dst hold `capacity` >= edge_factor << scale entries; *m_out = edges kept. */
+GPMA_API gpma_status gpma_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                          uint32_t *src, uint32_t *dst, uint64_t capacity, uint64_t *m_out);
+
+/* Chung-Lu power-law graph with exactly m distinct non-loop edges on n nodes:
+ * expected degrees ~ (i + i0)^(-1/(exponent-1)) with i0 set so the largest
+ * expected degree is max_degree; node 0 is the largest out-hub; the list is
+ * shuffled. */
+GPMA_API gpma_status gpma_gen_chung_lu(uint32_t n, uint64_t m, double exponent, uint32_t max_degree, uint64_t seed,
+                              uint32_t *src, uint32_t *dst);
+
+/* keys[i] = (src[i] << 32) + dst[i] (gpma_bfs_demo.cu:53). */
+GPMA_API gpma_status gpma_edges_to_keys(const uint32_t *src, const uint32_t *dst, uint64_t m, uint64_t *keys);
+
+/* Text edge list in the reference's format. With src == NULL or dst == NULL
+ * read only the header into *n_out and *m_out. */
+GPMA_API gpma_status gpma_read_edges_text(const char *path, uint32_t *n_out, uint64_t *m_out, uint32_t *src, uint32_t *dst,
+                                 uint64_t capacity);
+GPMA_API gpma_status gpma_write_edges_text(const char *path, uint32_t n, const uint32_t *src, const uint32_t *dst, uint64_t m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPMA_GB300_H */
