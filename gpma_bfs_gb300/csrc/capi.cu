@@ -75,8 +75,10 @@ void release(gpma_graph *g) {
         dev_free(g->wb[i]);
     }
     dev_free(g->leaf);
-    dev_free(g->ikeys);
-    dev_free(g->ivals);
+    for (int i = 0; i < 2; ++i) {
+        dev_free(g->ikeys[i]);
+        dev_free(g->ivals[i]);
+    }
     dev_free(g->ileaf);
     dev_free(g->wflag);
     dev_free(g->wlive);
@@ -247,7 +249,7 @@ gpma_status gpma_create(uint32_t row_num, void *stream, gpma_graph **out) {
         GPMA_TRY(ensure_batch(g, row_num));
         guard_keys_kernel<<<small_grid(row_num, g->sms), BLOCK, 0, s>>>(g->bkeys[0], g->bvals[0], row_num);
         GPMA_CUDA(cudaGetLastError());
-        return update_device(g, row_num, s);
+        return update_device(g, row_num, s, /*check_keys=*/false);  // the guards use the reserved column
     }();
     if (st != GPMA_OK) {
         release(g);

@@ -62,7 +62,9 @@ struct DeviceStatus {
     uint32_t remaining;     // insertions still pending after the level loop
     uint32_t rem_a;         // their start in the insertion arrays
     uint32_t levels;        // level iterations executed
+    uint32_t rem_buf;       // pending-insertion buffer holding them
     uint32_t pad;
+    uint32_t pad2;
     unsigned long long accepted_windows;
     unsigned long long accepted_slots;
     GridBarrier bar;
@@ -111,8 +113,8 @@ struct gpma_graph {
     uint64_t *bkeys[2] = {nullptr, nullptr};
     uint8_t *bvals[2] = {nullptr, nullptr};
     uint32_t *leaf = nullptr;
-    uint64_t *ikeys = nullptr;
-    uint8_t *ivals = nullptr;
+    uint64_t *ikeys[2] = {nullptr, nullptr};  // pending insertions, compacted per level (ping-pong)
+    uint8_t *ivals[2] = {nullptr, nullptr};
     uint32_t *ileaf = nullptr;
     uint32_t *wnode[2] = {nullptr, nullptr};
     uint32_t *wa[2] = {nullptr, nullptr};
@@ -127,7 +129,7 @@ struct gpma_graph {
     uint32_t *sort_status = nullptr;   // 8 * tiles * 256 look-back words
     uint64_t sort_status_cap = 0;
     // persistent-kernel scratch
-    uint32_t *cta_cnt = nullptr;       // 2 * grid
+    uint32_t *cta_cnt = nullptr;       // 4 * grid
     int update_grid = 0;
     gpma::DeviceStatus *status = nullptr;
     gpma::DeviceStatus *h_status = nullptr;  // pinned
@@ -196,8 +198,8 @@ void dev_free(T *&p) {
 gpma_status ensure_batch(gpma_graph *g, uint64_t n);
 gpma_status ensure_scratch(gpma_graph *g, uint32_t slots);
 gpma_status upload_geometry(gpma_graph *g, cudaStream_t s);
-gpma_status sort_batch(gpma_graph *g, uint64_t n, cudaStream_t s);
-gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s);
+gpma_status sort_batch(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys);
+gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys = true);
 gpma_status bfs_run(gpma_graph *g, uint32_t src, cudaStream_t s, uint64_t *reached);
 gpma_status bfs_multi_run(gpma_graph *g, const uint32_t *d_src, uint32_t k, cudaStream_t s);
 void free_bfs(gpma_graph *g);

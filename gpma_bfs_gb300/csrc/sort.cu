@@ -25,7 +25,7 @@ constexpr uint32_t FLAG_INC = 2u << 30;
 constexpr uint32_t VALUE_MASK = (1u << 30) - 1;
 
 __global__ void __launch_bounds__(BLOCK) hist_kernel(const uint64_t *__restrict__ keys, uint32_t n,
-                                                     uint32_t *__restrict__ hist, DeviceStatus *st) {
+                                                     uint32_t *__restrict__ hist, DeviceStatus *st, bool check_keys) {
     __shared__ uint32_t sh[8][256];
     for (int i = threadIdx.x; i < 8 * 256; i += BLOCK)
         (&sh[0][0])[i] = 0;
@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(BLOCK) hist_kernel(const uint64_t *__restrict_
         for (int p = 0; p < 8; ++p)
             atomicAdd(&sh[p][(k >> (8 * p)) & 255], 1u);
     }
-    if (__syncthreads_or(bad) && threadIdx.x == 0)
+    if (__syncthreads_or(bad) && check_keys && threadIdx.x == 0)
         atomicOr(&st->invalid_keys, 1u);
     for (int i = threadIdx.x; i < 8 * 256; i += BLOCK) {
         uint32_t c = (&sh[0][0])[i];
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(BLOCK) onesweep_kernel(int pass, uint64_t *k0,
 
 // Sorts bkeys[0]/bvals[0] (n entries); the result lands in
 // bkeys[plan.final_sel]. Also flags reserved-column keys in the status.
-gpma_status sort_batch(gpma_graph *g, uint64_t n, cudaStream_t s) {
+gpma_status sort_batch(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys) {
     if (n == 0)
         return GPMA_OK;
     const uint32_t tiles = (uint32_t)((n + SORT_TILE - 1) / SORT_TILE);
@@ -216,7 +216,7 @@ gpma_status sort_batch(gpma_graph *g, uint64_t n, cudaStream_t s) {
     GPMA_CUDA(cudaMemsetAsync(g->sort_tiles, 0, 8 * sizeof(uint32_t), s));
     GPMA_CUDA(cudaMemsetAsync(g->sort_status, 0, need * sizeof(uint32_t), s));
     int hist_grid = (int)std::min<uint64_t>((n + BLOCK * 8 - 1) / (BLOCK * 8), (uint64_t)g->sms * 4);
-    hist_kernel<<<hist_grid, BLOCK, 0, s>>>(g->bkeys[0], (uint32_t)n, g->sort_hist, g->status);
+    hist_kernel<<<hist_grid, BLOCK, 0, s>>>(g->bkeys[0], (uint32_t)n, g->sort_hist, g->status, check_keys);
     plan_kernel<<<1, BLOCK, 0, s>>>(g->sort_hist, (uint32_t)n, g->sort_base, g->sort_plan);
     for (int p = 0; p < 8; ++p)
         onesweep_kernel<<<tiles, BLOCK, 0, s>>>(p, g->bkeys[0], g->bvals[0], g->bkeys[1], g->bvals[1], (uint32_t)n,

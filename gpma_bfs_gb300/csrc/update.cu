@@ -71,8 +71,8 @@ struct UpdateArgs {
     const SortPlan *plan;
     uint32_t n;
     uint32_t *leaf;
-    uint64_t *ikeys;
-    uint8_t *ivals;
+    uint64_t *ikeys[2];
+    uint8_t *ivals[2];
     uint32_t *ileaf;
     uint32_t *wnode[2];
     uint32_t *wa[2];
@@ -200,7 +200,8 @@ __device__ void redispatch_chunk(uint64_t *keys, uint8_t *vals, uint32_t *row_of
 // ---- windows up to WARP_WINDOW_MAX slots: one group of min(W,32) lanes ------
 template <uint32_t W>
 __device__ void warp_windows(const UpdateArgs &A, const uint32_t *wn, const uint32_t *wa, const uint32_t *wb,
-                             uint32_t nw, uint32_t lo, uint32_t hi, unsigned char *smem, unsigned long long &acc) {
+                             uint32_t nw, uint32_t lo, uint32_t hi, const uint64_t *pk, const uint8_t *pv,
+                             unsigned char *smem, unsigned long long &acc) {
     constexpr uint32_t G = W < 32 ? W : 32;
     constexpr uint32_t GPW = 32 / G;
     constexpr uint32_t K = W / G;
@@ -258,8 +259,8 @@ __device__ void warp_windows(const UpdateArgs &A, const uint32_t *wn, const uint
         __syncwarp();
         if (accept) {
             for (uint32_t j = gl; j < p; j += G) {
-                sk[j] = A.ikeys[a + j];
-                sv[j] = A.ivals[a + j];
+                sk[j] = pk[a + j];
+                sv[j] = pv[a + j];
             }
         }
         __syncwarp();
@@ -308,8 +309,8 @@ __device__ void warp_windows(const UpdateArgs &A, const uint32_t *wn, const uint
 // ---- windows of 512..CTA_WINDOW_MAX slots: one CTA each ---------------------
 template <uint32_t W>
 __device__ void cta_windows(const UpdateArgs &A, const uint32_t *wn, const uint32_t *wa, const uint32_t *wb,
-                            uint32_t nw, uint32_t lo, uint32_t hi, unsigned char *smem, uint32_t *tmp,
-                            unsigned long long &acc) {
+                            uint32_t nw, uint32_t lo, uint32_t hi, const uint64_t *pk, const uint8_t *pv,
+                            unsigned char *smem, uint32_t *tmp, unsigned long long &acc) {
     constexpr uint32_t K = W / BLOCK;
     uint64_t *sk = reinterpret_cast<uint64_t *>(smem);
     uint64_t *ck = sk + W;
@@ -355,8 +356,8 @@ __device__ void cta_windows(const UpdateArgs &A, const uint32_t *wn, const uint3
         __syncthreads();
         if (accept) {
             for (uint32_t j = tid; j < p; j += BLOCK) {
-                sk[j] = A.ikeys[a + j];
-                sv[j] = A.ivals[a + j];
+                sk[j] = pk[a + j];
+                sv[j] = pv[a + j];
             }
         }
         __syncthreads();
@@ -404,8 +405,8 @@ __device__ void cta_windows(const UpdateArgs &A, const uint32_t *wn, const uint3
 
 // ---- windows wider than one CTA: the whole grid, chunk by chunk -------------
 __device__ bool grid_windows(const UpdateArgs &A, const uint32_t *wn, const uint32_t *wa, const uint32_t *wb,
-                             uint32_t nw, uint32_t W, uint32_t lo, uint32_t hi, unsigned char *smem, uint32_t *tmp,
-                             unsigned long long &acc) {
+                             uint32_t nw, uint32_t W, uint32_t lo, uint32_t hi, const uint64_t *pk,
+                             const uint8_t *pv, unsigned char *smem, uint32_t *tmp, unsigned long long &acc) {
     const uint32_t cpw = W / CHUNK;
     const uint32_t total = nw * cpw;
     constexpr uint32_t K = CHUNK / BLOCK;
@@ -485,7 +486,7 @@ __device__ bool grid_windows(const UpdateArgs &A, const uint32_t *wn, const uint
             continue;
         uint32_t node = wn[w], a = wa[w];
         redispatch_chunk(A.keys, A.vals, A.row_offset, A.row_num, node, A.log2seg, log2F, k * CHUNK, CHUNK,
-                         A.skeys + node, A.svals + node, A.wlive[w], A.ikeys + a, A.ivals + a, wb[w] - a, KEY_NONE,
+                         A.skeys + node, A.svals + node, A.wlive[w], pk + a, pv + a, wb[w] - a, KEY_NONE,
                          mk, mv);
     }
     return true;
@@ -494,11 +495,12 @@ __device__ bool grid_windows(const UpdateArgs &A, const uint32_t *wn, const uint
 template <uint32_t W>
 __device__ __forceinline__ void small_dispatch(const UpdateArgs &A, const uint32_t *wn, const uint32_t *wa,
                                                const uint32_t *wb, uint32_t nw, uint32_t lo, uint32_t hi,
-                                               unsigned char *smem, uint32_t *tmp, unsigned long long &acc) {
+                                               const uint64_t *pk, const uint8_t *pv, unsigned char *smem,
+                                               uint32_t *tmp, unsigned long long &acc) {
     if constexpr (W <= WARP_WINDOW_MAX)
-        warp_windows<W>(A, wn, wa, wb, nw, lo, hi, smem, acc);
+        warp_windows<W>(A, wn, wa, wb, nw, lo, hi, pk, pv, smem, acc);
     else
-        cta_windows<W>(A, wn, wa, wb, nw, lo, hi, smem, tmp, acc);
+        cta_windows<W>(A, wn, wa, wb, nw, lo, hi, pk, pv, smem, tmp, acc);
 }
 
 __global__ void __launch_bounds__(BLOCK) update_kernel(UpdateArgs A) {
@@ -513,6 +515,7 @@ __global__ void __launch_bounds__(BLOCK) update_kernel(UpdateArgs A) {
     const uint32_t G = gridDim.x;
     uint32_t scan_id = 0;
 #define CNT(id) ((id) ? A.cta_cnt + G : A.cta_cnt)
+#define CNTI(id) ((id) ? A.cta_cnt + 3 * G : A.cta_cnt + 2 * G)
     unsigned long long acc = 0, acc_slots = 0;
 
     // P1: locate every update, applying deletes / modifies in place.
@@ -542,8 +545,8 @@ __global__ void __launch_bounds__(BLOCK) update_kernel(UpdateArgs A) {
         uint32_t tot;
         uint32_t ex = block_excl_scan(f, &tot, tmp);
         if (f) {
-            A.ikeys[base + ex] = bk[i];
-            A.ivals[base + ex] = bv[i];
+            A.ikeys[0][base + ex] = bk[i];
+            A.ivals[0][base + ex] = bv[i];
             A.ileaf[base + ex] = A.leaf[i];
         }
         base += tot;
@@ -594,72 +597,109 @@ __global__ void __launch_bounds__(BLOCK) update_kernel(UpdateArgs A) {
     if (!grid_barrier(&st->bar, &st->err))
         return;
 
-    // Level loop.
+    // Level loop. Windows and their pending insertions live in ping-pong
+    // buffers selected by `cur`; each window's insertions are the contiguous
+    // range [wa, wb) of the current insertion buffer.
     uint32_t cur = 0, level = 0;
+    __shared__ uint32_t s_nb[BLOCK], s_src[BLOCK], s_cnt[BLOCK];
     for (; level <= A.height && nw > 0; ++level) {
         const uint32_t W = A.seg << level;
         const uint32_t lob = A.lower[level], hib = A.upper[level];
         const uint32_t *wn = cur ? A.wnode[1] : A.wnode[0];
         const uint32_t *wa = cur ? A.wa[1] : A.wa[0];
         const uint32_t *wb = cur ? A.wb[1] : A.wb[0];
+        const uint64_t *pk = cur ? A.ikeys[1] : A.ikeys[0];
+        const uint8_t *pv = cur ? A.ivals[1] : A.ivals[0];
         const unsigned long long before = acc;
         switch (W) {
-        case 2: small_dispatch<2>(A, wn, wa, wb, nw, lob, hib, smem, tmp, acc); break;
-        case 4: small_dispatch<4>(A, wn, wa, wb, nw, lob, hib, smem, tmp, acc); break;
-        case 8: small_dispatch<8>(A, wn, wa, wb, nw, lob, hib, smem, tmp, acc); break;
-        case 16: small_dispatch<16>(A, wn, wa, wb, nw, lob, hib, smem, tmp, acc); break;
-        case 32: small_dispatch<32>(A, wn, wa, wb, nw, lob, hib, smem, tmp, acc); break;
-        case 64: small_dispatch<64>(A, wn, wa, wb, nw, lob, hib, smem, tmp, acc); break;
-        case 128: small_dispatch<128>(A, wn, wa, wb, nw, lob, hib, smem, tmp, acc); break;
-        case 256: small_dispatch<256>(A, wn, wa, wb, nw, lob, hib, smem, tmp, acc); break;
-        case 512: small_dispatch<512>(A, wn, wa, wb, nw, lob, hib, smem, tmp, acc); break;
-        case 1024: small_dispatch<1024>(A, wn, wa, wb, nw, lob, hib, smem, tmp, acc); break;
-        case 2048: small_dispatch<2048>(A, wn, wa, wb, nw, lob, hib, smem, tmp, acc); break;
+        case 2: small_dispatch<2>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
+        case 4: small_dispatch<4>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
+        case 8: small_dispatch<8>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
+        case 16: small_dispatch<16>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
+        case 32: small_dispatch<32>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
+        case 64: small_dispatch<64>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
+        case 128: small_dispatch<128>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
+        case 256: small_dispatch<256>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
+        case 512: small_dispatch<512>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
+        case 1024: small_dispatch<1024>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
+        case 2048: small_dispatch<2048>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
         default:
-            if (!grid_windows(A, wn, wa, wb, nw, W, lob, hib, smem, tmp, acc))
+            if (!grid_windows(A, wn, wa, wb, nw, W, lob, hib, pk, pv, smem, tmp, acc))
                 return;
         }
         acc_slots += (acc - before) * (unsigned long long)W;
         if (!grid_barrier(&st->bar, &st->err))
             return;
-        // Next level: rejected windows, siblings merged into their parent.
+        // Next level. Rejected windows keep their insertions, which are
+        // compacted into the other buffer (new offsets from one scan over the
+        // windows, as compact_insertions does over insertions, gpma.cuh:1022);
+        // a rejected right sibling joins its rejected left sibling in the
+        // parent window (up_level, gpma.cuh:881-889 + regrouping).
         const uint32_t nxt = cur ^ 1;
+        uint32_t *nwn = nxt ? A.wnode[1] : A.wnode[0];
+        uint32_t *nwa = nxt ? A.wa[1] : A.wa[0];
+        uint32_t *nwb = nxt ? A.wb[1] : A.wb[0];
+        uint64_t *nk = nxt ? A.ikeys[1] : A.ikeys[0];
+        uint8_t *nv = nxt ? A.ivals[1] : A.ivals[0];
         cta_range(nw, lo, hi);
         {
-            uint32_t cl = 0;
+            uint32_t ch = 0, ci = 0;
             for (uint32_t w = lo + threadIdx.x; w < hi; w += BLOCK) {
                 if (A.wflag[w])
                     continue;
+                ci += wb[w] - wa[w];
                 uint32_t par = wn[w] & ~W;
                 bool merged = w > 0 && !A.wflag[w - 1] && (wn[w - 1] & ~W) == par;
-                cl += merged ? 0u : 1u;
+                ch += merged ? 0u : 1u;
             }
-            uint32_t t = block_sum(cl, tmp);
-            if (threadIdx.x == 0)
-                CNT(scan_id)[blockIdx.x] = t;
+            uint32_t th = block_sum(ch, tmp);
+            uint32_t ti = block_sum(ci, tmp);
+            if (threadIdx.x == 0) {
+                CNT(scan_id)[blockIdx.x] = th;
+                CNTI(scan_id)[blockIdx.x] = ti;
+            }
         }
         if (!grid_barrier(&st->bar, &st->err))
             return;
-        uint32_t nw_next;
+        uint32_t nw_next, base_i, total_i;
         cta_prefix(CNT(scan_id), base, nw_next, tmp);
+        cta_prefix(CNTI(scan_id), base_i, total_i, tmp);
         for (uint32_t w0 = lo; w0 < hi; w0 += BLOCK) {
-            uint32_t w = w0 + threadIdx.x;
+            const uint32_t w = w0 + threadIdx.x;
+            const bool rej = w < hi && !A.wflag[w];
+            const uint32_t c = rej ? wb[w] - wa[w] : 0u;
+            uint32_t tot_i;
+            const uint32_t nb = base_i + block_excl_scan(c, &tot_i, tmp);
             uint32_t head = 0, par = 0;
-            if (w < hi && !A.wflag[w]) {
+            if (rej) {
                 par = wn[w] & ~W;
                 bool merged = w > 0 && !A.wflag[w - 1] && (wn[w - 1] & ~W) == par;
                 head = merged ? 0u : 1u;
             }
-            uint32_t tot;
-            uint32_t ex = block_excl_scan(head, &tot, tmp);
+            uint32_t tot_h;
+            const uint32_t ex = block_excl_scan(head, &tot_h, tmp);
             if (head) {
-                uint32_t e = base + ex;
-                bool right = w + 1 < nw && !A.wflag[w + 1] && (wn[w + 1] & ~W) == par;
-                (nxt ? A.wnode[1] : A.wnode[0])[e] = par;
-                (nxt ? A.wa[1] : A.wa[0])[e] = wa[w];
-                (nxt ? A.wb[1] : A.wb[0])[e] = right ? wb[w + 1] : wb[w];
+                const uint32_t e = base + ex;
+                const bool right = w + 1 < nw && !A.wflag[w + 1] && (wn[w + 1] & ~W) == par;
+                nwn[e] = par;
+                nwa[e] = nb;
+                nwb[e] = nb + c + (right ? wb[w + 1] - wa[w + 1] : 0u);
             }
-            base += tot;
+            s_nb[threadIdx.x] = nb;
+            s_src[threadIdx.x] = rej ? wa[w] : 0u;
+            s_cnt[threadIdx.x] = c;
+            __syncthreads();
+            // copy the kept insertions, one warp per window of this tile
+            for (uint32_t t = threadIdx.x >> 5; t < BLOCK; t += BLOCK / 32) {
+                const uint32_t cc = s_cnt[t], from = s_src[t], to = s_nb[t];
+                for (uint32_t e = threadIdx.x & 31; e < cc; e += 32) {
+                    nk[to + e] = pk[from + e];
+                    nv[to + e] = pv[from + e];
+                }
+            }
+            __syncthreads();
+            base += tot_h;
+            base_i += tot_i;
         }
         scan_id ^= 1;
         if (!grid_barrier(&st->bar, &st->err))
@@ -694,8 +734,10 @@ __global__ void __launch_bounds__(BLOCK) update_kernel(UpdateArgs A) {
             const uint32_t ra = (cur ? A.wa[1] : A.wa[0])[0], rb = (cur ? A.wb[1] : A.wb[0])[0];
             st->remaining = rb - ra;
             st->rem_a = ra;
+            st->rem_buf = cur;
         }
 #undef CNT
+#undef CNTI
     }
 }
 
@@ -793,7 +835,10 @@ int grid_for(uint64_t work, int sms, int per_sm) {
 }
 
 // resize_gpma + (root rebalance | significant_insert) on the device.
-gpma_status root_rebuild(gpma_graph *g, bool significant, uint32_t pend_a, uint32_t pend_n, cudaStream_t s) {
+gpma_status root_rebuild(gpma_graph *g, bool significant, uint32_t pend_buf, uint32_t pend_a, uint32_t pend_n,
+                         cudaStream_t s) {
+    const uint64_t *pend_k = g->ikeys[pend_buf] + pend_a;
+    const uint8_t *pend_v = g->ivals[pend_buf] + pend_a;
     const uint32_t size = g->geo.size;
     const uint32_t chunks = (size + CHUNK - 1) / CHUNK;
     // 1. stable compaction of the live slots (resize_gpma, gpma.cuh:909-915)
@@ -848,7 +893,7 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, uint32_t pend_a, uint3
     if (significant) {
         // significant_insert: everything redispatched, gaps are key 0 / value 0
         rebuild_kernel<<<rgrid, BLOCK, rsmem, s>>>(g->keys, g->values, g->row_offset, g->row_num, geo.size, log2seg,
-                                                    log2F, g->skeys, g->svals, live, g->ikeys, g->ivals, pend_n, 0ull);
+                                                    log2F, g->skeys, g->svals, live, pend_k, pend_v, pend_n, 0ull);
         g->stats.significant++;
         g->stats.accepted_windows++;
         g->stats.accepted_slots += geo.size;
@@ -856,8 +901,8 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, uint32_t pend_a, uint3
         const uint32_t h = geo.height;
         if (geo.lower[h] <= merge && merge <= geo.upper[h]) {
             rebuild_kernel<<<rgrid, BLOCK, rsmem, s>>>(g->keys, g->values, g->row_offset, g->row_num, geo.size,
-                                                        log2seg, log2F, g->skeys, g->svals, live, g->ikeys + pend_a,
-                                                        g->ivals + pend_a, pend_n, KEY_NONE);
+                                                        log2seg, log2F, g->skeys, g->svals, live, pend_k, pend_v,
+                                                        pend_n, KEY_NONE);
             g->stats.accepted_windows++;
             g->stats.accepted_slots += geo.size;
         } else {
@@ -918,8 +963,10 @@ gpma_status ensure_batch(gpma_graph *g, uint64_t n) {
         dev_free(g->wb[i]);
     }
     dev_free(g->leaf);
-    dev_free(g->ikeys);
-    dev_free(g->ivals);
+    for (int i = 0; i < 2; ++i) {
+        dev_free(g->ikeys[i]);
+        dev_free(g->ivals[i]);
+    }
     dev_free(g->ileaf);
     dev_free(g->wflag);
     dev_free(g->wlive);
@@ -932,8 +979,10 @@ gpma_status ensure_batch(gpma_graph *g, uint64_t n) {
         GPMA_TRY(dev_alloc(&g->wb[i], cap));
     }
     GPMA_TRY(dev_alloc(&g->leaf, cap));
-    GPMA_TRY(dev_alloc(&g->ikeys, cap));
-    GPMA_TRY(dev_alloc(&g->ivals, cap));
+    for (int i = 0; i < 2; ++i) {
+        GPMA_TRY(dev_alloc(&g->ikeys[i], cap));
+        GPMA_TRY(dev_alloc(&g->ivals[i], cap));
+    }
     GPMA_TRY(dev_alloc(&g->ileaf, cap));
     GPMA_TRY(dev_alloc(&g->wflag, cap));
     GPMA_TRY(dev_alloc(&g->wlive, cap));
@@ -942,7 +991,7 @@ gpma_status ensure_batch(gpma_graph *g, uint64_t n) {
 }
 
 // Runs the update of the n-key batch already staged in bkeys[0]/bvals[0].
-gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s) {
+gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys) {
     if (g->update_grid == 0) {
         GPMA_CUDA(cudaFuncSetAttribute(update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)UPDATE_SMEM));
         GPMA_CUDA(cudaFuncSetAttribute(rebuild_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(CHUNK * 9)));
@@ -953,10 +1002,10 @@ gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s) {
             return GPMA_ERR_CUDA;
         }
         g->update_grid = g->sms * std::min(per_sm, 4);
-        GPMA_TRY(dev_alloc(&g->cta_cnt, 2ull * g->update_grid));
+        GPMA_TRY(dev_alloc(&g->cta_cnt, 4ull * g->update_grid));
     }
     GPMA_CUDA(cudaMemsetAsync(g->status, 0, sizeof(DeviceStatus), s));
-    GPMA_TRY(sort_batch(g, n, s));
+    GPMA_TRY(sort_batch(g, n, s, check_keys));
     UpdateArgs A;
     A.keys = g->keys;
     A.vals = g->values;
@@ -975,8 +1024,10 @@ gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s) {
     A.plan = g->sort_plan;
     A.n = (uint32_t)n;
     A.leaf = g->leaf;
-    A.ikeys = g->ikeys;
-    A.ivals = g->ivals;
+    for (int i = 0; i < 2; ++i) {
+        A.ikeys[i] = g->ikeys[i];
+        A.ivals[i] = g->ivals[i];
+    }
     A.ileaf = g->ileaf;
     for (int i = 0; i < 2; ++i) {
         A.wnode[i] = g->wnode[i];
@@ -1009,9 +1060,9 @@ gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s) {
     g->stats.accepted_slots += h.accepted_slots;
     g->stats.last_inserts = h.inserts;
     if (h.significant)
-        return root_rebuild(g, true, 0, h.inserts, s);
+        return root_rebuild(g, true, 0, 0, h.inserts, s);
     if (h.remaining > 0)
-        return root_rebuild(g, false, h.rem_a, h.remaining, s);
+        return root_rebuild(g, false, h.rem_buf, h.rem_a, h.remaining, s);
     return GPMA_OK;
 }
 

@@ -1,0 +1,120 @@
+"""C ABI boundary and host logic (no GPU needed, no compute calls on a GPU)."""
+import ctypes
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        for m in re.finditer(r"GPMA_API\s+[\w\s\*]+?\b(gpma_\w+)\s*\(", h.read_text()):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for core in ("gpma_create", "gpma_destroy", "gpma_update", "gpma_bfs", "gpma_bfs_multi",
+                 "gpma_export_layout", "gpma_get_geometry"):
+        assert core in names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(ROOT / "gpma_bfs_gb300" / "libgpma_gb300.so")],
+                         capture_output=True, text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [n for n in declared_symbols() if n not in exported]
+    assert not missing, f"declared but not exported: {missing}"
+    for n in declared_symbols():
+        assert getattr(built_lib, n) is not None
+
+
+def test_status_strings(built_lib):
+    built_lib.gpma_status_string.restype = ctypes.c_char_p
+    assert built_lib.gpma_status_string(0) == b"ok"
+    assert built_lib.gpma_status_string(1) == b"invalid argument"
+    assert b"sm_103a" in built_lib.gpma_version()
+
+
+def test_null_arguments_rejected_without_gpu(built_lib):
+    import gpma_bfs_gb300 as G
+
+    assert built_lib.gpma_create(5, None, None) == 1
+    assert built_lib.gpma_update(None, None, None, 0, None) == 1
+    assert built_lib.gpma_bfs(None, 0, None, None, None) == 1
+    assert b"null" in built_lib.gpma_last_error() or b"NULL" in built_lib.gpma_last_error()
+    with pytest.raises(ValueError):
+        G.update_gpma(object(), np.zeros(3, np.uint64), np.zeros(2, np.uint8))
+
+
+def test_rmat_generator_deterministic(built_lib):
+    import gpma_bfs_gb300 as G
+
+    s1, d1 = G.gen_rmat(12, 8, seed=9)
+    s2, d2 = G.gen_rmat(12, 8, seed=9)
+    assert np.array_equal(s1, s2) and np.array_equal(d1, d2)
+    k = G.edges_to_keys(s1, d1)
+    assert len(np.unique(k)) == len(k), "duplicates survived"
+    assert not np.any(s1 == d1), "self-loops survived"
+    assert s1.max() < 4096 and d1.max() < 4096
+    # R-MAT skew: quadrant a dominates, so low ids are heavy
+    assert np.mean(s1 < 2048) > 0.7
+    s3, _ = G.gen_rmat(12, 8, seed=10)
+    assert not np.array_equal(s1, s3)
+
+
+def test_chung_lu_generator(built_lib):
+    import gpma_bfs_gb300 as G
+
+    n, m = 20000, 150000
+    s, d = G.gen_chung_lu(n, m, 2.3, 900, seed=4)
+    assert len(s) == m
+    k = G.edges_to_keys(s, d)
+    assert len(np.unique(k)) == m and not np.any(s == d)
+    deg = np.bincount(s, minlength=n)
+    assert deg.argmax() == 0, "node 0 is the top out-hub"
+    assert 400 < deg[0] <= 1100, deg[0]
+    assert np.median(deg) < m / n, "power law: median below mean"
+
+
+def test_text_format_round_trip(tmp_path, built_lib):
+    import gpma_bfs_gb300 as G
+
+    s, d = G.gen_rmat(8, 4, seed=2)
+    p = tmp_path / "g.txt"
+    G.write_edges_text(p, 256, s, d)
+    first = p.read_text().splitlines()[0]
+    assert first == f"256 {len(s)}"
+    n, s2, d2 = G.read_edges_text(p)
+    assert n == 256 and np.array_equal(s, s2) and np.array_equal(d, d2)
+
+
+def test_sliding_window_schedule(built_lib):
+    from gpma_bfs_gb300.workloads import sliding_window
+
+    s = np.arange(1000, dtype=np.uint32)
+    d = s + 1
+    sw = sliding_window(s, d, num_slide=100)
+    assert sw.half == 500 and sw.step == 5
+    k, v = sw.slide_keys[3], sw.slide_values[3]
+    # inserts first (next edges), then deletes (oldest edges): gpma_bfs_demo.cu:85-104
+    assert list(k[:5] >> np.uint64(32)) == [515, 516, 517, 518, 519]
+    assert list(k[5:] >> np.uint64(32)) == [15, 16, 17, 18, 19]
+    assert list(v) == [1] * 5 + [0] * 5
+
+
+def test_oracle_thresholds_follow_reference_formula():
+    """recalculate_density (gpma.cuh:147-168) on a known geometry."""
+    from oracle.oracle import OracleGPMA
+
+    o = OracleGPMA(0)
+    lo, hi = o.thresholds()
+    # initial structure: 4 slots, segment 2, height 1
+    assert o.geometry() == {"size": 4, "segment_length": 2, "tree_height": 1, "row_num": 0}
+    assert list(lo) == [1, 2] and list(hi) == [1, 2]
