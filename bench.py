@@ -1,0 +1,386 @@
+#!/usr/bin/env python
+"""Sliding-window GPMA+ benchmark on GB300 (edge updates/s, BFS GTEPS).
+
+Workload (the reference demo, gpma_bfs_demo.cu:32-116, on its social-graph
+configuration): a seeded Chung-Lu graph with 1,632,803 nodes and 30,622,564
+directed edges (power law, exponent 2.3, largest expected degree 9,000; a
+synthetic stand-in for the unavailable pokec file) is shuffled, its first
+half loaded, a BFS run from node 0, then slide steps each insert the next
+153,112 edges and delete the oldest 153,112 in one batch; a BFS from node 0
+follows. One step = one slide update. The schedule wraps around the edge
+list when warm-up + timed steps exceed its 100 slides.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpma|reference]
+
+value  - updates/s over K steps with batches resident in HBM, device time
+         from CUDA events on the launching stream; L2 flushed before every
+         step (outside the timed span).
+e2e    - the same through the C ABI from pinned host buffers: the batch
+         upload and the read-back of the update status are inside the span.
+--impl reference - the reference algorithm on the host cores (the C
+         restatement in oracle/, OpenMP on all cores), same workload/metric.
+Several GPUs run independent replicas (the path does not shard); value sums
+the ranks' updates over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "edge updates/s + BFS GTEPS on 1 GB300, batched vs plain GPMA; p99 query latency"
+UNIT = "edge updates/s"
+GRAPH = "social"
+DATA = ("synthetic: seeded Chung-Lu power-law graph with pokec's shape (1,632,803 nodes, 30,622,564 edges, "
+        "exponent 2.3, max expected degree 9,000, seed 2), shuffled")
+L2_FLUSH_BYTES = 256 << 20
+
+
+def workload_config(n, m, step):
+    return {"workload": f"social sliding window: {n:,} nodes, {m:,} edges, half-load then slides of "
+                        f"{step:,} inserts + {step:,} deletes",
+            "graph": GRAPH, "nodes": n, "edges": m, "batch": 2 * step, "bfs_source": 0,
+            "l2": "flushed (256 MiB write) before every timed step", "parallelism": "replicas"}
+
+
+def schedule(keys, num_slide=100):
+    """Slide i: insert keys[half + i*step ..], delete keys[i*step ..] (cyclic)."""
+    m = len(keys)
+    half = m // 2
+    step = half // num_slide
+
+    def slide(i):
+        ins_idx = (half + i * step + np.arange(step)) % m
+        del_idx = (i * step + np.arange(step)) % m
+        k = np.concatenate([keys[ins_idx], keys[del_idx]])
+        v = np.concatenate([np.ones(step, np.uint8), np.zeros(step, np.uint8)])
+        return k, v
+
+    return half, step, slide
+
+
+def peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        if d.get("hbm_gbs"):
+            return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+def profiled_traffic(kernel: str):
+    """Per-launch DRAM bytes of `kernel` from a committed ncu summary, if any."""
+    f = ROOT / "profiles" / f"{kernel}.social.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch:"):
+            return float(line.split(":", 1)[1].split()[0])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+        else:
+            self.lines = []
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() in ("active", "0x1", "1"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def live_out_degree_sum(g, levels):
+    """Edges traversed by a BFS: live out-edges of the reached nodes."""
+    keys, vals, ro = g.export_layout()
+    valid = ((keys & np.uint64(0xFFFFFFFF)) != np.uint64(0xFFFFFFFF)) & (vals != 0)
+    csum = np.concatenate([[0], np.cumsum(valid, dtype=np.int64)])
+    ro = ro.astype(np.int64)
+    per_row = csum[ro[1:]] - csum[ro[:-1]]
+    return int(per_row[levels != 0].sum())
+
+
+def run_gpu(args):
+    import torch
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import gpma_bfs_gb300 as G
+    from gpma_bfs_gb300.workloads import make_graph
+
+    t0 = time.time()
+    n, src, dst = make_graph(GRAPH)
+    keys = G.edges_to_keys(src, dst)
+    m = len(keys)
+    half, step, slide = schedule(keys)
+    gen_s = time.time() - t0
+    stream = torch.cuda.current_stream()
+    g = G.GPMA(n, stream)
+    G.update_gpma(g, keys[:half], np.ones(half, np.uint8), stream)
+    g.set_profiling(True)
+
+    def timed_bfs(repeats):
+        out = torch.empty(n, dtype=torch.int32, device="cuda")
+        times = []
+        reached = 0
+        for _ in range(repeats):
+            g.reset_profile()
+            _, reached = G.gpma_bfs(g, n, m, 0, out, stream)
+            times.append(g.profile()["bfs_ms"])
+        levels = out.cpu().numpy().view(np.uint32)
+        edges = live_out_degree_sum(g, levels)
+        ms = statistics.median(times)
+        return {"reached": int(reached), "edges_traversed": edges, "ms": ms, "gteps": edges / (ms * 1e-3) / 1e9}
+
+    bfs_before = timed_bfs(args.bfs_repeats)
+
+    total = args.warmup + args.steps
+    dk, dv = [], []
+    for i in range(total):
+        k, v = slide(i)
+        dk.append(torch.from_numpy(k.view(np.int64)).cuda())
+        dv.append(torch.from_numpy(v).cuda())
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    for i in range(args.warmup):
+        G.update_gpma(g, dk[i], dv[i], stream)
+
+    st0 = g.stats()
+    g.reset_profile()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for j in range(args.steps):
+            flush.fill_(j & 0xFF)
+            a, b = ev[j]
+            a.record(stream)
+            G.update_gpma(g, dk[args.warmup + j], dv[args.warmup + j], stream)
+            b.record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    prof = g.profile()
+    st1 = g.stats()
+    time_s = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([time_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        time_s = float(t.item())
+    batch = 2 * step
+    updates = batch * args.steps * world
+    value = updates / time_s
+    accepted_slots = (st1["accepted_slots"] - st0["accepted_slots"]) / args.steps
+
+    # roofline of the dominant kernel (the persistent update kernel):
+    # algorithmic bytes per launch = 9 B x batch (read the sorted batch)
+    #                              + 18 B x slots of redispatched windows (read + write)
+    upd_ms = prof["update_kernel_ms"] / max(1, prof["update_kernels"])
+    upd_bytes = 9.0 * batch + 18.0 * accepted_slots
+    peak, peak_src = peak_hbm()
+    achieved = upd_bytes / (upd_ms * 1e-3) / 1e9
+    traffic = profiled_traffic("update_kernel")
+    step_bytes = 18.0 * batch + 18.0 * accepted_slots
+
+    # BFS after the slides (the demo's second BFS)
+    bfs_after = timed_bfs(args.bfs_repeats)
+
+    # e2e: next K slides through the C ABI from pinned host buffers
+    hk, hv = [], []
+    for i in range(total, total + args.steps):
+        k, v = slide(i)
+        hk.append(torch.from_numpy(k.view(np.int64)).pin_memory())
+        hv.append(torch.from_numpy(v).pin_memory())
+    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for j in range(args.steps):
+        flush.fill_(j & 0xFF)
+        a, b = e2e_ev[j]
+        a.record(stream)
+        G.update_gpma(g, hk[j], hv[j], stream)
+        b.record(stream)
+    torch.cuda.synchronize()
+    e2e_s = sum(a.elapsed_time(b) for a, b in e2e_ev) / 1e3
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(n, keys, half, slide, args.cpu_sample_steps)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * time_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": DATA,
+            "config": workload_config(n, m, step),
+            "roofline": {"bound": "hbm", "kernel": "update_kernel", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": upd_bytes, "launch_ms": upd_ms, "peak_source": peak_src,
+                         "step_bytes": step_bytes, "step_frac": step_bytes / (1e-3 * time_s * 1e3 / args.steps)
+                         / 1e9 / peak},
+            "e2e": {"value": updates / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 9 * batch,
+                    "d2h_bytes_per_step": 64},
+            "gpu_launches": prof["kernel_launches"],
+            "clocks": clk.summary(),
+            "bfs": {"before": bfs_before, "after": bfs_after, "unit": "GTEPS",
+                    "gteps": bfs_after["gteps"]},
+            "phases_ms_per_step": {"sort": prof["sort_ms"] / args.steps,
+                                   "update_kernel": prof["update_kernel_ms"] / args.steps,
+                                   "root_rebuild": prof["rebuild_ms"] / args.steps},
+            "levels_per_step": (st1["levels_visited"] - st0["levels_visited"]) / args.steps,
+            "setup_s": {"generate": gen_s},
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    g.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(n, keys, half, slide, steps):
+    """The oracle restatement on all host cores: load untimed, `steps` slides timed."""
+    from oracle.oracle import OracleGPMA, build
+
+    build()
+    cores = os.cpu_count() or 1
+    o = OracleGPMA(n, threads=cores)
+    o.update(keys[:half], np.ones(half, np.uint8))
+    t = 0.0
+    batch = 0
+    for i in range(steps):
+        k, v = slide(i)
+        t0 = time.perf_counter()
+        o.update(k, v)
+        t += time.perf_counter() - t0
+        batch = len(k)
+    o.close()
+    return {"value": steps * batch / t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{steps} slide updates of {batch:,} keys after an untimed load of {half:,} edges "
+                      f"(same graph), OpenMP on {cores} threads"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    import gpma_bfs_gb300 as G
+    from gpma_bfs_gb300.workloads import make_graph
+    from oracle.oracle import OracleGPMA, build
+
+    build()
+    n, src, dst = make_graph(GRAPH)
+    keys = G.edges_to_keys(src, dst)
+    half, step, slide = schedule(keys)
+    cores = os.cpu_count() or 1
+    o = OracleGPMA(n, threads=cores)
+    o.update(keys[:half], np.ones(half, np.uint8))
+    for i in range(args.warmup):
+        o.update(*slide(i))
+    t = 0.0
+    for j in range(args.steps):
+        k, v = slide(args.warmup + j)
+        t0 = time.perf_counter()
+        o.update(k, v)
+        t += time.perf_counter() - t0
+    value = 2 * step * args.steps / t
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64", "data": DATA, "config": workload_config(n, len(keys), step), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} timed slide updates of {2 * step:,} keys after {args.warmup} "
+                                   f"warm-up slides and an untimed load of {half:,} edges"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gpma", "reference"], default="gpma")
+    ap.add_argument("--bfs-repeats", type=int, default=3)
+    ap.add_argument("--cpu-sample-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -58,6 +58,12 @@ class _Stats(ctypes.Structure):
         "root_resizes", "root_drops", "significant")]
 
 
+class _Profile(ctypes.Structure):
+    _fields_ = [("sort_ms", ctypes.c_double), ("update_kernel_ms", ctypes.c_double), ("rebuild_ms", ctypes.c_double),
+                ("bfs_ms", ctypes.c_double), ("update_kernels", ctypes.c_uint64), ("bfs_kernels", ctypes.c_uint64),
+                ("kernel_launches", ctypes.c_uint64)]
+
+
 _lib = None
 
 
@@ -83,6 +89,9 @@ def lib() -> ctypes.CDLL:
         "gpma_export_compact": (st, [P, P, u64, ctypes.POINTER(u64), P]),
         "gpma_device_arrays": (st, [P, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P)]),
         "gpma_get_stats": (st, [P, ctypes.POINTER(_Stats)]),
+        "gpma_set_profiling": (st, [P, ctypes.c_int]),
+        "gpma_get_profile": (st, [P, ctypes.POINTER(_Profile)]),
+        "gpma_reset_profile": (st, [P]),
         "gpma_status_string": (ctypes.c_char_p, [st]),
         "gpma_last_error": (ctypes.c_char_p, []),
         "gpma_version": (ctypes.c_char_p, []),
@@ -237,6 +246,18 @@ class GPMA:
         s = _Stats()
         _check(lib().gpma_get_stats(self.handle, ctypes.byref(s)), "gpma_get_stats")
         return {name: getattr(s, name) for name, _ in _Stats._fields_}
+
+    def set_profiling(self, enabled: bool = True) -> None:
+        """Time each phase with CUDA events on the calling stream."""
+        _check(lib().gpma_set_profiling(self.handle, int(bool(enabled))), "gpma_set_profiling")
+
+    def profile(self) -> dict:
+        p = _Profile()
+        _check(lib().gpma_get_profile(self.handle, ctypes.byref(p)), "gpma_get_profile")
+        return {name: getattr(p, name) for name, _ in _Profile._fields_}
+
+    def reset_profile(self) -> None:
+        _check(lib().gpma_reset_profile(self.handle), "gpma_reset_profile")
 
     def device_arrays(self) -> tuple[int, int, int]:
         k, v, r = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()

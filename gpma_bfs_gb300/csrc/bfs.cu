@@ -280,6 +280,7 @@ gpma_status bfs_run(gpma_graph *g, uint32_t src, cudaStream_t s, uint64_t *reach
     GPMA_CUDA(cudaMemsetAsync(g->bfs_levels, 0, sizeof(uint32_t) * n, s));
     GPMA_CUDA(cudaMemsetAsync(g->bfs_visited, 0, sizeof(uint32_t) * (n / 32 + 2), s));
     GPMA_CUDA(cudaMemsetAsync(g->bfs_ctl, 0, sizeof(uint32_t) * CTL_WORDS, s));
+    prof_mark(g, 0, s);
     bfs_init_kernel<<<1, 1, 0, s>>>(g->bfs_levels, g->bfs_visited, g->bfs_queue[0], g->bfs_ctl, src);
     BfsArgs A;
     A.keys = g->keys;
@@ -294,8 +295,12 @@ gpma_status bfs_run(gpma_graph *g, uint32_t src, cudaStream_t s, uint64_t *reach
     A.ctl = g->bfs_ctl;
     void *params[] = {&A};
     GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)bfs_kernel, dim3(g->bfs_grid), dim3(BLOCK), params, 0, s));
+    prof_mark(g, 1, s);
     GPMA_CUDA(cudaMemcpyAsync(g->h_bfs_ctl, g->bfs_ctl, sizeof(uint32_t) * CTL_WORDS, cudaMemcpyDeviceToHost, s));
     GPMA_CUDA(cudaStreamSynchronize(s));
+    g->prof.kernel_launches += 2;
+    g->prof.bfs_kernels++;
+    g->prof.bfs_ms += prof_elapsed(g, 0, 1);
     if (g->h_bfs_ctl[CTL_ERR]) {
         set_error("device-side wait gave up in the BFS kernel (code %u)", g->h_bfs_ctl[CTL_ERR]);
         return GPMA_ERR_TIMEOUT;
@@ -338,7 +343,9 @@ gpma_status bfs_multi_run(gpma_graph *g, const uint32_t *d_src, uint32_t k, cuda
     A.levels = g->msbfs_levels;
     A.ctl = g->bfs_ctl;
     void *params[] = {&A};
+    prof_mark(g, 0, s);
     GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)msbfs_kernel, dim3(g->bfs_grid), dim3(BLOCK), params, 0, s));
+    prof_mark(g, 1, s);
     unsigned long long *reached = reinterpret_cast<unsigned long long *>(g->bfs_ctl + CTL_WORDS);
     count_reached_kernel<<<std::max(1, std::min(g->sms * 4, (int)((n + BLOCK - 1) / BLOCK))), BLOCK, 0, s>>>(
         g->msbfs_levels, n, k, reached);
@@ -346,6 +353,9 @@ gpma_status bfs_multi_run(gpma_graph *g, const uint32_t *d_src, uint32_t k, cuda
     GPMA_CUDA(cudaMemcpyAsync(g->h_bfs_ctl, g->bfs_ctl, sizeof(uint32_t) * (CTL_WORDS + 2 * 64),
                               cudaMemcpyDeviceToHost, s));
     GPMA_CUDA(cudaStreamSynchronize(s));
+    g->prof.kernel_launches += 2;
+    g->prof.bfs_kernels++;
+    g->prof.bfs_ms += prof_elapsed(g, 0, 1);
     if (g->h_bfs_ctl[CTL_ERR]) {
         set_error("device-side wait gave up in the multi-source BFS kernel (code %u)", g->h_bfs_ctl[CTL_ERR]);
         return GPMA_ERR_TIMEOUT;

@@ -93,6 +93,9 @@ void release(gpma_graph *g) {
         cudaFreeHost(g->h_status);
     g->h_status = nullptr;
     free_bfs(g);
+    for (auto &e : g->ev)
+        if (e)
+            cudaEventDestroy(e);
     if (g->h_bfs_ctl)
         cudaFreeHost(g->h_bfs_ctl);
     g->h_bfs_ctl = nullptr;
@@ -257,6 +260,7 @@ gpma_status gpma_create(uint32_t row_num, void *stream, gpma_graph **out) {
         return st;
     }
     g->stats = gpma_stats{};
+    g->prof = gpma_profile{};
     *out = g;
     return GPMA_OK;
 }
@@ -440,6 +444,37 @@ gpma_status gpma_device_arrays(gpma_graph *g, const uint64_t **keys, const uint8
         *values = g->values;
     if (row_offset)
         *row_offset = g->row_offset;
+    return GPMA_OK;
+}
+
+gpma_status gpma_set_profiling(gpma_graph *g, int enabled) {
+    if (!g) {
+        set_error("gpma_set_profiling: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    if (enabled && !g->ev[0]) {
+        for (auto &e : g->ev)
+            GPMA_CUDA(cudaEventCreate(&e));
+    }
+    g->profiling = enabled != 0;
+    return GPMA_OK;
+}
+
+gpma_status gpma_get_profile(const gpma_graph *g, gpma_profile *out) {
+    if (!g || !out) {
+        set_error("gpma_get_profile: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    *out = g->prof;
+    return GPMA_OK;
+}
+
+gpma_status gpma_reset_profile(gpma_graph *g) {
+    if (!g) {
+        set_error("gpma_reset_profile: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    g->prof = gpma_profile{};
     return GPMA_OK;
 }
 

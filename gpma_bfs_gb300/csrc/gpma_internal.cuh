@@ -145,10 +145,11 @@ struct gpma_graph {
     uint32_t *msbfs_levels = nullptr;
     uint64_t msbfs_levels_cap = 0;
     uint32_t *msbfs_src = nullptr;
-    // staging for host pointers
-    void *h_stage = nullptr;
-    size_t h_stage_cap = 0;
     gpma_stats stats{};
+    // profiling: events on the caller's stream around each phase
+    bool profiling = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    gpma_profile prof{};
 };
 
 namespace gpma {
@@ -192,6 +193,21 @@ void dev_free(T *&p) {
     if (p)
         cudaFree((void *)p);
     p = nullptr;
+}
+
+// ---- profiling helpers -------------------------------------------------------
+inline void prof_mark(gpma_graph *g, int i, cudaStream_t s) {
+    if (g->profiling)
+        cudaEventRecord(g->ev[i], s);
+}
+// elapsed ms between two recorded events (both complete: call after a sync)
+inline double prof_elapsed(gpma_graph *g, int a, int b) {
+    float ms = 0.f;
+    if (g->profiling && cudaEventElapsedTime(&ms, g->ev[a], g->ev[b]) != cudaSuccess) {
+        cudaGetLastError();
+        ms = 0.f;
+    }
+    return ms;
 }
 
 // ---- host entry points implemented per translation unit -------------------

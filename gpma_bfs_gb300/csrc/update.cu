@@ -841,6 +841,8 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, uint32_t pend_buf, uin
     const uint8_t *pend_v = g->ivals[pend_buf] + pend_a;
     const uint32_t size = g->geo.size;
     const uint32_t chunks = (size + CHUNK - 1) / CHUNK;
+    prof_mark(g, 0, s);
+    g->prof.kernel_launches += 4;
     // 1. stable compaction of the live slots (resize_gpma, gpma.cuh:909-915)
     chunk_live_kernel<<<grid_for((uint64_t)chunks * BLOCK, g->sms, 8), BLOCK, 0, s>>>(g->keys, g->values, size,
                                                                                        g->chunk_cnt);
@@ -914,9 +916,11 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, uint32_t pend_buf, uin
         g->stats.root_resizes++;
     }
     GPMA_CUDA(cudaGetLastError());
+    prof_mark(g, 1, s);
     g->geo = geo;
     GPMA_TRY(upload_geometry(g, s));
     GPMA_CUDA(cudaStreamSynchronize(s));
+    g->prof.rebuild_ms += prof_elapsed(g, 0, 1);
     // the scratch must cover the whole array for later wide windows
     GPMA_TRY(ensure_scratch(g, geo.size));
     return GPMA_OK;
@@ -1005,7 +1009,9 @@ gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_
         GPMA_TRY(dev_alloc(&g->cta_cnt, 4ull * g->update_grid));
     }
     GPMA_CUDA(cudaMemsetAsync(g->status, 0, sizeof(DeviceStatus), s));
+    prof_mark(g, 0, s);
     GPMA_TRY(sort_batch(g, n, s, check_keys));
+    prof_mark(g, 1, s);
     UpdateArgs A;
     A.keys = g->keys;
     A.vals = g->values;
@@ -1044,8 +1050,13 @@ gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_
     void *params[] = {&A};
     GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)update_kernel, dim3(g->update_grid), dim3(BLOCK), params,
                                           UPDATE_SMEM, s));
+    prof_mark(g, 2, s);
     GPMA_CUDA(cudaMemcpyAsync(g->h_status, g->status, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
     GPMA_CUDA(cudaStreamSynchronize(s));
+    g->prof.kernel_launches += 11;  // histogram, plan, 8 digit passes, update kernel
+    g->prof.update_kernels++;
+    g->prof.sort_ms += prof_elapsed(g, 0, 1);
+    g->prof.update_kernel_ms += prof_elapsed(g, 1, 2);
     const DeviceStatus &h = *g->h_status;
     if (h.invalid_keys) {
         set_error("update batch holds keys whose column is 0xFFFFFFFF (reserved for row guards and empty slots)");

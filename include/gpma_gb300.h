@@ -126,6 +126,25 @@ GPMA_API gpma_status gpma_device_arrays(gpma_graph *g, const uint64_t **keys, co
 
 GPMA_API gpma_status gpma_get_stats(const gpma_graph *g, gpma_stats *out);
 
+/* ---- profiling -------------------------------------------------------------
+ * With profiling on, CUDA events recorded on the caller's stream time each
+ * phase; times accumulate until gpma_reset_profile. kernel_launches counts
+ * every kernel the library launched on the graph's behalf (always on).
+ * No reference counterpart (the reference printed wall-clock deltas,
+ * rdebug.hpp:8-17). */
+typedef struct gpma_profile {
+    double sort_ms;          /* batch radix sort (histogram, plan, digit passes) */
+    double update_kernel_ms; /* persistent update kernel: locate .. level loop */
+    double rebuild_ms;       /* root resize / bulk rebuild kernels */
+    double bfs_ms;           /* BFS kernels (single- and multi-source) */
+    uint64_t update_kernels; /* launches of the persistent update kernel */
+    uint64_t bfs_kernels;    /* launches of BFS traversal kernels */
+    uint64_t kernel_launches;
+} gpma_profile;
+GPMA_API gpma_status gpma_set_profiling(gpma_graph *g, int enabled);
+GPMA_API gpma_status gpma_get_profile(const gpma_graph *g, gpma_profile *out);
+GPMA_API gpma_status gpma_reset_profile(gpma_graph *g);
+
 /* ---- diagnostics ---------------------------------------------------------- */
 GPMA_API const char *gpma_status_string(gpma_status s);
 /* Detail text of the last failing call on this host thread ("" if none). */
