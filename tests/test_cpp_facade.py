@@ -1,0 +1,52 @@
+"""The C++ drop-in facade (include/gpma_compat.hpp) used the way the
+reference demo uses its API (gpma_bfs_demo.cu:32-116)."""
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+LIBDIR = ROOT / "gpma_bfs_gb300"
+
+
+def build_demo(tmp_path) -> Path:
+    exe = tmp_path / "facade_demo"
+    subprocess.run(["g++", "-O2", "-std=c++17", f"-I{ROOT / 'include'}", str(ROOT / "tests/cpp/facade_demo.cpp"),
+                    f"-L{LIBDIR}", "-lgpma_gb300", f"-Wl,-rpath,{LIBDIR}", "-o", str(exe)],
+                   check=True, capture_output=True, text=True)
+    return exe
+
+
+def test_facade_compiles_and_links(tmp_path, built_lib):
+    exe = build_demo(tmp_path)
+    assert exe.exists()
+    # no GPU needed for argument handling
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert "Invalid arguments." in r.stdout
+
+
+@pytest.mark.gpu
+def test_facade_demo_matches_oracle(tmp_path, built_lib):
+    import gpma_bfs_gb300 as G
+    from oracle.oracle import OracleGPMA
+
+    src, dst = G.gen_rmat(12, 16, seed=17)
+    n = 1 << 12
+    path = tmp_path / "g.txt"
+    G.write_edges_text(path, n, src, dst)
+    exe = build_demo(tmp_path)
+    out = subprocess.run([str(exe), str(path), "0"], capture_output=True, text=True, check=True).stdout
+    got = [int(line.rsplit(":", 1)[1]) for line in out.splitlines() if "reachable" in line]
+    keys = G.edges_to_keys(src, dst)
+    half = len(keys) // 2
+    step = half // 100
+    o = OracleGPMA(n, threads=4)
+    o.update(keys[:half], np.ones(half, np.uint8))
+    want = [o.bfs(0)[1]]
+    for i in range(100):
+        ins = keys[half + i * step: half + (i + 1) * step]
+        dels = keys[i * step: (i + 1) * step]
+        o.update(np.concatenate([ins, dels]), np.r_[np.ones(step, np.uint8), np.zeros(step, np.uint8)])
+    want.append(o.bfs(0)[1])
+    assert got == want
