@@ -83,6 +83,7 @@ def lib() -> ctypes.CDLL:
         "gpma_update": (st, [P, P, P, u64, P]),
         "gpma_bfs": (st, [P, u32, P, ctypes.POINTER(u64), P]),
         "gpma_bfs_multi": (st, [P, P, u32, P, P, P]),
+        "gpma_bfs_noalloc": (st, [P, u32, P, ctypes.POINTER(u64), P]),
         "gpma_get_geometry": (st, [P, ctypes.POINTER(_Geometry)]),
         "gpma_get_thresholds": (st, [P, P, P]),
         "gpma_export_layout": (st, [P, P, P, P, P]),

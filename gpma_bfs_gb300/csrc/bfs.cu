@@ -23,6 +23,7 @@
 #include "gpma_internal.cuh"
 
 #include <algorithm>
+#include <mutex>
 
 namespace gpma {
 namespace {
@@ -360,6 +361,104 @@ gpma_status bfs_multi_run(gpma_graph *g, const uint32_t *d_src, uint32_t k, cuda
         set_error("device-side wait gave up in the multi-source BFS kernel (code %u)", g->h_bfs_ctl[CTL_ERR]);
         return GPMA_ERR_TIMEOUT;
     }
+    return GPMA_OK;
+}
+
+// ---- BFS without device allocation ------------------------------------------
+// Some callers cannot allocate device memory on the fly: code that runs under
+// a host-side memory arena or a fixed device-memory budget, plug-ins whose
+// host process owns every cudaMalloc, or hosts whose pool forbids growth once
+// serving starts. For them gpma_bfs_noalloc keeps the BFS working set (visited
+// bitmap, two frontier queues, control words) in one file-scope device array
+// of a fixed size instead of buffers allocated per graph. Every GPU that loads
+// this library holds the array (about 17 MB) until the process exits.
+namespace {
+
+constexpr uint32_t NOALLOC_MAX_ROWS = 1u << 21;  // 2,097,152 nodes
+constexpr uint32_t NOALLOC_VISITED_WORDS = NOALLOC_MAX_ROWS / 32 + 2;
+constexpr size_t NOALLOC_WORDS = CTL_WORDS + NOALLOC_VISITED_WORDS + 2ull * NOALLOC_MAX_ROWS;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+static __device__ __align__(256) uint32_t g_noalloc_scratch[NOALLOC_WORDS];
+
+std::mutex g_noalloc_mu;
+uint32_t *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+int g_noalloc_grid[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of the scratch array on the current device. The host-side
+// symbol is only a stand-in, so the address is looked up once per device
+// (with that device current) and cached.
+gpma_status noalloc_scratch(uint32_t **out, int *grid, int sms) {
+    int dev = 0;
+    GPMA_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+        set_error("gpma_bfs_noalloc: device %d outside the supported range 0..%d", dev, NOALLOC_MAX_DEVICES - 1);
+        return GPMA_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bfs_kernel, BLOCK, 0);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor(bfs_kernel)");
+        if (per_sm < 1) {
+            set_error("gpma_bfs_noalloc: BFS kernel cannot be resident (occupancy 0)");
+            return GPMA_ERR_CUDA;
+        }
+        g_noalloc_grid[dev] = sms * std::min(per_sm, 8);
+        g_noalloc_ptr[dev] = static_cast<uint32_t *>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    *grid = g_noalloc_grid[dev];
+    return GPMA_OK;
+}
+
+}  // namespace
+
+gpma_status bfs_noalloc_run(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached, cudaStream_t s) {
+    const uint32_t n = g->row_num;
+    if (n > NOALLOC_MAX_ROWS) {
+        set_error("gpma_bfs_noalloc: graph has %u nodes; the fixed scratch holds at most %u", n, NOALLOC_MAX_ROWS);
+        return GPMA_ERR_CAPACITY;
+    }
+    uint32_t *scratch = nullptr;
+    int grid = 0;
+    GPMA_TRY(noalloc_scratch(&scratch, &grid, g->sms));
+    uint32_t *ctl = scratch;
+    uint32_t *visited = scratch + CTL_WORDS;
+    uint32_t *q0 = visited + NOALLOC_VISITED_WORDS;
+    uint32_t *q1 = q0 + NOALLOC_MAX_ROWS;
+    // the scratch keeps the previous call's contents: clear what must start at zero
+    GPMA_CUDA(cudaMemsetAsync(levels, 0, sizeof(uint32_t) * n, s));
+    GPMA_CUDA(cudaMemsetAsync(visited, 0, sizeof(uint32_t) * (n / 32 + 2), s));
+    GPMA_CUDA(cudaMemsetAsync(ctl, 0, sizeof(uint32_t) * CTL_WORDS, s));
+    bfs_init_kernel<<<1, 1, 0, s>>>(levels, visited, q0, ctl, src);
+    BfsArgs A;
+    A.keys = g->keys;
+    A.vals = g->values;
+    A.ro = g->row_offset;
+    A.n = n;
+    A.size = g->geo.size;
+    A.levels = levels;
+    A.visited = visited;
+    A.q0 = q0;
+    A.q1 = q1;
+    A.ctl = ctl;
+    void *params[] = {&A};
+    GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)bfs_kernel, dim3(grid), dim3(BLOCK), params, 0, s));
+    uint32_t h_ctl[CTL_WORDS];
+    GPMA_CUDA(cudaMemcpyAsync(h_ctl, ctl, sizeof(h_ctl), cudaMemcpyDeviceToHost, s));
+    GPMA_CUDA(cudaStreamSynchronize(s));
+    if (h_ctl[CTL_ERR]) {
+        set_error("device-side wait gave up in the BFS kernel (code %u)", h_ctl[CTL_ERR]);
+        return GPMA_ERR_TIMEOUT;
+    }
+    if (reached)
+        *reached = h_ctl[CTL_REACHED];
     return GPMA_OK;
 }
 

@@ -310,6 +310,22 @@ gpma_status gpma_bfs(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *re
     return GPMA_OK;
 }
 
+gpma_status gpma_bfs_noalloc(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached, void *stream) {
+    if (!g || !levels) {
+        set_error("gpma_bfs_noalloc: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    if (src >= g->row_num) {
+        set_error("gpma_bfs_noalloc: start node %u out of range (row_num %u)", src, g->row_num);
+        return GPMA_ERR_INVALID;
+    }
+    if (!is_device_pointer(levels)) {
+        set_error("gpma_bfs_noalloc: levels must be device memory (no staging buffer can be allocated)");
+        return GPMA_ERR_INVALID;
+    }
+    return bfs_noalloc_run(g, src, levels, reached, (cudaStream_t)stream);
+}
+
 gpma_status gpma_bfs_multi(gpma_graph *g, const uint32_t *srcs, uint32_t k, uint32_t *levels, uint64_t *reached,
                            void *stream) {
     if (!g || !srcs || !levels || k == 0 || k > 64) {

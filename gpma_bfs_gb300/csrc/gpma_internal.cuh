@@ -218,6 +218,7 @@ gpma_status sort_batch(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_key
 gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys = true);
 gpma_status bfs_run(gpma_graph *g, uint32_t src, cudaStream_t s, uint64_t *reached);
 gpma_status bfs_multi_run(gpma_graph *g, const uint32_t *d_src, uint32_t k, cudaStream_t s);
+gpma_status bfs_noalloc_run(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached, cudaStream_t s);
 void free_bfs(gpma_graph *g);
 
 }  // namespace gpma

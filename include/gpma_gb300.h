@@ -100,6 +100,22 @@ GPMA_API gpma_status gpma_bfs(gpma_graph *g, uint32_t src, uint32_t *levels, uin
 GPMA_API gpma_status gpma_bfs_multi(gpma_graph *g, const uint32_t *srcs, uint32_t k, uint32_t *levels, uint64_t *reached,
                            void *stream);
 
+/* BFS for callers that cannot allocate device memory (a host-side arena or a
+ * fixed device budget owns every allocation, or allocation is forbidden
+ * while serving). No counterpart in the reference. Same result as gpma_bfs,
+ * but it allocates nothing: its working set (visited bitmap, two frontier
+ * queues, control words) is one fixed device array inside the library, about
+ * 17 MB, held by every GPU that loads the library until the process exits.
+ * Limits: row_num <= 2,097,152 (GPMA_ERR_CAPACITY beyond); levels must be
+ * device memory of row_num entries (GPMA_ERR_INVALID otherwise); reached is an
+ * optional host pointer. The first call on a device looks up the array's
+ * device address with that device current; make that first call before any
+ * stream capture. All calls share the one array and it keeps the last call's
+ * contents, so calls whose work overlaps on the GPU (other threads, other
+ * streams) race: serialise them. */
+GPMA_API gpma_status gpma_bfs_noalloc(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached,
+                                      void *stream);
+
 /* ---- views ---------------------------------------------------------------
  * GPMA's public members (gpma.cuh:31-52) as read-only views. */
 GPMA_API gpma_status gpma_get_geometry(const gpma_graph *g, gpma_geometry *out);
