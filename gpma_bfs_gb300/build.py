@@ -27,9 +27,9 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", f"-I{INCLUDE}"]
 CC_FLAGS = ["-O2", "-std=c11", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall", f"-I{INCLUDE}"]
 
-CU_SOURCES = ["sort.cu", "update.cu", "bfs.cu", "capi.cu"]
+CU_SOURCES = ["update.cu", "bfs.cu", "capi.cu"]
 C_SOURCES = ["graphgen.c"]
-HEADERS = [CSRC / "gpma_internal.cuh", INCLUDE / "gpma_gb300.h"]
+HEADERS = [CSRC / "gpma_internal.cuh", CSRC / "sort.cuh", INCLUDE / "gpma_gb300.h"]
 
 
 def _nvcc() -> str:
@@ -55,11 +55,22 @@ def _run(cmd: list[str]) -> None:
 
 
 def build(verbose: bool = False, ptxas_info: bool = False) -> Path:
-    """Compiles (if needed) and returns the path of libgpma_gb300.so."""
+    """Compiles (if needed) and returns the path of libgpma_gb300.so.
+
+    GPMA_UPDATE_MIN_BLOCKS (environment) sets the update kernel's minimum
+    resident CTAs per SM for register allocation; changing it rebuilds.
+    """
     if verbose:
         os.environ["GPMA_BUILD_VERBOSE"] = "1"
     nvcc = _nvcc()
     BUILD.mkdir(exist_ok=True)
+    min_blocks = os.environ.get("GPMA_UPDATE_MIN_BLOCKS", "2")
+    stamp = BUILD / "options.txt"
+    options = f"GPMA_UPDATE_MIN_BLOCKS={min_blocks}\n"
+    if not stamp.exists() or stamp.read_text() != options:
+        stamp.write_text(options)
+    NVCC_FLAGS.append(f"-DGPMA_UPDATE_MIN_BLOCKS={min_blocks}")
+    HEADERS.append(stamp)
     jobs = []
     objs = []
     for name in CU_SOURCES:

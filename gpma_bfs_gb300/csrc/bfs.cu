@@ -9,11 +9,14 @@
 // from level L gets L+1.
 //
 // Single source: one persistent cooperative kernel runs every level,
-// separated by bounded grid barriers. The frontier is a queue; a warp scans
-// the slot range of one frontier node with coalesced 8-byte key and 1-byte
-// value loads; the visited set is a bitmap claimed with atomicOr (a plain
-// load filters already-visited targets first); new nodes are appended with
-// one warp-aggregated atomic per warp step.
+// separated by bounded grid barriers. Frontiers are bitmaps (no queue, no
+// queue atomics). Per level, phase 1 gives each warp one frontier word at a
+// time: the short rows of its up to 32 nodes are walked as one concatenated
+// slot range (warp-level load balancing, two slots per lane per step, all
+// loads issued before any claim) and long rows are queued as 64-slot chunks;
+// phase 2 spreads those chunks over every warp. A target is claimed with
+// atomicOr on the visited bitmap (a plain load filters visited targets first)
+// and enters the next frontier bitmap.
 //
 // Multi-source (k <= 64): one bit lane per source in 64-bit masks
 // (visited, frontier, next); per level a warp takes 32 nodes, and for each
@@ -30,13 +33,22 @@ namespace {
 
 // bfs_ctl layout (u32 words)
 enum : uint32_t {
-    CTL_CNT = 0,      // 3 rotating queue counters
-    CTL_ERR = 4,
-    CTL_LEVELS = 5,
-    CTL_REACHED = 6,
-    CTL_BAR = 8,      // GridBarrier (2 words)
+    CTL_CNT = 0,      // 3 rotating counters: nodes first reached per level
+    CTL_CHUNKS = 3,   // 3 rotating counters: big-row chunks queued per level
+    CTL_ERR = 6,
+    CTL_LEVELS = 7,
+    CTL_REACHED = 8,
+    CTL_BAR = 10,     // GridBarrier (2 words)
     CTL_WORDS = 16,
 };
+
+// Rows longer than BIG_ROW slots are cut into CHUNK_SLOTS-slot chunks that
+// every warp of the grid shares in a second phase of the level; shorter rows
+// of one frontier word are walked together by one warp. (With node ids
+// ordered by degree, one word can otherwise hold 32 heavy rows.)
+constexpr uint32_t BIG_ROW = 32;
+constexpr uint32_t CHUNK_SLOTS = 64;
+constexpr uint32_t BFS_CHUNK_CAP = 1u << 20;
 
 struct BfsArgs {
     const uint64_t *keys;
@@ -46,10 +58,64 @@ struct BfsArgs {
     uint32_t size;
     uint32_t *levels;
     uint32_t *visited;
-    uint32_t *q0;
-    uint32_t *q1;
+    uint32_t *front0;  // frontier bitmaps (ping-pong), n/32+2 words each
+    uint32_t *front1;
+    uint2 *chunks;     // [slot begin, slot end) of big-row chunks
+    uint32_t chunk_cap;
     uint32_t *ctl;
 };
+
+// Two edge slots per lane (s < SIZE_NONE means present): all loads are
+// issued before any claim, so each lane keeps several requests in flight.
+// Returns the number of nodes this lane claimed.
+__device__ __forceinline__ uint32_t visit_pair(const BfsArgs &A, uint32_t sa, uint32_t sb, uint32_t next_level,
+                                               uint32_t *front_next) {
+    uint64_t ka = KEY_NONE, kb = KEY_NONE;
+    uint8_t va = 0, vb = 0;
+    if (sa != SIZE_NONE) {
+        ka = A.keys[sa];
+        va = A.vals[sa];
+    }
+    if (sb != SIZE_NONE) {
+        kb = A.keys[sb];
+        vb = A.vals[sb];
+    }
+    const uint32_t wa = (uint32_t)ka, wb = (uint32_t)kb;
+    const bool oka = wa != 0xFFFFFFFFu && va != 0 && wa < A.n;
+    const bool okb = wb != 0xFFFFFFFFu && vb != 0 && wb < A.n;
+    const uint32_t bita = 1u << (wa & 31), bitb = 1u << (wb & 31);
+    const uint32_t seen_a = oka ? A.visited[wa >> 5] : 0xFFFFFFFFu;
+    const uint32_t seen_b = okb ? A.visited[wb >> 5] : 0xFFFFFFFFu;
+    uint32_t fresh = 0;
+    if (!(seen_a & bita) && !(atomicOr(&A.visited[wa >> 5], bita) & bita)) {
+        A.levels[wa] = next_level;
+        atomicOr(&front_next[wa >> 5], bita);
+        ++fresh;
+    }
+    if (!(seen_b & bitb) && !(atomicOr(&A.visited[wb >> 5], bitb) & bitb)) {
+        A.levels[wb] = next_level;
+        atomicOr(&front_next[wb >> 5], bitb);
+        ++fresh;
+    }
+    return fresh;
+}
+
+// Slot of concatenated-range position p (< total) of a warp's rows: lane r
+// holds its row start b and exclusive prefix excl; finds the last r with
+// excl[r] <= p. All lanes must call it together.
+__device__ __forceinline__ uint32_t lb_slot(uint32_t p, uint32_t total, uint32_t b, uint32_t excl) {
+    uint32_t r = 0;
+#pragma unroll
+    for (uint32_t step = 16; step >= 1; step >>= 1) {
+        const uint32_t cand = r + step;
+        const uint32_t ex_c = __shfl_sync(0xFFFFFFFFu, excl, cand & 31);
+        if (cand < 32 && ex_c <= p)
+            r = cand;
+    }
+    const uint32_t rb = __shfl_sync(0xFFFFFFFFu, b, r);
+    const uint32_t rex = __shfl_sync(0xFFFFFFFFu, excl, r);
+    return p < total ? rb + (p - rex) : SIZE_NONE;
+}
 
 __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
     GridBarrier *bar = reinterpret_cast<GridBarrier *>(A.ctl + CTL_BAR);
@@ -57,66 +123,98 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t gwarp = blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5);
     const uint32_t nwarps = gridDim.x * (BLOCK / 32);
+    const uint32_t words = (A.n + 31) >> 5;
     uint32_t added = 0;
     uint32_t i = 0;
     for (;; ++i) {
-        const uint32_t nq = ld_volatile(A.ctl + CTL_CNT + i % 3);
-        if (nq == 0)
+        if (ld_volatile(A.ctl + CTL_CNT + i % 3) == 0)
             break;
-        if (blockIdx.x == 0 && threadIdx.x == 0)
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
             A.ctl[CTL_CNT + (i + 2) % 3] = 0;
-        uint32_t *out_cnt = A.ctl + CTL_CNT + (i + 1) % 3;
-        const uint32_t *qin = (i & 1) ? A.q1 : A.q0;
-        uint32_t *qout = (i & 1) ? A.q0 : A.q1;
+            A.ctl[CTL_CHUNKS + (i + 1) % 3] = 0;
+        }
+        uint32_t *front_cur = (i & 1) ? A.front1 : A.front0;
+        uint32_t *front_next = (i & 1) ? A.front0 : A.front1;
+        uint32_t *chunk_cnt = A.ctl + CTL_CHUNKS + i % 3;
         const uint32_t next_level = i + 2;
-        for (uint32_t idx = gwarp; idx < nq; idx += nwarps) {
-            const uint32_t u = qin[idx];
-            uint32_t b = A.ro[u], e = A.ro[u + 1];
-            e = min(e, A.size);
-            for (uint32_t s0 = b; s0 < e; s0 += 32) {
-                const uint32_t s = s0 + lane;
-                bool fresh = false;
-                uint32_t w = 0;
-                if (s < e) {
-                    const uint64_t k = A.keys[s];
-                    const uint8_t v = A.vals[s];
-                    w = (uint32_t)k;
-                    if (w != 0xFFFFFFFFu && v != 0 && w < A.n) {
-                        const uint32_t bit = 1u << (w & 31);
-                        if (!(A.visited[w >> 5] & bit)) {
-                            const uint32_t old = atomicOr(&A.visited[w >> 5], bit);
-                            fresh = !(old & bit);
-                        }
-                    }
+        uint32_t fresh = 0;
+        // Phase 1: each warp takes one frontier word at a time, lane l owning
+        // node 32*word + l. Short rows are walked as one concatenated slot
+        // range, 64 slots per step; long rows are queued as chunks.
+        for (uint32_t wi = gwarp; wi < words; wi += nwarps) {
+            const uint32_t f = front_cur[wi];
+            if (f == 0)
+                continue;
+            if (lane == 0)
+                front_cur[wi] = 0;  // cleared for its reuse two levels later
+            uint32_t b = 0, e = 0, len = 0;
+            if (f & (1u << lane)) {
+                const uint32_t u = (wi << 5) + lane;
+                b = A.ro[u];
+                e = min(A.ro[u + 1], A.size);
+                len = e > b ? e - b : 0;
+            }
+            uint32_t nch = len > BIG_ROW ? (len + CHUNK_SLOTS - 1) / CHUNK_SLOTS : 0;
+            const uint32_t ch_incl = warp_incl_scan(nch);
+            const uint32_t ch_total = __shfl_sync(0xFFFFFFFFu, ch_incl, 31);
+            if (ch_total) {
+                uint32_t base = 0;
+                if (lane == 0)
+                    base = atomicAdd(chunk_cnt, ch_total);
+                base = __shfl_sync(0xFFFFFFFFu, base, 0);
+                if (base + ch_total <= A.chunk_cap) {
+                    const uint32_t pos = base + ch_incl - nch;
+                    for (uint32_t c = 0; c < nch; ++c)
+                        A.chunks[pos + c] = make_uint2(b + c * CHUNK_SLOTS, min(e, b + (c + 1) * CHUNK_SLOTS));
+                    if (nch)
+                        len = 0;
+                } else {
+                    // list full: neutralise the claimed entries, walk the rows here
+                    for (uint32_t c = base + lane; c < min(base + ch_total, A.chunk_cap); c += 32)
+                        A.chunks[c] = make_uint2(0, 0);
                 }
-                const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, fresh);
-                if (ballot) {
-                    uint32_t basepos = 0;
-                    const int leader = __ffs(ballot) - 1;
-                    if ((int)lane == leader)
-                        basepos = atomicAdd(out_cnt, __popc(ballot));
-                    basepos = __shfl_sync(0xFFFFFFFFu, basepos, leader);
-                    if (fresh) {
-                        A.levels[w] = next_level;
-                        qout[basepos + __popc(ballot & lanemask_lt())] = w;
-                    }
-                    added += (lane == (uint32_t)leader) ? __popc(ballot) : 0;
-                }
+            }
+            const uint32_t incl = warp_incl_scan(len);
+            const uint32_t excl = incl - len;
+            const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            for (uint32_t p0 = 0; p0 < total; p0 += 64) {
+                const uint32_t sa = lb_slot(p0 + lane, total, b, excl);
+                const uint32_t sb = lb_slot(p0 + 32 + lane, total, b, excl);
+                fresh += visit_pair(A, sa, sb, next_level, front_next);
             }
         }
         if (!grid_barrier(bar, err))
             return;
+        // Phase 2: long-row chunks, one warp per chunk (64 slots = one step).
+        const uint32_t nch_all = min(ld_volatile(chunk_cnt), A.chunk_cap);
+        for (uint32_t c = gwarp; c < nch_all; c += nwarps) {
+            const uint2 ch = A.chunks[c];
+            for (uint32_t s0 = ch.x; s0 < ch.y; s0 += 64) {
+                const uint32_t sa = s0 + lane < ch.y ? s0 + lane : SIZE_NONE;
+                const uint32_t sb = s0 + 32 + lane < ch.y ? s0 + 32 + lane : SIZE_NONE;
+                fresh += visit_pair(A, sa, sb, next_level, front_next);
+            }
+        }
+        // nodes first reached this level: one atomic per warp
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1)
+            fresh += __shfl_xor_sync(0xFFFFFFFFu, fresh, d);
+        if (lane == 0 && fresh)
+            atomicAdd(A.ctl + CTL_CNT + (i + 1) % 3, fresh);
+        added += fresh;
+        if (!grid_barrier(bar, err))
+            return;
     }
-    if (added)
+    if (lane == 0 && added)
         atomicAdd(A.ctl + CTL_REACHED, added);
     if (blockIdx.x == 0 && threadIdx.x == 0)
         A.ctl[CTL_LEVELS] = i;
 }
 
-__global__ void bfs_init_kernel(uint32_t *levels, uint32_t *visited, uint32_t *q0, uint32_t *ctl, uint32_t src) {
+__global__ void bfs_init_kernel(uint32_t *levels, uint32_t *visited, uint32_t *front0, uint32_t *ctl, uint32_t src) {
     levels[src] = 1;
     visited[src >> 5] = 1u << (src & 31);
-    q0[0] = src;
+    front0[src >> 5] = 1u << (src & 31);
     ctl[CTL_CNT + 0] = 1;
     ctl[CTL_CNT + 1] = 0;
     ctl[CTL_CNT + 2] = 0;
@@ -234,8 +332,9 @@ gpma_status ensure_bfs(gpma_graph *g) {
     uint32_t n = std::max<uint32_t>(g->row_num, 1);
     GPMA_TRY(dev_alloc(&g->bfs_levels, n));
     GPMA_TRY(dev_alloc(&g->bfs_visited, n / 32 + 2));
-    GPMA_TRY(dev_alloc(&g->bfs_queue[0], n));
-    GPMA_TRY(dev_alloc(&g->bfs_queue[1], n));
+    GPMA_TRY(dev_alloc(&g->bfs_front[0], n / 32 + 2));
+    GPMA_TRY(dev_alloc(&g->bfs_front[1], n / 32 + 2));
+    GPMA_TRY(dev_alloc(&g->bfs_chunks, BFS_CHUNK_CAP));
     GPMA_TRY(dev_alloc(&g->bfs_ctl, CTL_WORDS + 2 * 64));
     if (!g->h_bfs_ctl) {
         cudaError_t e = cudaMallocHost((void **)&g->h_bfs_ctl, sizeof(uint32_t) * (CTL_WORDS + 2 * 64));
@@ -263,8 +362,9 @@ gpma_status ensure_bfs(gpma_graph *g) {
 void free_bfs(gpma_graph *g) {
     dev_free(g->bfs_levels);
     dev_free(g->bfs_visited);
-    dev_free(g->bfs_queue[0]);
-    dev_free(g->bfs_queue[1]);
+    dev_free(g->bfs_front[0]);
+    dev_free(g->bfs_front[1]);
+    dev_free(g->bfs_chunks);
     dev_free(g->bfs_ctl);
     for (int i = 0; i < 3; ++i)
         dev_free(g->msbfs_mask[i]);
@@ -282,7 +382,9 @@ gpma_status bfs_run(gpma_graph *g, uint32_t src, cudaStream_t s, uint64_t *reach
     GPMA_CUDA(cudaMemsetAsync(g->bfs_visited, 0, sizeof(uint32_t) * (n / 32 + 2), s));
     GPMA_CUDA(cudaMemsetAsync(g->bfs_ctl, 0, sizeof(uint32_t) * CTL_WORDS, s));
     prof_mark(g, 0, s);
-    bfs_init_kernel<<<1, 1, 0, s>>>(g->bfs_levels, g->bfs_visited, g->bfs_queue[0], g->bfs_ctl, src);
+    GPMA_CUDA(cudaMemsetAsync(g->bfs_front[0], 0, sizeof(uint32_t) * (n / 32 + 2), s));
+    GPMA_CUDA(cudaMemsetAsync(g->bfs_front[1], 0, sizeof(uint32_t) * (n / 32 + 2), s));
+    bfs_init_kernel<<<1, 1, 0, s>>>(g->bfs_levels, g->bfs_visited, g->bfs_front[0], g->bfs_ctl, src);
     BfsArgs A;
     A.keys = g->keys;
     A.vals = g->values;
@@ -291,8 +393,10 @@ gpma_status bfs_run(gpma_graph *g, uint32_t src, cudaStream_t s, uint64_t *reach
     A.size = g->geo.size;
     A.levels = g->bfs_levels;
     A.visited = g->bfs_visited;
-    A.q0 = g->bfs_queue[0];
-    A.q1 = g->bfs_queue[1];
+    A.front0 = g->bfs_front[0];
+    A.front1 = g->bfs_front[1];
+    A.chunks = g->bfs_chunks;
+    A.chunk_cap = BFS_CHUNK_CAP;
     A.ctl = g->bfs_ctl;
     void *params[] = {&A};
     GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)bfs_kernel, dim3(g->bfs_grid), dim3(BLOCK), params, 0, s));
@@ -369,14 +473,15 @@ gpma_status bfs_multi_run(gpma_graph *g, const uint32_t *d_src, uint32_t k, cuda
 // a host-side memory arena or a fixed device-memory budget, plug-ins whose
 // host process owns every cudaMalloc, or hosts whose pool forbids growth once
 // serving starts. For them gpma_bfs_noalloc keeps the BFS working set (visited
-// bitmap, two frontier queues, control words) in one file-scope device array
+// bitmap, two frontier bitmaps, big-row chunk list, control words) in one file-scope device array
 // of a fixed size instead of buffers allocated per graph. Every GPU that loads
-// this library holds the array (about 17 MB) until the process exits.
+// this library holds the array (about 1.3 MB) until the process exits.
 namespace {
 
 constexpr uint32_t NOALLOC_MAX_ROWS = 1u << 21;  // 2,097,152 nodes
-constexpr uint32_t NOALLOC_VISITED_WORDS = NOALLOC_MAX_ROWS / 32 + 2;
-constexpr size_t NOALLOC_WORDS = CTL_WORDS + NOALLOC_VISITED_WORDS + 2ull * NOALLOC_MAX_ROWS;
+constexpr uint32_t NOALLOC_BITMAP_WORDS = NOALLOC_MAX_ROWS / 32 + 2;
+constexpr uint32_t NOALLOC_CHUNK_CAP = 1u << 16;  // more big-row chunks are walked in place
+constexpr size_t NOALLOC_WORDS = CTL_WORDS + 3ull * NOALLOC_BITMAP_WORDS + 2ull * NOALLOC_CHUNK_CAP;
 constexpr int NOALLOC_MAX_DEVICES = 64;
 
 static __device__ __align__(256) uint32_t g_noalloc_scratch[NOALLOC_WORDS];
@@ -430,13 +535,16 @@ gpma_status bfs_noalloc_run(gpma_graph *g, uint32_t src, uint32_t *levels, uint6
     GPMA_TRY(noalloc_scratch(&scratch, &grid, g->sms));
     uint32_t *ctl = scratch;
     uint32_t *visited = scratch + CTL_WORDS;
-    uint32_t *q0 = visited + NOALLOC_VISITED_WORDS;
-    uint32_t *q1 = q0 + NOALLOC_MAX_ROWS;
+    uint32_t *front0 = visited + NOALLOC_BITMAP_WORDS;
+    uint32_t *front1 = front0 + NOALLOC_BITMAP_WORDS;
+    uint2 *chunks = reinterpret_cast<uint2 *>(front1 + NOALLOC_BITMAP_WORDS);
     // the scratch keeps the previous call's contents: clear what must start at zero
     GPMA_CUDA(cudaMemsetAsync(levels, 0, sizeof(uint32_t) * n, s));
     GPMA_CUDA(cudaMemsetAsync(visited, 0, sizeof(uint32_t) * (n / 32 + 2), s));
+    GPMA_CUDA(cudaMemsetAsync(front0, 0, sizeof(uint32_t) * (n / 32 + 2), s));
+    GPMA_CUDA(cudaMemsetAsync(front1, 0, sizeof(uint32_t) * (n / 32 + 2), s));
     GPMA_CUDA(cudaMemsetAsync(ctl, 0, sizeof(uint32_t) * CTL_WORDS, s));
-    bfs_init_kernel<<<1, 1, 0, s>>>(levels, visited, q0, ctl, src);
+    bfs_init_kernel<<<1, 1, 0, s>>>(levels, visited, front0, ctl, src);
     BfsArgs A;
     A.keys = g->keys;
     A.vals = g->values;
@@ -445,8 +553,10 @@ gpma_status bfs_noalloc_run(gpma_graph *g, uint32_t src, uint32_t *levels, uint6
     A.size = g->geo.size;
     A.levels = levels;
     A.visited = visited;
-    A.q0 = q0;
-    A.q1 = q1;
+    A.front0 = front0;
+    A.front1 = front1;
+    A.chunks = chunks;
+    A.chunk_cap = NOALLOC_CHUNK_CAP;
     A.ctl = ctl;
     void *params[] = {&A};
     GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)bfs_kernel, dim3(grid), dim3(BLOCK), params, 0, s));

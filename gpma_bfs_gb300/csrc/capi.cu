@@ -84,7 +84,6 @@ void release(gpma_graph *g) {
     dev_free(g->wlive);
     dev_free(g->sort_hist);
     dev_free(g->sort_base);
-    dev_free(g->sort_plan);
     dev_free(g->sort_tiles);
     dev_free(g->sort_status);
     dev_free(g->cta_cnt);
@@ -232,7 +231,6 @@ gpma_status gpma_create(uint32_t row_num, void *stream, gpma_graph **out) {
         GPMA_TRY(dev_alloc(&g->d_upper, 32));
         GPMA_TRY(dev_alloc(&g->sort_hist, 8 * 256));
         GPMA_TRY(dev_alloc(&g->sort_base, 8 * 256));
-        GPMA_TRY(dev_alloc(&g->sort_plan, 1));
         GPMA_TRY(dev_alloc(&g->sort_tiles, 8));
         GPMA_TRY(dev_alloc(&g->status, 1));
         cudaError_t e = cudaMallocHost((void **)&g->h_status, sizeof(DeviceStatus));

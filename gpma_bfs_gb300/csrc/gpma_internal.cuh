@@ -70,15 +70,6 @@ struct DeviceStatus {
     GridBarrier bar;
 };
 
-// Sort plan for one batch: which digit passes are trivial and where each
-// pass reads from.
-struct SortPlan {
-    uint32_t trivial[8];
-    uint32_t in_sel[8];   // ping-pong buffer read by pass p
-    uint32_t final_sel;   // buffer holding the sorted batch
-    uint32_t pad[7];
-};
-
 struct Geometry {
     uint32_t size = 0, seg = 0, height = 0;
     std::vector<uint32_t> lower, upper;
@@ -124,7 +115,6 @@ struct gpma_graph {
     // sort scratch
     uint32_t *sort_hist = nullptr;     // 8 * 256
     uint32_t *sort_base = nullptr;     // 8 * 256
-    gpma::SortPlan *sort_plan = nullptr;
     uint32_t *sort_tiles = nullptr;    // 8 tile counters
     uint32_t *sort_status = nullptr;   // 8 * tiles * 256 look-back words
     uint64_t sort_status_cap = 0;
@@ -135,8 +125,9 @@ struct gpma_graph {
     gpma::DeviceStatus *h_status = nullptr;  // pinned
     // BFS state
     uint32_t bfs_cap = 0;
-    uint32_t *bfs_visited = nullptr;   // row_num/32 + 1 words
-    uint32_t *bfs_queue[2] = {nullptr, nullptr};
+    uint32_t *bfs_visited = nullptr;   // row_num/32 + 2 words
+    uint32_t *bfs_front[2] = {nullptr, nullptr};  // frontier bitmaps, row_num/32 + 2 words
+    uint2 *bfs_chunks = nullptr;       // big-row chunk list
     uint32_t *bfs_levels = nullptr;
     uint32_t *bfs_ctl = nullptr;       // counters + status
     uint32_t *h_bfs_ctl = nullptr;     // pinned
@@ -214,7 +205,6 @@ inline double prof_elapsed(gpma_graph *g, int a, int b) {
 gpma_status ensure_batch(gpma_graph *g, uint64_t n);
 gpma_status ensure_scratch(gpma_graph *g, uint32_t slots);
 gpma_status upload_geometry(gpma_graph *g, cudaStream_t s);
-gpma_status sort_batch(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys);
 gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys = true);
 gpma_status bfs_run(gpma_graph *g, uint32_t src, cudaStream_t s, uint64_t *reached);
 gpma_status bfs_multi_run(gpma_graph *g, const uint32_t *d_src, uint32_t k, cudaStream_t s);

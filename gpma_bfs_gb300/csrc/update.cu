@@ -20,6 +20,7 @@
 // The host reads one status block at the end. Only the root resize
 // (:1034-1044) and the >= 5M-insertion rebuild (:936-966) run host-driven.
 #include "gpma_internal.cuh"
+#include "sort.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -66,9 +67,12 @@ struct UpdateArgs {
     uint32_t size, seg, log2seg, height;
     const uint32_t *lower;
     const uint32_t *upper;
-    const uint64_t *bk[2];
-    const uint8_t *bv[2];
-    const SortPlan *plan;
+    uint64_t *bk[2];  // batch, ping-pong buffers of the radix sort (input in [0])
+    uint8_t *bv[2];
+    uint32_t *sort_hist;    // 8 x 256 digit counts (zeroed per update)
+    uint32_t *sort_tiles;   // 8 tile counters (zeroed per update)
+    uint32_t *sort_status;  // look-back words, 8 x tiles x 256 (zeroed per update)
+    bool check_keys;
     uint32_t n;
     uint32_t *leaf;
     uint64_t *ikeys[2];
@@ -88,10 +92,24 @@ struct UpdateArgs {
 
 // ---- P1: locate ------------------------------------------------------------
 
-__device__ __forceinline__ uint32_t locate_one(const UpdateArgs &A, uint64_t key, uint8_t value) {
+// The top levels of the descent read segment first keys at multiples of
+// `stride` slots; each CTA copies those (at most LOCATE_CACHE of them) into
+// shared memory once, so a key walks the upper levels in shared memory and
+// only the last log2(stride/seg) levels in HBM. The comparisons and their
+// order are the reference's bit-by-bit descent (gpma.cuh:209-216).
+constexpr uint32_t LOCATE_CACHE = 4096;
+
+__device__ __forceinline__ uint32_t locate_one(const UpdateArgs &A, uint64_t key, uint8_t value, const uint64_t *fk,
+                                               uint32_t log2stride) {
     const uint32_t seg = A.seg;
+    const uint32_t stride = 1u << log2stride;
     uint32_t prefix = 0;
     uint32_t bit = (seg << A.height) >> 1;
+    while (stride <= bit) {
+        if (fk[(prefix | bit) >> log2stride] <= key)
+            prefix |= bit;
+        bit >>= 1;
+    }
     while (seg <= bit) {
         if (A.keys[prefix | bit] <= key)
             prefix |= bit;
@@ -197,23 +215,92 @@ __device__ void redispatch_chunk(uint64_t *keys, uint8_t *vals, uint32_t *row_of
     __syncthreads();
 }
 
-// ---- windows up to WARP_WINDOW_MAX slots: one group of min(W,32) lanes ------
+// ---- windows up to WARP_WINDOW_MAX slots: a group of lanes per window -------
+// K contiguous slots per lane (4, or 8 at 256 slots), loaded and stored with
+// 16-byte key and 4/8-byte value vectors; a W-slot window takes W/K lanes, so
+// a warp holds 32K/W windows at once.
+
+template <uint32_t K>
+__device__ __forceinline__ void load_slots(const uint64_t *keys, const uint8_t *vals, uint32_t t0, uint64_t (&k)[K],
+                                           uint8_t (&v)[K]) {
+    if constexpr (K >= 2) {
+#pragma unroll
+        for (uint32_t j = 0; j < K; j += 2) {
+            const ulonglong2 q = *reinterpret_cast<const ulonglong2 *>(keys + t0 + j);
+            k[j] = q.x;
+            k[j + 1] = q.y;
+        }
+    } else {
+        k[0] = keys[t0];
+    }
+    if constexpr (K == 8) {
+        const uint2 q = *reinterpret_cast<const uint2 *>(vals + t0);
+#pragma unroll
+        for (uint32_t j = 0; j < 4; ++j) {
+            v[j] = (uint8_t)(q.x >> (8 * j));
+            v[4 + j] = (uint8_t)(q.y >> (8 * j));
+        }
+    } else if constexpr (K == 4) {
+        const uint32_t q = *reinterpret_cast<const uint32_t *>(vals + t0);
+#pragma unroll
+        for (uint32_t j = 0; j < 4; ++j)
+            v[j] = (uint8_t)(q >> (8 * j));
+    } else if constexpr (K == 2) {
+        const uint16_t q = *reinterpret_cast<const uint16_t *>(vals + t0);
+        v[0] = (uint8_t)q;
+        v[1] = (uint8_t)(q >> 8);
+    } else {
+        v[0] = vals[t0];
+    }
+}
+
+template <uint32_t K>
+__device__ __forceinline__ void store_slots(uint64_t *keys, uint8_t *vals, uint32_t t0, const uint64_t (&k)[K],
+                                            const uint8_t (&v)[K]) {
+    if constexpr (K >= 2) {
+#pragma unroll
+        for (uint32_t j = 0; j < K; j += 2)
+            *reinterpret_cast<ulonglong2 *>(keys + t0 + j) = make_ulonglong2(k[j], k[j + 1]);
+    } else {
+        keys[t0] = k[0];
+    }
+    if constexpr (K == 8) {
+        uint2 q = make_uint2(0, 0);
+#pragma unroll
+        for (uint32_t j = 0; j < 4; ++j) {
+            q.x |= (uint32_t)v[j] << (8 * j);
+            q.y |= (uint32_t)v[4 + j] << (8 * j);
+        }
+        *reinterpret_cast<uint2 *>(vals + t0) = q;
+    } else if constexpr (K == 4) {
+        uint32_t q = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < 4; ++j)
+            q |= (uint32_t)v[j] << (8 * j);
+        *reinterpret_cast<uint32_t *>(vals + t0) = q;
+    } else if constexpr (K == 2) {
+        *reinterpret_cast<uint16_t *>(vals + t0) = (uint16_t)(v[0] | ((uint32_t)v[1] << 8));
+    } else {
+        vals[t0] = v[0];
+    }
+}
+
 template <uint32_t W>
 __device__ void warp_windows(const UpdateArgs &A, const uint32_t *wn, const uint32_t *wa, const uint32_t *wb,
                              uint32_t nw, uint32_t lo, uint32_t hi, const uint64_t *pk, const uint8_t *pv,
                              unsigned char *smem, unsigned long long &acc) {
-    constexpr uint32_t G = W < 32 ? W : 32;
-    constexpr uint32_t GPW = 32 / G;
-    constexpr uint32_t K = W / G;
+    constexpr uint32_t G = W >= 128 ? 32 : (W >= 4 ? W / 4 : 1);  // lanes per window
+    constexpr uint32_t GPW = 32 / G;                                // windows per warp
+    constexpr uint32_t K = W / G;                                   // slots per lane
     constexpr uint32_t STRIDE = (27 * W + 15) & ~15u;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t gl = lane % G, grp = lane / G;
     unsigned char *base = smem + (warp * GPW + grp) * STRIDE;
-    uint64_t *sk = reinterpret_cast<uint64_t *>(base);
-    uint64_t *ck = sk + W;
-    uint64_t *mk = ck + W;
-    uint8_t *sv = reinterpret_cast<uint8_t *>(mk + W);
-    uint8_t *cv = sv + W;
+    uint64_t *pend_k = reinterpret_cast<uint64_t *>(base);  // the window's pending insertions
+    uint64_t *ck = pend_k + W;                               // its live entries, compacted
+    uint64_t *mk = ck + W;                                   // the merge
+    uint8_t *pend_v = reinterpret_cast<uint8_t *>(mk + W);
+    uint8_t *cv = pend_v + W;
     uint8_t *mv = cv + W;
     const uint32_t seg_mask = A.seg - 1, log2seg = A.log2seg;
     const uint32_t log2F = (31 - __clz(W)) - log2seg;
@@ -222,22 +309,15 @@ __device__ void warp_windows(const UpdateArgs &A, const uint32_t *wn, const uint
         const uint32_t w = wbase + grp;
         const bool has = w < nw;
         const uint32_t node = has ? wn[w] : 0, a = has ? wa[w] : 0, b = has ? wb[w] : 0;
-        if (has) {
-#pragma unroll
-            for (uint32_t j = 0; j < K; ++j) {
-                uint32_t t = gl + j * G;
-                sk[t] = A.keys[node + t];
-                sv[t] = A.vals[node + t];
-            }
-        }
-        __syncwarp();
+        const uint32_t t0 = node + gl * K;
+        uint64_t k[K];
+        uint8_t v[K];
         uint32_t c_l = 0;
         if (has) {
+            load_slots<K>(A.keys, A.vals, t0, k, v);
 #pragma unroll
-            for (uint32_t j = 0; j < K; ++j) {
-                uint32_t t = gl * K + j;
-                c_l += (sk[t] != KEY_NONE && sv[t] != 0);
-            }
+            for (uint32_t j = 0; j < K; ++j)
+                c_l += (k[j] != KEY_NONE && v[j] != 0);
         }
         const uint32_t inc = warp_incl_scan(c_l, G);
         const uint32_t c = __shfl_sync(0xFFFFFFFFu, inc, grp * G + G - 1);
@@ -248,55 +328,50 @@ __device__ void warp_windows(const UpdateArgs &A, const uint32_t *wn, const uint
             uint32_t o = inc - c_l;
 #pragma unroll
             for (uint32_t j = 0; j < K; ++j) {
-                uint32_t t = gl * K + j;
-                if (sk[t] != KEY_NONE && sv[t] != 0) {
-                    ck[o] = sk[t];
-                    cv[o] = sv[t];
+                if (k[j] != KEY_NONE && v[j] != 0) {
+                    ck[o] = k[j];
+                    cv[o] = v[j];
                     ++o;
                 }
             }
-        }
-        __syncwarp();
-        if (accept) {
             for (uint32_t j = gl; j < p; j += G) {
-                sk[j] = pk[a + j];
-                sv[j] = pv[a + j];
+                pend_k[j] = pk[a + j];
+                pend_v[j] = pv[a + j];
             }
         }
         __syncwarp();
         if (accept) {
             for (uint32_t r = gl; r < c; r += G) {
-                uint32_t pos = r + lower_bound_u64(sk, p, ck[r]);
+                uint32_t pos = r + lower_bound_u64(pend_k, p, ck[r]);
                 mk[pos] = ck[r];
                 mv[pos] = cv[r];
             }
             for (uint32_t j = gl; j < p; j += G) {
-                uint32_t pos = j + upper_bound_u64(ck, c, sk[j]);
-                mk[pos] = sk[j];
-                mv[pos] = sv[j];
+                uint32_t pos = j + upper_bound_u64(ck, c, pend_k[j]);
+                mk[pos] = pend_k[j];
+                mv[pos] = pend_v[j];
             }
         }
         __syncwarp();
         if (accept) {
 #pragma unroll
             for (uint32_t j = 0; j < K; ++j) {
-                uint32_t t = gl + j * G;
-                uint32_t s = t >> log2seg, ln = t & seg_mask;
-                uint32_t f0 = (uint32_t)seg_first(s, M, log2F), f1 = (uint32_t)seg_first(s + 1, M, log2F);
-                uint64_t k = KEY_NONE;
-                uint8_t v = 0;
+                const uint32_t t = gl * K + j;
+                const uint32_t s = t >> log2seg, ln = t & seg_mask;
+                const uint32_t f0 = (uint32_t)seg_first(s, M, log2F), f1 = (uint32_t)seg_first(s + 1, M, log2F);
+                k[j] = KEY_NONE;
+                v[j] = 0;
                 if (ln < f1 - f0) {
-                    k = mk[f0 + ln];
-                    v = mv[f0 + ln];
+                    k[j] = mk[f0 + ln];
+                    v[j] = mv[f0 + ln];
                 }
-                A.keys[node + t] = k;
-                A.vals[node + t] = v;
-                if (is_guard(k)) {
-                    uint32_t row = (uint32_t)(k >> 32);
+                if (is_guard(k[j])) {
+                    const uint32_t row = (uint32_t)(k[j] >> 32);
                     if (row < A.row_num)
                         A.row_offset[row + 1] = node + t;
                 }
             }
+            store_slots<K>(A.keys, A.vals, t0, k, v);
             if (gl == 0)
                 ++acc;
         }
@@ -503,13 +578,51 @@ __device__ __forceinline__ void small_dispatch(const UpdateArgs &A, const uint32
         cta_windows<W>(A, wn, wa, wb, nw, lo, hi, pk, pv, smem, tmp, acc);
 }
 
-__global__ void __launch_bounds__(BLOCK) update_kernel(UpdateArgs A) {
+// Minimum resident CTAs per SM the register allocation must allow (build
+// option; 2 keeps every path spill-free).
+#ifndef GPMA_UPDATE_MIN_BLOCKS
+#define GPMA_UPDATE_MIN_BLOCKS 2
+#endif
+
+__global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(UpdateArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint32_t tmp[BLOCK / 32 + 1];
     DeviceStatus *st = A.st;
-    if (ld_volatile(&st->invalid_keys) != 0)
+
+    // S: stable radix sort of the batch (gpma.cuh:977); digit passes are
+    // separated by grid barriers, constant digits skipped.
+    sort_histogram(A.bk[0], A.n, A.sort_hist, st, A.check_keys, reinterpret_cast<uint32_t *>(smem));
+    if (!grid_barrier(&st->bar, &st->err))
         return;
-    const uint32_t sel = A.n ? A.plan->final_sel : 0;
+    if (ld_volatile(&st->invalid_keys) != 0)
+        return;  // reserved-column keys: reject the batch before any change
+    uint32_t sel = 0;
+    {
+        const uint32_t trivial = sort_trivial_mask(A.sort_hist, A.n);
+        const uint32_t tiles = (A.n + SORT_TILE - 1) / SORT_TILE;
+        __shared__ uint32_t s_tile;
+        for (int p = 0; p < 8; ++p) {
+            if (trivial & (1u << p))
+                continue;
+            const uint64_t *ink = sel ? A.bk[1] : A.bk[0];
+            const uint8_t *inv = sel ? A.bv[1] : A.bv[0];
+            uint64_t *outk = sel ? A.bk[0] : A.bk[1];
+            uint8_t *outv = sel ? A.bv[0] : A.bv[1];
+            for (;;) {
+                if (threadIdx.x == 0)
+                    s_tile = atomicAdd(&A.sort_tiles[p], 1u);
+                __syncthreads();
+                const uint32_t tile = s_tile;
+                __syncthreads();
+                if (tile >= tiles)
+                    break;
+                sort_tile(p, tile, ink, inv, outk, outv, A.n, A.sort_hist, A.sort_status, st, smem, tmp);
+            }
+            sel ^= 1u;
+            if (!grid_barrier(&st->bar, &st->err))
+                return;
+        }
+    }
     const uint64_t *bk = sel ? A.bk[1] : A.bk[0];
     const uint8_t *bv = sel ? A.bv[1] : A.bv[0];
     const uint32_t G = gridDim.x;
@@ -518,9 +631,21 @@ __global__ void __launch_bounds__(BLOCK) update_kernel(UpdateArgs A) {
 #define CNTI(id) ((id) ? A.cta_cnt + 3 * G : A.cta_cnt + 2 * G)
     unsigned long long acc = 0, acc_slots = 0;
 
-    // P1: locate every update, applying deletes / modifies in place.
-    for (uint32_t i = blockIdx.x * BLOCK + threadIdx.x; i < A.n; i += G * BLOCK)
-        A.leaf[i] = locate_one(A, bk[i], bv[i]);
+    // P1: locate every update, applying deletes / modifies in place. The top
+    // of the descent comes from a shared-memory copy of the first keys at
+    // every `stride`-th slot.
+    {
+        const uint32_t segs = A.size >> A.log2seg;
+        const uint32_t cached = segs < LOCATE_CACHE ? segs : LOCATE_CACHE;
+        const uint32_t log2stride = (31 - __clz(A.size / cached));
+        uint64_t *fk = reinterpret_cast<uint64_t *>(smem);
+        for (uint32_t j = threadIdx.x; j < cached; j += BLOCK)
+            fk[j] = A.keys[(size_t)j << log2stride];
+        __syncthreads();
+        for (uint32_t i = blockIdx.x * BLOCK + threadIdx.x; i < A.n; i += G * BLOCK)
+            A.leaf[i] = locate_one(A, bk[i], bv[i], fk, log2stride);
+        __syncthreads();
+    }
     if (!grid_barrier(&st->bar, &st->err))
         return;
 
@@ -1008,9 +1133,17 @@ gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_
         g->update_grid = g->sms * std::min(per_sm, 4);
         GPMA_TRY(dev_alloc(&g->cta_cnt, 4ull * g->update_grid));
     }
+    const uint32_t tiles = (uint32_t)((n + SORT_TILE - 1) / SORT_TILE);
+    const uint64_t status_words = 8ull * tiles * 256;
+    if (status_words > g->sort_status_cap) {
+        dev_free(g->sort_status);
+        GPMA_TRY(dev_alloc(&g->sort_status, status_words));
+        g->sort_status_cap = status_words;
+    }
     GPMA_CUDA(cudaMemsetAsync(g->status, 0, sizeof(DeviceStatus), s));
-    prof_mark(g, 0, s);
-    GPMA_TRY(sort_batch(g, n, s, check_keys));
+    GPMA_CUDA(cudaMemsetAsync(g->sort_hist, 0, 8 * 256 * sizeof(uint32_t), s));
+    GPMA_CUDA(cudaMemsetAsync(g->sort_tiles, 0, 8 * sizeof(uint32_t), s));
+    GPMA_CUDA(cudaMemsetAsync(g->sort_status, 0, status_words * sizeof(uint32_t), s));
     prof_mark(g, 1, s);
     UpdateArgs A;
     A.keys = g->keys;
@@ -1027,7 +1160,10 @@ gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_
     A.bk[1] = g->bkeys[1];
     A.bv[0] = g->bvals[0];
     A.bv[1] = g->bvals[1];
-    A.plan = g->sort_plan;
+    A.sort_hist = g->sort_hist;
+    A.sort_tiles = g->sort_tiles;
+    A.sort_status = g->sort_status;
+    A.check_keys = check_keys;
     A.n = (uint32_t)n;
     A.leaf = g->leaf;
     for (int i = 0; i < 2; ++i) {
@@ -1053,9 +1189,8 @@ gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_
     prof_mark(g, 2, s);
     GPMA_CUDA(cudaMemcpyAsync(g->h_status, g->status, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
     GPMA_CUDA(cudaStreamSynchronize(s));
-    g->prof.kernel_launches += 11;  // histogram, plan, 8 digit passes, update kernel
+    g->prof.kernel_launches += 1;  // the sort runs inside the update kernel
     g->prof.update_kernels++;
-    g->prof.sort_ms += prof_elapsed(g, 0, 1);
     g->prof.update_kernel_ms += prof_elapsed(g, 1, 2);
     const DeviceStatus &h = *g->h_status;
     if (h.invalid_keys) {

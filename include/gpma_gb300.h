@@ -104,8 +104,9 @@ GPMA_API gpma_status gpma_bfs_multi(gpma_graph *g, const uint32_t *srcs, uint32_
  * fixed device budget owns every allocation, or allocation is forbidden
  * while serving). No counterpart in the reference. Same result as gpma_bfs,
  * but it allocates nothing: its working set (visited bitmap, two frontier
- * queues, control words) is one fixed device array inside the library, about
- * 17 MB, held by every GPU that loads the library until the process exits.
+ * bitmaps, big-row chunk list, control words) is one fixed device array inside
+ * the library, about 1.3 MB, held by every GPU that loads the library until
+ * the process exits.
  * Limits: row_num <= 2,097,152 (GPMA_ERR_CAPACITY beyond); levels must be
  * device memory of row_num entries (GPMA_ERR_INVALID otherwise); reached is an
  * optional host pointer. The first call on a device looks up the array's
