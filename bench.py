@@ -292,8 +292,11 @@ def run_gpu(args):
             "clocks": clk.summary(),
             "bfs": {"before": bfs_before, "after": bfs_after, "unit": "GTEPS",
                     "gteps": bfs_after["gteps"]},
-            "phases_ms_per_step": {"sort": prof["sort_ms"] / args.steps,
-                                   "update_kernel": prof["update_kernel_ms"] / args.steps,
+            "phases_ms_per_step": {"update_kernel": prof["update_kernel_ms"] / args.steps,
+                                   "in_kernel_sort": prof["sort_ms"] / args.steps,
+                                   "in_kernel_locate": prof["locate_ms"] / args.steps,
+                                   "in_kernel_group": prof["group_ms"] / args.steps,
+                                   "in_kernel_levels": prof["levels_ms"] / args.steps,
                                    "root_rebuild": prof["rebuild_ms"] / args.steps},
             "levels_per_step": (st1["levels_visited"] - st0["levels_visited"]) / args.steps,
             "setup_s": {"generate": gen_s},

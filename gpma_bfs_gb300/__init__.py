@@ -59,9 +59,10 @@ class _Stats(ctypes.Structure):
 
 
 class _Profile(ctypes.Structure):
-    _fields_ = [("sort_ms", ctypes.c_double), ("update_kernel_ms", ctypes.c_double), ("rebuild_ms", ctypes.c_double),
+    _fields_ = [("sort_ms", ctypes.c_double), ("locate_ms", ctypes.c_double), ("group_ms", ctypes.c_double),
+                ("levels_ms", ctypes.c_double), ("update_kernel_ms", ctypes.c_double), ("rebuild_ms", ctypes.c_double),
                 ("bfs_ms", ctypes.c_double), ("update_kernels", ctypes.c_uint64), ("bfs_kernels", ctypes.c_uint64),
-                ("kernel_launches", ctypes.c_uint64)]
+                ("kernel_launches", ctypes.c_uint64), ("bfs_edges", ctypes.c_uint64)]
 
 
 _lib = None
@@ -90,6 +91,13 @@ def lib() -> ctypes.CDLL:
         "gpma_export_compact": (st, [P, P, u64, ctypes.POINTER(u64), P]),
         "gpma_device_arrays": (st, [P, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P)]),
         "gpma_get_stats": (st, [P, ctypes.POINTER(_Stats)]),
+        "gpma_batch_create": (st, [ctypes.POINTER(P)]),
+        "gpma_batch_destroy": (st, [P]),
+        "gpma_batch_update": (st, [P, P, P, P, P, u32, P]),
+        "gpma_batch_bfs_multi": (st, [P, P, P, P, u32, P, P, P]),
+        "gpma_batch_set_profiling": (st, [P, ctypes.c_int]),
+        "gpma_batch_get_profile": (st, [P, ctypes.POINTER(_Profile)]),
+        "gpma_batch_reset_profile": (st, [P]),
         "gpma_set_profiling": (st, [P, ctypes.c_int]),
         "gpma_get_profile": (st, [P, ctypes.POINTER(_Profile)]),
         "gpma_reset_profile": (st, [P]),
@@ -369,3 +377,78 @@ def read_edges_text(path: str):
     _check(lib().gpma_read_edges_text(str(path).encode(), ctypes.byref(n), ctypes.byref(m), src.ctypes.data,
                                       dst.ctypes.data, m.value), "gpma_read_edges_text")
     return n.value, src, dst
+
+
+class Batch:
+    """Many graphs per launch (no reference counterpart).
+
+    ``update(graphs, keys, values)`` applies one batch per graph in a single
+    persistent kernel launch; ``bfs_multi(graphs, sources)`` runs up to 64
+    searches per graph for all graphs in one launch.
+    """
+
+    def __init__(self):
+        h = ctypes.c_void_p()
+        _check(lib().gpma_batch_create(ctypes.byref(h)), "gpma_batch_create")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().gpma_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def update(self, graphs, keys, values, stream=None) -> None:
+        k = len(graphs)
+        if not (len(keys) == len(values) == k):
+            raise ValueError("one key array and one value array per graph")
+        keep = []
+        kp, vp, cnt = (ctypes.c_void_p * k)(), (ctypes.c_void_p * k)(), (ctypes.c_uint64 * k)()
+        hs = (ctypes.c_void_p * k)()
+        for i, (g, kk, vv) in enumerate(zip(graphs, keys, values)):
+            if len(kk) != len(vv):
+                raise ValueError("Inconsistant kv size.")
+            if isinstance(kk, np.ndarray):
+                kk = np.ascontiguousarray(kk, dtype=np.uint64)
+            if isinstance(vv, np.ndarray):
+                vv = np.ascontiguousarray(vv).view(np.uint8) if vv.dtype.itemsize == 1 \
+                    else np.ascontiguousarray(vv, dtype=np.uint8)
+            a, ka = _ptr(kk)
+            b, kb = _ptr(vv)
+            keep += [ka, kb]
+            kp[i], vp[i], cnt[i], hs[i] = a, b, len(kk), g.handle.value
+        _check(lib().gpma_batch_update(self._h, hs, kp, vp, cnt, k, _stream_ptr(stream)), "gpma_batch_update")
+
+    def bfs_multi(self, graphs, sources, levels: bool = False, stream=None):
+        """(levels per graph or None, reached per graph) for up to 64 sources per graph."""
+        k = len(graphs)
+        srcs = [np.ascontiguousarray(np.asarray(s, np.uint32)) for s in sources]
+        hs = (ctypes.c_void_p * k)(*[g.handle.value for g in graphs])
+        sp = (ctypes.c_void_p * k)(*[s.ctypes.data for s in srcs])
+        ns = (ctypes.c_uint32 * k)(*[len(s) for s in srcs])
+        outs = [np.zeros((len(s), g.row_num), np.uint32) for s, g in zip(srcs, graphs)] if levels else None
+        lp = (ctypes.c_void_p * k)(*[o.ctypes.data for o in outs]) if levels else None
+        reached = np.zeros(sum(len(s) for s in srcs), np.uint64)
+        _check(lib().gpma_batch_bfs_multi(self._h, hs, sp, ns, k, lp, reached.ctypes.data, _stream_ptr(stream)),
+               "gpma_batch_bfs_multi")
+        parts, o = [], 0
+        for s in srcs:
+            parts.append(reached[o:o + len(s)])
+            o += len(s)
+        return outs, parts
+
+    def set_profiling(self, enabled: bool = True) -> None:
+        _check(lib().gpma_batch_set_profiling(self._h, int(bool(enabled))), "gpma_batch_set_profiling")
+
+    def profile(self) -> dict:
+        p = _Profile()
+        _check(lib().gpma_batch_get_profile(self._h, ctypes.byref(p)), "gpma_batch_get_profile")
+        return {name: getattr(p, name) for name, _ in _Profile._fields_}
+
+    def reset_profile(self) -> None:
+        _check(lib().gpma_batch_reset_profile(self._h), "gpma_batch_reset_profile")

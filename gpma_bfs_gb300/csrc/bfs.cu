@@ -18,11 +18,6 @@
 // atomicOr on the visited bitmap (a plain load filters visited targets first)
 // and enters the next frontier bitmap.
 //
-// Multi-source (k <= 64): one bit lane per source in 64-bit masks
-// (visited, frontier, next); per level a warp takes 32 nodes, and for each
-// node with a non-empty frontier mask the whole warp scans its row and ORs
-// the mask into next[w]; a second sweep turns next into the new frontier and
-// writes levels for each newly set lane.
 #include "gpma_internal.cuh"
 
 #include <algorithm>
@@ -221,110 +216,6 @@ __global__ void bfs_init_kernel(uint32_t *levels, uint32_t *visited, uint32_t *f
     ctl[CTL_REACHED] = 1;
 }
 
-// ---- multi-source ----------------------------------------------------------
-
-struct MsArgs {
-    const uint64_t *keys;
-    const uint8_t *vals;
-    const uint32_t *ro;
-    uint32_t n, size, k;
-    const uint32_t *src;
-    uint64_t *visited;
-    uint64_t *frontier;
-    uint64_t *next;
-    uint32_t *levels;  // [k][n]
-    uint32_t *ctl;
-};
-
-__global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
-    GridBarrier *bar = reinterpret_cast<GridBarrier *>(A.ctl + CTL_BAR);
-    uint32_t *err = A.ctl + CTL_ERR;
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t gwarp = blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5);
-    const uint32_t nwarps = gridDim.x * (BLOCK / 32);
-    const uint32_t gtid = blockIdx.x * BLOCK + threadIdx.x;
-    const uint32_t nthreads = gridDim.x * BLOCK;
-    // init: masks cleared by the host; seed the sources
-    if (gtid < A.k) {
-        uint32_t s = A.src[gtid];
-        atomicOr((unsigned long long *)&A.visited[s], 1ull << gtid);
-        atomicOr((unsigned long long *)&A.frontier[s], 1ull << gtid);
-        A.levels[(uint64_t)gtid * A.n + s] = 1;
-    }
-    if (!grid_barrier(bar, err))
-        return;
-    uint32_t level = 1;
-    for (;; ++level) {
-        // expand: every node with a frontier mask pushes it to its targets
-        for (uint32_t base = gwarp * 32; base < A.n; base += nwarps * 32) {
-            const uint32_t u = base + lane;
-            const uint64_t f = u < A.n ? A.frontier[u] : 0ull;
-            uint32_t todo = __ballot_sync(0xFFFFFFFFu, f != 0ull);
-            while (todo) {
-                const int src_lane = __ffs(todo) - 1;
-                todo &= todo - 1;
-                const uint32_t uu = base + src_lane;
-                const uint64_t fm = __shfl_sync(0xFFFFFFFFu, f, src_lane);
-                const uint32_t b = A.ro[uu], e = min(A.ro[uu + 1], A.size);
-                for (uint32_t s = b + lane; s < e; s += 32) {
-                    const uint64_t key = A.keys[s];
-                    const uint32_t w = (uint32_t)key;
-                    if (w == 0xFFFFFFFFu || A.vals[s] == 0 || w >= A.n)
-                        continue;
-                    const uint64_t nb = fm & ~A.visited[w];
-                    if (nb && (A.next[w] & nb) != nb)
-                        atomicOr((unsigned long long *)&A.next[w], nb);
-                }
-            }
-        }
-        if (!grid_barrier(bar, err))
-            return;
-        // commit: next -> frontier, record levels of newly reached lanes
-        uint32_t changed = 0;
-        for (uint32_t w = gtid; w < A.n; w += nthreads) {
-            const uint64_t nx = A.next[w] & ~A.visited[w];
-            A.frontier[w] = nx;
-            if (nx) {
-                A.next[w] = 0;
-                A.visited[w] |= nx;
-                uint64_t m = nx;
-                while (m) {
-                    const int bit = __ffsll((long long)m) - 1;
-                    m &= m - 1;
-                    A.levels[(uint64_t)bit * A.n + w] = level + 1;
-                }
-                changed = 1;
-            } else if (A.next[w]) {
-                A.next[w] = 0;
-            }
-        }
-        const uint32_t any = __syncthreads_or(changed);
-        if (any && threadIdx.x == 0)
-            atomicAdd(A.ctl + CTL_CNT + (level % 3), 1u);
-        if (blockIdx.x == 0 && threadIdx.x == 0)
-            A.ctl[CTL_CNT + ((level + 1) % 3)] = 0;
-        if (!grid_barrier(bar, err))
-            return;
-        if (ld_volatile(A.ctl + CTL_CNT + (level % 3)) == 0)
-            break;
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        A.ctl[CTL_LEVELS] = level;
-}
-
-// reached[i] = number of non-zero entries of levels[i][0..n)
-__global__ void count_reached_kernel(const uint32_t *levels, uint32_t n, uint32_t k, unsigned long long *reached) {
-    __shared__ uint32_t tmp[BLOCK / 32 + 1];
-    for (uint32_t i = 0; i < k; ++i) {
-        uint32_t c = 0;
-        for (uint32_t w = blockIdx.x * BLOCK + threadIdx.x; w < n; w += gridDim.x * BLOCK)
-            c += levels[(uint64_t)i * n + w] != 0;
-        uint32_t t = block_sum(c, tmp);
-        if (threadIdx.x == 0 && t)
-            atomicAdd(&reached[i], (unsigned long long)t);
-    }
-}
-
 gpma_status ensure_bfs(gpma_graph *g) {
     if (g->bfs_cap >= g->row_num && g->bfs_levels)
         return GPMA_OK;
@@ -345,9 +236,6 @@ gpma_status ensure_bfs(gpma_graph *g) {
     if (g->bfs_grid == 0) {
         int per_sm = 0;
         GPMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bfs_kernel, BLOCK, 0));
-        int per_sm2 = 0;
-        GPMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, msbfs_kernel, BLOCK, 0));
-        per_sm = std::min(per_sm, per_sm2);
         if (per_sm < 1) {
             set_error("BFS kernel cannot be resident (occupancy 0)");
             return GPMA_ERR_CUDA;
@@ -366,11 +254,6 @@ void free_bfs(gpma_graph *g) {
     dev_free(g->bfs_front[1]);
     dev_free(g->bfs_chunks);
     dev_free(g->bfs_ctl);
-    for (int i = 0; i < 3; ++i)
-        dev_free(g->msbfs_mask[i]);
-    dev_free(g->msbfs_levels);
-    dev_free(g->msbfs_src);
-    g->msbfs_levels_cap = 0;
     g->bfs_cap = 0;
 }
 
@@ -412,59 +295,6 @@ gpma_status bfs_run(gpma_graph *g, uint32_t src, cudaStream_t s, uint64_t *reach
     }
     if (reached)
         *reached = g->h_bfs_ctl[CTL_REACHED];
-    return GPMA_OK;
-}
-
-// Levels land in g->msbfs_levels ([k][n]); reached counts in the tail of
-// bfs_ctl (read back by the caller).
-gpma_status bfs_multi_run(gpma_graph *g, const uint32_t *d_src, uint32_t k, cudaStream_t s) {
-    GPMA_TRY(ensure_bfs(g));
-    const uint32_t n = g->row_num;
-    if (!g->msbfs_mask[0]) {
-        for (int i = 0; i < 3; ++i)
-            GPMA_TRY(dev_alloc(&g->msbfs_mask[i], std::max<uint32_t>(n, 1)));
-    }
-    const uint64_t need = (uint64_t)k * n;
-    if (need > g->msbfs_levels_cap) {
-        dev_free(g->msbfs_levels);
-        GPMA_TRY(dev_alloc(&g->msbfs_levels, need));
-        g->msbfs_levels_cap = need;
-    }
-    for (int i = 0; i < 3; ++i)
-        GPMA_CUDA(cudaMemsetAsync(g->msbfs_mask[i], 0, sizeof(uint64_t) * n, s));
-    GPMA_CUDA(cudaMemsetAsync(g->msbfs_levels, 0, sizeof(uint32_t) * need, s));
-    GPMA_CUDA(cudaMemsetAsync(g->bfs_ctl, 0, sizeof(uint32_t) * (CTL_WORDS + 2 * 64), s));
-    MsArgs A;
-    A.keys = g->keys;
-    A.vals = g->values;
-    A.ro = g->row_offset;
-    A.n = n;
-    A.size = g->geo.size;
-    A.k = k;
-    A.src = d_src;
-    A.visited = g->msbfs_mask[0];
-    A.frontier = g->msbfs_mask[1];
-    A.next = g->msbfs_mask[2];
-    A.levels = g->msbfs_levels;
-    A.ctl = g->bfs_ctl;
-    void *params[] = {&A};
-    prof_mark(g, 0, s);
-    GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)msbfs_kernel, dim3(g->bfs_grid), dim3(BLOCK), params, 0, s));
-    prof_mark(g, 1, s);
-    unsigned long long *reached = reinterpret_cast<unsigned long long *>(g->bfs_ctl + CTL_WORDS);
-    count_reached_kernel<<<std::max(1, std::min(g->sms * 4, (int)((n + BLOCK - 1) / BLOCK))), BLOCK, 0, s>>>(
-        g->msbfs_levels, n, k, reached);
-    GPMA_CUDA(cudaGetLastError());
-    GPMA_CUDA(cudaMemcpyAsync(g->h_bfs_ctl, g->bfs_ctl, sizeof(uint32_t) * (CTL_WORDS + 2 * 64),
-                              cudaMemcpyDeviceToHost, s));
-    GPMA_CUDA(cudaStreamSynchronize(s));
-    g->prof.kernel_launches += 2;
-    g->prof.bfs_kernels++;
-    g->prof.bfs_ms += prof_elapsed(g, 0, 1);
-    if (g->h_bfs_ctl[CTL_ERR]) {
-        set_error("device-side wait gave up in the multi-source BFS kernel (code %u)", g->h_bfs_ctl[CTL_ERR]);
-        return GPMA_ERR_TIMEOUT;
-    }
     return GPMA_OK;
 }
 

@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 namespace gpma {
 
@@ -62,36 +63,14 @@ void release(gpma_graph *g) {
     dev_free(g->keys);
     dev_free(g->values);
     dev_free(g->row_offset);
-    dev_free(g->d_lower);
-    dev_free(g->d_upper);
     dev_free(g->skeys);
     dev_free(g->svals);
     dev_free(g->chunk_cnt);
-    for (int i = 0; i < 2; ++i) {
-        dev_free(g->bkeys[i]);
-        dev_free(g->bvals[i]);
-        dev_free(g->wnode[i]);
-        dev_free(g->wa[i]);
-        dev_free(g->wb[i]);
-    }
-    dev_free(g->leaf);
-    for (int i = 0; i < 2; ++i) {
-        dev_free(g->ikeys[i]);
-        dev_free(g->ivals[i]);
-    }
-    dev_free(g->ileaf);
-    dev_free(g->wflag);
-    dev_free(g->wlive);
-    dev_free(g->sort_hist);
-    dev_free(g->sort_base);
-    dev_free(g->sort_tiles);
-    dev_free(g->sort_status);
-    dev_free(g->cta_cnt);
-    dev_free(g->status);
-    if (g->h_status)
-        cudaFreeHost(g->h_status);
-    g->h_status = nullptr;
+    free_buffers(g->buf);
     free_bfs(g);
+    if (g->own_batch)
+        gpma_batch_destroy(g->own_batch);
+    g->own_batch = nullptr;
     for (auto &e : g->ev)
         if (e)
             cudaEventDestroy(e);
@@ -227,15 +206,6 @@ gpma_status gpma_create(uint32_t row_num, void *stream, gpma_graph **out) {
         GPMA_TRY(dev_alloc(&g->keys, 4));
         GPMA_TRY(dev_alloc(&g->values, 4));
         GPMA_TRY(dev_alloc(&g->row_offset, (uint64_t)row_num + 1));
-        GPMA_TRY(dev_alloc(&g->d_lower, 32));
-        GPMA_TRY(dev_alloc(&g->d_upper, 32));
-        GPMA_TRY(dev_alloc(&g->sort_hist, 8 * 256));
-        GPMA_TRY(dev_alloc(&g->sort_base, 8 * 256));
-        GPMA_TRY(dev_alloc(&g->sort_tiles, 8));
-        GPMA_TRY(dev_alloc(&g->status, 1));
-        cudaError_t e = cudaMallocHost((void **)&g->h_status, sizeof(DeviceStatus));
-        if (e != cudaSuccess)
-            return cuda_fail(e, "cudaMallocHost(status)");
         GPMA_TRY(ensure_scratch(g, 4));
         GPMA_CUDA(cudaMemsetAsync(g->row_offset, 0, sizeof(uint32_t) * ((uint64_t)row_num + 1), s));
         init_layout_kernel<<<1, 32, 0, s>>>(g->keys, g->values);
@@ -244,11 +214,10 @@ gpma_status gpma_create(uint32_t row_num, void *stream, gpma_graph **out) {
         g->geo.seg = 2;
         g->geo.height = 1;
         recalculate_density(g->geo);
-        GPMA_TRY(upload_geometry(g, s));
         if (row_num == 0)
             return GPMA_OK;
-        GPMA_TRY(ensure_batch(g, row_num));
-        guard_keys_kernel<<<small_grid(row_num, g->sms), BLOCK, 0, s>>>(g->bkeys[0], g->bvals[0], row_num);
+        GPMA_TRY(ensure_buffers(g->buf, row_num, 1));
+        guard_keys_kernel<<<small_grid(row_num, g->sms), BLOCK, 0, s>>>(g->buf.bkeys[0], g->buf.bvals[0], row_num);
         GPMA_CUDA(cudaGetLastError());
         return update_device(g, row_num, s, /*check_keys=*/false);  // the guards use the reserved column
     }();
@@ -286,9 +255,9 @@ gpma_status gpma_update(gpma_graph *g, const uint64_t *keys, const uint8_t *valu
     if (n == 0)
         return GPMA_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    GPMA_TRY(ensure_batch(g, n));
-    GPMA_TRY(copy_in(g, g->bkeys[0], keys, n * sizeof(uint64_t), s));
-    GPMA_TRY(copy_in(g, g->bvals[0], values, n, s));
+    GPMA_TRY(ensure_buffers(g->buf, n, 1));
+    GPMA_TRY(copy_in(g, g->buf.bkeys[0], keys, n * sizeof(uint64_t), s));
+    GPMA_TRY(copy_in(g, g->buf.bvals[0], values, n, s));
     return update_device(g, n, s);
 }
 
@@ -340,17 +309,191 @@ gpma_status gpma_bfs_multi(gpma_graph *g, const uint32_t *srcs, uint32_t k, uint
             return GPMA_ERR_INVALID;
         }
     }
-    if (!g->msbfs_src)
-        GPMA_TRY(dev_alloc(&g->msbfs_src, 64));
-    GPMA_CUDA(cudaMemcpyAsync(g->msbfs_src, hs, sizeof(uint32_t) * k, cudaMemcpyHostToDevice, s));
-    GPMA_TRY(bfs_multi_run(g, g->msbfs_src, k, s));
-    GPMA_TRY(copy_any(levels, g->msbfs_levels, sizeof(uint32_t) * (uint64_t)k * g->row_num, s));
-    GPMA_CUDA(cudaStreamSynchronize(s));
-    if (reached) {
-        const unsigned long long *r = reinterpret_cast<const unsigned long long *>(g->h_bfs_ctl + 16);
-        for (uint32_t i = 0; i < k; ++i)
-            reached[i] = r[i];
+    if (!g->own_batch)
+        GPMA_TRY(gpma_batch_create(&g->own_batch));
+    gpma_graph *gl[1] = {g};
+    const uint32_t *sl[1] = {hs};
+    uint32_t *ll[1] = {levels};
+    const uint32_t nl[1] = {k};
+    g->own_batch->profiling = g->profiling;
+    if (g->profiling && !g->own_batch->ev[0])
+        for (auto &e : g->own_batch->ev)
+            GPMA_CUDA(cudaEventCreate(&e));
+    const gpma_profile before = g->own_batch->prof;
+    GPMA_TRY(batch_bfs_run(g->own_batch, gl, sl, nl, 1, ll, reached, s));
+    const gpma_profile &after = g->own_batch->prof;
+    g->prof.bfs_ms += after.bfs_ms - before.bfs_ms;
+    g->prof.bfs_kernels += after.bfs_kernels - before.bfs_kernels;
+    g->prof.kernel_launches += after.kernel_launches - before.kernel_launches;
+    g->prof.bfs_edges += after.bfs_edges - before.bfs_edges;
+    return GPMA_OK;
+}
+
+// ---- many graphs per launch ---------------------------------------------------
+
+gpma_status gpma_batch_create(gpma_batch **out) {
+    if (!out) {
+        set_error("gpma_batch_create: out is NULL");
+        return GPMA_ERR_INVALID;
     }
+    gpma_batch *b = new (std::nothrow) gpma_batch();
+    if (!b) {
+        set_error("gpma_batch_create: host allocation failed");
+        return GPMA_ERR_NOMEM;
+    }
+    cudaError_t e = cudaGetDevice(&b->device);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
+    if (e != cudaSuccess) {
+        delete b;
+        return cuda_fail(e, "gpma_batch_create");
+    }
+    *out = b;
+    return GPMA_OK;
+}
+
+gpma_status gpma_batch_destroy(gpma_batch *b) {
+    if (!b)
+        return GPMA_OK;
+    cudaDeviceSynchronize();
+    free_buffers(b->buf);
+    free_batch_bfs(b);
+    for (auto &e : b->ev)
+        if (e)
+            cudaEventDestroy(e);
+    delete b;
+    return GPMA_OK;
+}
+
+gpma_status gpma_batch_update(gpma_batch *b, gpma_graph *const *graphs, const uint64_t *const *keys,
+                              const uint8_t *const *values, const uint64_t *counts, uint32_t k, void *stream) {
+    if (!b || (k && (!graphs || !keys || !values || !counts))) {
+        set_error("gpma_batch_update: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<uint32_t> order;
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < k; ++i) {
+        if (!graphs[i] || (counts[i] && (!keys[i] || !values[i]))) {
+            set_error("gpma_batch_update: null graph or batch %u", i);
+            return GPMA_ERR_INVALID;
+        }
+        for (uint32_t j = 0; j < i; ++j)
+            if (graphs[j] == graphs[i]) {
+                set_error("gpma_batch_update: graph %u appears twice", i);
+                return GPMA_ERR_INVALID;
+            }
+        if (counts[i] >= (1ull << 30)) {
+            set_error("gpma_batch_update: batch %u of %llu keys exceeds 2^30", i, (unsigned long long)counts[i]);
+            return GPMA_ERR_CAPACITY;
+        }
+    }
+    for (uint32_t i = 0; i < k; ++i) {
+        graphs[i]->stats.updates++;
+        graphs[i]->stats.submitted += counts[i];
+        if (counts[i] == 0)
+            continue;
+        if (counts[i] >= SIGNIFICANT_INSERTS) {
+            // a possible bulk rebuild: the single-graph path, on the graph's own buffers
+            GPMA_TRY(ensure_buffers(graphs[i]->buf, counts[i], 1));
+            GPMA_TRY(copy_in(graphs[i], graphs[i]->buf.bkeys[0], keys[i], counts[i] * sizeof(uint64_t), s));
+            GPMA_TRY(copy_in(graphs[i], graphs[i]->buf.bvals[0], values[i], counts[i], s));
+            GPMA_TRY(update_device(graphs[i], counts[i], s));
+            continue;
+        }
+        order.push_back(i);
+        total += counts[i];
+    }
+    if (order.empty())
+        return GPMA_OK;
+    if (total >= (1ull << 31)) {
+        set_error("gpma_batch_update: %llu keys in one call exceed 2^31", (unsigned long long)total);
+        return GPMA_ERR_CAPACITY;
+    }
+    // the kernel wants graphs ordered by segment length
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint32_t x, uint32_t y) { return graphs[x]->geo.seg < graphs[y]->geo.seg; });
+    GPMA_TRY(ensure_buffers(b->buf, total, (uint32_t)order.size()));
+    std::vector<gpma_graph *> gs(order.size());
+    std::vector<uint64_t> off(order.size() + 1, 0);
+    for (size_t j = 0; j < order.size(); ++j) {
+        const uint32_t i = order[j];
+        gs[j] = graphs[i];
+        off[j + 1] = off[j] + counts[i];
+        GPMA_TRY(copy_in(graphs[i], b->buf.bkeys[0] + off[j], keys[i], counts[i] * sizeof(uint64_t), s));
+        GPMA_TRY(copy_in(graphs[i], b->buf.bvals[0] + off[j], values[i], counts[i], s));
+    }
+    return update_graphs(gs.data(), off.data(), (uint32_t)gs.size(), b->buf, b->sms, s, true, b->profiling, b->ev,
+                         &b->prof);
+}
+
+gpma_status gpma_batch_bfs_multi(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs,
+                                 const uint32_t *nsrc, uint32_t k, uint32_t *const *levels, uint64_t *reached,
+                                 void *stream) {
+    if (!b || (k && (!graphs || !srcs || !nsrc))) {
+        set_error("gpma_batch_bfs_multi: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    if (k == 0)
+        return GPMA_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<std::vector<uint32_t>> hs(k);
+    std::vector<const uint32_t *> hp(k);
+    uint64_t nodes = 0;
+    for (uint32_t i = 0; i < k; ++i) {
+        if (!graphs[i] || !srcs[i] || nsrc[i] == 0 || nsrc[i] > 64) {
+            set_error("gpma_batch_bfs_multi: graph %u: null pointer or source count not in 1..64", i);
+            return GPMA_ERR_INVALID;
+        }
+        hs[i].resize(nsrc[i]);
+        GPMA_TRY(copy_any(hs[i].data(), srcs[i], sizeof(uint32_t) * nsrc[i], s));
+        nodes += graphs[i]->row_num;
+    }
+    GPMA_CUDA(cudaStreamSynchronize(s));
+    if (nodes >= (1ull << 32)) {
+        set_error("gpma_batch_bfs_multi: %llu nodes in one call exceed 2^32", (unsigned long long)nodes);
+        return GPMA_ERR_CAPACITY;
+    }
+    for (uint32_t i = 0; i < k; ++i) {
+        for (uint32_t v : hs[i])
+            if (v >= graphs[i]->row_num) {
+                set_error("gpma_batch_bfs_multi: graph %u: source %u out of range (row_num %u)", i, v,
+                          graphs[i]->row_num);
+                return GPMA_ERR_INVALID;
+            }
+        hp[i] = hs[i].data();
+    }
+    return batch_bfs_run(b, graphs, hp.data(), nsrc, k, levels, reached, s);
+}
+
+gpma_status gpma_batch_set_profiling(gpma_batch *b, int enabled) {
+    if (!b) {
+        set_error("gpma_batch_set_profiling: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    if (enabled && !b->ev[0])
+        for (auto &e : b->ev)
+            GPMA_CUDA(cudaEventCreate(&e));
+    b->profiling = enabled != 0;
+    return GPMA_OK;
+}
+
+gpma_status gpma_batch_get_profile(const gpma_batch *b, gpma_profile *out) {
+    if (!b || !out) {
+        set_error("gpma_batch_get_profile: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    *out = b->prof;
+    return GPMA_OK;
+}
+
+gpma_status gpma_batch_reset_profile(gpma_batch *b) {
+    if (!b) {
+        set_error("gpma_batch_reset_profile: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    b->prof = gpma_profile{};
     return GPMA_OK;
 }
 

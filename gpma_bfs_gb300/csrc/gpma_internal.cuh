@@ -5,7 +5,8 @@
 //   values[cap]  u8   1 = live (or any non-zero value), 0 = tombstone
 //   row_offset[row_num+1] u32, row_offset[r+1] = slot of row r's guard
 //   scratch keys/values [cap] for windows wider than one CTA and resizes
-// plus per-batch buffers sized by the largest batch seen.
+// plus update buffers (BatchBuffers) sized by the largest batch seen, owned
+// by a graph (single-graph updates) or by a gpma_batch (many graphs at once).
 #pragma once
 
 #include "../../include/gpma_gb300.h"
@@ -26,6 +27,7 @@ constexpr uint64_t COL_NONE = 0xFFFFFFFFull;
 constexpr double LOWER_LEAF = 0.08, LOWER_ROOT = 0.42, UPPER_LEAF = 0.92, UPPER_ROOT = 0.84;
 constexpr uint64_t SIGNIFICANT_INSERTS = 5000000ull;
 constexpr uint32_t MAX_SLOTS = 1u << 31;
+constexpr uint32_t MAX_LEVELS = 32;  // tree_height <= 31
 
 // Launch shapes.
 constexpr int BLOCK = 256;                 // threads of every persistent kernel
@@ -33,7 +35,7 @@ constexpr uint32_t WARP_WINDOW_MAX = 256;  // widest window handled by one warp 
 constexpr uint32_t CTA_WINDOW_MAX = 2048;  // widest window handled by one CTA in shared memory
 constexpr uint32_t CHUNK = 2048;           // slots per CTA step for wider windows
 // Shared memory of the update kernel: three staging arrays (keys + values)
-// of CTA_WINDOW_MAX slots.
+// of CTA_WINDOW_MAX slots (also holds the sort tile and the locate cache).
 constexpr size_t UPDATE_SMEM = 3ull * CTA_WINDOW_MAX * 9ull + 64;
 
 // Device error codes (DeviceStatus::err).
@@ -57,17 +59,37 @@ struct GridBarrier {
 struct DeviceStatus {
     uint32_t err;
     uint32_t invalid_keys;  // keys whose column is the reserved 0xFFFFFFFF
-    uint32_t significant;   // >= SIGNIFICANT_INSERTS insertions: host rebuild
-    uint32_t inserts;       // insertions after delete/modify
-    uint32_t remaining;     // insertions still pending after the level loop
-    uint32_t rem_a;         // their start in the insertion arrays
+    uint32_t significant;   // single graph: >= SIGNIFICANT_INSERTS insertions (host rebuild)
+    uint32_t inserts;       // insertions after delete/modify (all graphs)
     uint32_t levels;        // level iterations executed
-    uint32_t rem_buf;       // pending-insertion buffer holding them
-    uint32_t pad;
-    uint32_t pad2;
+    uint32_t pad[3];
     unsigned long long accepted_windows;
     unsigned long long accepted_slots;
     GridBarrier bar;
+    // %globaltimer stamps taken by CTA 0 at phase boundaries: start, sorted,
+    // located, grouped, level loop done
+    unsigned long long stamp[5];
+};
+
+// One graph as the update kernel sees it (device table, one entry per graph).
+struct GraphDesc {
+    uint64_t *keys;
+    uint8_t *vals;
+    uint32_t *row_offset;
+    uint64_t *skeys;  // scratch of `size` slots
+    uint8_t *svals;
+    uint32_t row_num, size, seg, log2seg, height;
+    uint32_t pad[3];
+    uint32_t lower[MAX_LEVELS];
+    uint32_t upper[MAX_LEVELS];
+};
+
+// Per-graph result of one update launch.
+struct GraphStatus {
+    uint32_t inserts;    // insertions of this graph after delete/modify
+    uint32_t remaining;  // insertions the root rebalance still has to place
+    uint32_t ins_base;   // first insertion of this graph in the compacted order
+    uint32_t pad;
 };
 
 struct Geometry {
@@ -81,6 +103,49 @@ struct Geometry {
 void recalculate_density(Geometry &geo);
 uint32_t fls32(uint32_t x);
 
+// Buffers of one update launch (batch keys of all graphs, insertions, window
+// lists, sort state, per-graph tables).
+struct BatchBuffers {
+    uint64_t cap = 0;  // keys
+    uint64_t *bkeys[2] = {nullptr, nullptr};
+    uint8_t *bvals[2] = {nullptr, nullptr};
+    uint32_t *leaf = nullptr;
+    uint64_t *ikeys[2] = {nullptr, nullptr};  // pending insertions, compacted per level (ping-pong)
+    uint8_t *ivals[2] = {nullptr, nullptr};
+    uint32_t *ileaf = nullptr;
+    uint32_t *igraph = nullptr;
+    uint32_t *wnode[2] = {nullptr, nullptr};
+    uint32_t *wgraph[2] = {nullptr, nullptr};
+    uint32_t *wa[2] = {nullptr, nullptr};
+    uint32_t *wb[2] = {nullptr, nullptr};
+    uint32_t *wflag = nullptr;
+    uint32_t *wlive = nullptr;
+    uint64_t *rkeys = nullptr;  // insertions left for the root rebalance
+    uint8_t *rvals = nullptr;
+    // sort state
+    uint32_t *sort_tiles = nullptr;    // 8 tile counters
+    uint32_t *sort_status = nullptr;   // look-back words, 8 x tiles x 256
+    uint64_t sort_status_cap = 0;
+    uint32_t *sort_hist = nullptr;     // [graph][8][256] digit counts
+    uint32_t hist_cap = 0;             // graphs
+    // per-graph tables
+    uint32_t gcap = 0;
+    GraphDesc *gd = nullptr;
+    GraphStatus *gs = nullptr;
+    GraphStatus *h_gs = nullptr;       // pinned
+    uint32_t *boff = nullptr;          // batch offsets, graphs + 1
+    uint32_t *toff = nullptr;          // sort tile offsets, graphs + 1
+    std::vector<GraphDesc> h_gd;
+    std::vector<uint32_t> h_off;       // boff then toff
+    // grid-path chunk counts (sum of window widths / CHUNK)
+    uint32_t *chunk_cnt = nullptr;
+    uint64_t chunk_cap = 0;
+    // persistent-kernel scratch
+    uint32_t *cta_cnt = nullptr;       // 4 * grid
+    DeviceStatus *status = nullptr;
+    DeviceStatus *h_status = nullptr;  // pinned
+};
+
 }  // namespace gpma
 
 // Opaque handle of the C ABI.
@@ -93,36 +158,11 @@ struct gpma_graph {
     uint64_t *keys = nullptr;
     uint8_t *values = nullptr;
     uint32_t *row_offset = nullptr;
-    uint32_t *d_lower = nullptr;      // 33 entries (height <= 31)
-    uint32_t *d_upper = nullptr;
     uint32_t scratch_cap = 0;
     uint64_t *skeys = nullptr;        // scratch for wide windows and resizes
     uint8_t *svals = nullptr;
-    uint32_t *chunk_cnt = nullptr;    // scratch_cap / CHUNK + 1 entries
-    // per-batch buffers
-    uint64_t batch_cap = 0;
-    uint64_t *bkeys[2] = {nullptr, nullptr};
-    uint8_t *bvals[2] = {nullptr, nullptr};
-    uint32_t *leaf = nullptr;
-    uint64_t *ikeys[2] = {nullptr, nullptr};  // pending insertions, compacted per level (ping-pong)
-    uint8_t *ivals[2] = {nullptr, nullptr};
-    uint32_t *ileaf = nullptr;
-    uint32_t *wnode[2] = {nullptr, nullptr};
-    uint32_t *wa[2] = {nullptr, nullptr};
-    uint32_t *wb[2] = {nullptr, nullptr};
-    uint32_t *wflag = nullptr;
-    uint32_t *wlive = nullptr;
-    // sort scratch
-    uint32_t *sort_hist = nullptr;     // 8 * 256
-    uint32_t *sort_base = nullptr;     // 8 * 256
-    uint32_t *sort_tiles = nullptr;    // 8 tile counters
-    uint32_t *sort_status = nullptr;   // 8 * tiles * 256 look-back words
-    uint64_t sort_status_cap = 0;
-    // persistent-kernel scratch
-    uint32_t *cta_cnt = nullptr;       // 4 * grid
-    int update_grid = 0;
-    gpma::DeviceStatus *status = nullptr;
-    gpma::DeviceStatus *h_status = nullptr;  // pinned
+    uint32_t *chunk_cnt = nullptr;    // scratch_cap / CHUNK + 2 entries (root rebuild)
+    gpma::BatchBuffers buf;           // single-graph update buffers
     // BFS state
     uint32_t bfs_cap = 0;
     uint32_t *bfs_visited = nullptr;   // row_num/32 + 2 words
@@ -132,15 +172,35 @@ struct gpma_graph {
     uint32_t *bfs_ctl = nullptr;       // counters + status
     uint32_t *h_bfs_ctl = nullptr;     // pinned
     int bfs_grid = 0;
-    uint64_t *msbfs_mask[3] = {nullptr, nullptr, nullptr};
-    uint32_t *msbfs_levels = nullptr;
-    uint64_t msbfs_levels_cap = 0;
-    uint32_t *msbfs_src = nullptr;
+    gpma_batch *own_batch = nullptr;   // multi-source BFS context of this graph
     gpma_stats stats{};
     // profiling: events on the caller's stream around each phase
     bool profiling = false;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     gpma_profile prof{};
+};
+
+// Many graphs updated (and searched) per launch.
+struct gpma_batch {
+    int device = 0;
+    int sms = 0;
+    gpma::BatchBuffers buf;
+    bool profiling = false;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    gpma_profile prof{};
+    // multi-source BFS state over all graphs of a call
+    uint64_t ms_cap = 0;               // nodes
+    uint64_t *ms_mask[3] = {nullptr, nullptr, nullptr};
+    uint32_t *ms_voff = nullptr;       // node offsets, graphs + 1
+    uint32_t *ms_src = nullptr;        // sources, graphs * 64
+    uint32_t *ms_nsrc = nullptr;       // sources per graph
+    uint32_t *ms_ctl = nullptr;
+    uint32_t *h_ms_ctl = nullptr;      // pinned
+    void *ms_gdesc = nullptr;          // BFS graph table
+    uint64_t *ms_reached = nullptr;    // graphs * 64
+    uint2 *ms_chunks = nullptr;
+    uint32_t ms_gcap = 0;
+    uint64_t last_traversed = 0;       // edges scanned by the last multi-source BFS, all lanes
 };
 
 namespace gpma {
@@ -187,29 +247,39 @@ void dev_free(T *&p) {
 }
 
 // ---- profiling helpers -------------------------------------------------------
-inline void prof_mark(gpma_graph *g, int i, cudaStream_t s) {
-    if (g->profiling)
-        cudaEventRecord(g->ev[i], s);
+inline void prof_mark(bool on, cudaEvent_t *ev, int i, cudaStream_t s) {
+    if (on)
+        cudaEventRecord(ev[i], s);
 }
 // elapsed ms between two recorded events (both complete: call after a sync)
-inline double prof_elapsed(gpma_graph *g, int a, int b) {
+inline double prof_elapsed(bool on, cudaEvent_t *ev, int a, int b) {
     float ms = 0.f;
-    if (g->profiling && cudaEventElapsedTime(&ms, g->ev[a], g->ev[b]) != cudaSuccess) {
+    if (on && cudaEventElapsedTime(&ms, ev[a], ev[b]) != cudaSuccess) {
         cudaGetLastError();
         ms = 0.f;
     }
     return ms;
 }
+inline void prof_mark(gpma_graph *g, int i, cudaStream_t s) { prof_mark(g->profiling, g->ev, i, s); }
+inline double prof_elapsed(gpma_graph *g, int a, int b) { return prof_elapsed(g->profiling, g->ev, a, b); }
 
 // ---- host entry points implemented per translation unit -------------------
-gpma_status ensure_batch(gpma_graph *g, uint64_t n);
+gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs);
+void free_buffers(BatchBuffers &b);
 gpma_status ensure_scratch(gpma_graph *g, uint32_t slots);
-gpma_status upload_geometry(gpma_graph *g, cudaStream_t s);
+// One launch updating graphs[0..k) with the batches already staged in
+// buf.bkeys[0]/bvals[0] at offsets off[0..k]. Graphs must be ordered by
+// segment length. check_keys=false only for the internal guard insertion.
+gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32_t k, BatchBuffers &buf, int sms,
+                          cudaStream_t s, bool check_keys, bool profiling, cudaEvent_t *ev, gpma_profile *prof);
 gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys = true);
 gpma_status bfs_run(gpma_graph *g, uint32_t src, cudaStream_t s, uint64_t *reached);
-gpma_status bfs_multi_run(gpma_graph *g, const uint32_t *d_src, uint32_t k, cudaStream_t s);
 gpma_status bfs_noalloc_run(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached, cudaStream_t s);
+gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs, const uint32_t *nsrc,
+                          uint32_t k, uint32_t *const *levels, uint64_t *reached, cudaStream_t s);
 void free_bfs(gpma_graph *g);
+void free_batch_bfs(gpma_batch *b);
+int update_grid_size(int sms);
 
 }  // namespace gpma
 
@@ -331,6 +401,20 @@ __device__ __forceinline__ uint32_t upper_bound_u64(P a, uint32_t n, uint64_t ke
         uint32_t mid = (lo + hi) >> 1;
         if (a[mid] <= key)
             lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// Index of the segment of a[0..n] (increasing offsets, a[0] = 0) holding x:
+// the last i with a[i] <= x.
+__device__ __forceinline__ uint32_t segment_of(const uint32_t *a, uint32_t n, uint32_t x) {
+    uint32_t lo = 0, hi = n;  // answer in [0, n)
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] <= x)
+            lo = mid;
         else
             hi = mid;
     }

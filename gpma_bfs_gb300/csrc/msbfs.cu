@@ -1,0 +1,423 @@
+// msbfs.cu - multi-source BFS over one or many GPMA graphs in one launch.
+//
+// No reference counterpart (the reference BFS, gpma_bfs.cuh:446-533, takes one
+// source of one graph); each of the up to 64 searches per graph has the
+// reference's level semantics (levels[src] = 1, a node first reached from
+// level L gets L+1, slots with column 0xFFFFFFFF or value 0 are not edges).
+//
+// The nodes of all graphs form one index space (graph g owns
+// [voff[g], voff[g+1])). Each node carries three 64-bit masks, one bit lane
+// per source: visited, frontier, next. One persistent cooperative kernel runs
+// every level, separated by bounded grid barriers:
+//   expand (phase 1): a warp takes 32 consecutive nodes; the rows of those in
+//     the frontier are walked as one concatenated slot range (warp-level load
+//     balancing) and every edge ORs the source's frontier mask, minus the
+//     target's visited lanes, into next[target]; rows longer than 64 slots
+//     are queued as 128-slot chunks instead;
+//   expand (phase 2): every warp takes chunks;
+//   commit: next minus visited becomes the new frontier, joins visited, and
+//     gives each newly reached (node, lane) its level.
+// The traversed-edge count (edges scanned from reached nodes, per source) is
+// summed on the fly for GTEPS.
+#include "gpma_internal.cuh"
+
+#include <algorithm>
+#include <numeric>
+
+namespace gpma {
+namespace {
+
+enum : uint32_t {
+    MS_CHANGE = 0,  // 3 rotating counters: CTAs that reached a new (node, lane)
+    MS_CHUNKS = 3,  // 3 rotating chunk counters
+    MS_ERR = 6,
+    MS_LEVELS = 7,
+    MS_BAR = 10,    // GridBarrier (2 words)
+    MS_CTL_WORDS = 16,
+};
+
+constexpr uint32_t MS_BIG_ROW = 64;
+constexpr uint32_t MS_CHUNK_SLOTS = 128;
+constexpr uint32_t MS_CHUNK_CAP = 1u << 20;
+
+struct MsGraph {
+    const uint64_t *keys;
+    const uint8_t *vals;
+    const uint32_t *ro;
+    uint32_t *levels;  // [nsrc][n] or null
+    uint32_t n, size, nsrc, pad;
+};
+
+struct MsArgs {
+    const MsGraph *gr;
+    uint32_t G;
+    const uint32_t *voff;  // G + 1
+    const uint32_t *src;   // G * 64
+    uint64_t *visited;
+    uint64_t *frontier;
+    uint64_t *next;
+    uint4 *chunks;         // {slot begin, slot end, graph, node}
+    uint32_t chunk_cap;
+    uint32_t *ctl;
+    unsigned long long *reached;  // G * 64
+    unsigned long long *traversed;
+};
+
+__device__ __forceinline__ uint32_t graph_of_node(const MsArgs &A, uint32_t u) {
+    return A.G == 1 ? 0u : segment_of(A.voff, A.G, u);
+}
+
+// One slot of graph g scanned with frontier mask fm; returns 1 if it is an edge.
+__device__ __forceinline__ uint32_t ms_visit(const MsArgs &A, const MsGraph &Gr, uint32_t g, uint32_t s, uint64_t fm) {
+    const uint64_t key = Gr.keys[s];
+    const uint32_t w = (uint32_t)key;
+    if (w == 0xFFFFFFFFu || Gr.vals[s] == 0 || w >= Gr.n)
+        return 0;
+    const uint32_t gw = A.voff[g] + w;
+    const uint64_t nb = fm & ~A.visited[gw];
+    if (nb && (A.next[gw] & nb) != nb)
+        atomicOr((unsigned long long *)&A.next[gw], (unsigned long long)nb);
+    return 1;
+}
+
+__global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
+    GridBarrier *bar = reinterpret_cast<GridBarrier *>(A.ctl + MS_BAR);
+    uint32_t *err = A.ctl + MS_ERR;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gwarp = blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5);
+    const uint32_t nwarps = gridDim.x * (BLOCK / 32);
+    const uint32_t gtid = blockIdx.x * BLOCK + threadIdx.x;
+    const uint32_t nthreads = gridDim.x * BLOCK;
+    const uint32_t N = A.voff[A.G];
+    unsigned long long traversed = 0;
+    // seed the sources (masks cleared by the host)
+    for (uint32_t t = gtid; t < A.G * 64; t += nthreads) {
+        const uint32_t g = t >> 6, j = t & 63;
+        const MsGraph &Gr = A.gr[g];
+        if (j >= Gr.nsrc)
+            continue;
+        const uint32_t s = A.src[t];
+        atomicOr((unsigned long long *)&A.visited[A.voff[g] + s], 1ull << j);
+        atomicOr((unsigned long long *)&A.frontier[A.voff[g] + s], 1ull << j);
+        if (Gr.levels)
+            Gr.levels[(size_t)j * Gr.n + s] = 1;
+    }
+    if (!grid_barrier(bar, err))
+        return;
+    uint32_t level = 1;
+    for (;; ++level) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            A.ctl[MS_CHANGE + (level + 1) % 3] = 0;
+            A.ctl[MS_CHUNKS + (level + 1) % 3] = 0;
+        }
+        uint32_t *chunk_cnt = A.ctl + MS_CHUNKS + level % 3;
+        // expand, phase 1
+        for (uint32_t base = gwarp * 32; base < N; base += nwarps * 32) {
+            const uint32_t u = base + lane;
+            const uint64_t f = u < N ? A.frontier[u] : 0ull;
+            if (__ballot_sync(0xFFFFFFFFu, f != 0ull) == 0)
+                continue;
+            uint32_t g = 0, b = 0, e = 0, len = 0;
+            if (f) {
+                A.frontier[u] = 0;  // consumed; the commit phase writes the next frontier
+                g = graph_of_node(A, u);
+                const MsGraph &Gr = A.gr[g];
+                const uint32_t lu = u - A.voff[g];
+                b = Gr.ro[lu];
+                e = min(Gr.ro[lu + 1], Gr.size);
+                len = e > b ? e - b : 0;
+            }
+            const uint32_t nch = len > MS_BIG_ROW ? (len + MS_CHUNK_SLOTS - 1) / MS_CHUNK_SLOTS : 0;
+            const uint32_t ch_incl = warp_incl_scan(nch);
+            const uint32_t ch_total = __shfl_sync(0xFFFFFFFFu, ch_incl, 31);
+            if (ch_total) {
+                uint32_t cb = 0;
+                if (lane == 0)
+                    cb = atomicAdd(chunk_cnt, ch_total);
+                cb = __shfl_sync(0xFFFFFFFFu, cb, 0);
+                if (cb + ch_total <= A.chunk_cap) {
+                    const uint32_t pos = cb + ch_incl - nch;
+                    for (uint32_t c = 0; c < nch; ++c)
+                        A.chunks[pos + c] = make_uint4(b + c * MS_CHUNK_SLOTS, min(e, b + (c + 1) * MS_CHUNK_SLOTS), g, u);
+                    if (nch) {
+                        // the chunk reads the mask from frontier[u]: keep it until commit
+                        A.frontier[u] = f;
+                        len = 0;
+                    }
+                } else {
+                    for (uint32_t c = cb + lane; c < min(cb + ch_total, A.chunk_cap); c += 32)
+                        A.chunks[c] = make_uint4(0, 0, 0, 0);
+                }
+            }
+            const uint32_t incl = warp_incl_scan(len);
+            const uint32_t excl = incl - len;
+            const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            for (uint32_t p0 = 0; p0 < total; p0 += 32) {
+                const uint32_t p = p0 + lane;
+                uint32_t r = 0;
+#pragma unroll
+                for (uint32_t step = 16; step >= 1; step >>= 1) {
+                    const uint32_t cand = r + step;
+                    const uint32_t ex_c = __shfl_sync(0xFFFFFFFFu, excl, cand & 31);
+                    if (cand < 32 && ex_c <= p)
+                        r = cand;
+                }
+                const uint32_t rb = __shfl_sync(0xFFFFFFFFu, b, r);
+                const uint32_t rex = __shfl_sync(0xFFFFFFFFu, excl, r);
+                const uint32_t rg = __shfl_sync(0xFFFFFFFFu, g, r);
+                const uint64_t rf = __shfl_sync(0xFFFFFFFFu, f, r);
+                if (p < total)
+                    traversed += ms_visit(A, A.gr[rg], rg, rb + (p - rex), rf) * (unsigned long long)__popcll(rf);
+            }
+        }
+        if (!grid_barrier(bar, err))
+            return;
+        // expand, phase 2: long-row chunks
+        const uint32_t nch_all = min(ld_volatile(chunk_cnt), A.chunk_cap);
+        for (uint32_t c = gwarp; c < nch_all; c += nwarps) {
+            const uint4 ch = A.chunks[c];
+            if (ch.x >= ch.y)
+                continue;
+            const uint64_t fm = A.frontier[ch.w];
+            const MsGraph &Gr = A.gr[ch.z];
+            for (uint32_t s = ch.x + lane; s < ch.y; s += 32)
+                traversed += ms_visit(A, Gr, ch.z, s, fm) * (unsigned long long)__popcll(fm);
+        }
+        if (!grid_barrier(bar, err))
+            return;
+        // commit
+        uint32_t changed = 0;
+        for (uint32_t w = gtid; w < N; w += nthreads) {
+            const uint64_t nxt = A.next[w];
+            const uint64_t vis = A.visited[w];
+            const uint64_t nx = nxt & ~vis;
+            if (A.frontier[w])
+                A.frontier[w] = 0;  // chunked rows kept their mask until now
+            if (nxt)
+                A.next[w] = 0;
+            if (nx) {
+                A.frontier[w] = nx;
+                A.visited[w] = vis | nx;
+                changed = 1;
+                const uint32_t g = graph_of_node(A, w);
+                const MsGraph &Gr = A.gr[g];
+                if (Gr.levels) {
+                    const uint32_t lw = w - A.voff[g];
+                    uint64_t m = nx;
+                    while (m) {
+                        const int bit = __ffsll((long long)m) - 1;
+                        m &= m - 1;
+                        Gr.levels[(size_t)bit * Gr.n + lw] = level + 1;
+                    }
+                }
+            }
+        }
+        if (__syncthreads_or(changed) && threadIdx.x == 0)
+            atomicAdd(A.ctl + MS_CHANGE + level % 3, 1u);
+        if (!grid_barrier(bar, err))
+            return;
+        if (ld_volatile(A.ctl + MS_CHANGE + level % 3) == 0)
+            break;
+    }
+    // reached (graph, lane) counts: each CTA walks a contiguous node range
+    // graph by graph with shared-memory lane counters
+    __shared__ unsigned int cnt[64];
+    const uint32_t per = (N + gridDim.x - 1) / gridDim.x;
+    const uint32_t lo = min(N, blockIdx.x * per), hi = min(N, lo + per);
+    uint32_t pos = lo;
+    while (__syncthreads_or(pos < hi)) {
+        const uint32_t g = graph_of_node(A, pos);
+        const uint32_t end = min(hi, A.voff[g + 1]);
+        if (threadIdx.x < 64)
+            cnt[threadIdx.x] = 0;
+        __syncthreads();
+        for (uint32_t w = pos + threadIdx.x; w < end; w += BLOCK) {
+            uint64_t m = A.visited[w];
+            while (m) {
+                const int bit = __ffsll((long long)m) - 1;
+                m &= m - 1;
+                atomicAdd(&cnt[bit], 1u);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 64 && cnt[threadIdx.x])
+            atomicAdd(&A.reached[(size_t)g * 64 + threadIdx.x], (unsigned long long)cnt[threadIdx.x]);
+        pos = end;
+    }
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1)
+        traversed += __shfl_xor_sync(0xFFFFFFFFu, traversed, d);
+    if (lane == 0 && traversed)
+        atomicAdd(A.traversed, traversed);
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        A.ctl[MS_LEVELS] = level;
+}
+
+int g_ms_grid[64] = {};
+
+int ms_grid_size(int sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64)
+        dev = 0;
+    if (g_ms_grid[dev] == 0) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, msbfs_kernel, BLOCK, 0) != cudaSuccess)
+            return 0;
+        g_ms_grid[dev] = sms * std::min(per_sm, 8);
+    }
+    return g_ms_grid[dev];
+}
+
+}  // namespace
+
+void free_batch_bfs(gpma_batch *b) {
+    for (int i = 0; i < 3; ++i)
+        dev_free(b->ms_mask[i]);
+    dev_free(b->ms_voff);
+    dev_free(b->ms_src);
+    dev_free(b->ms_nsrc);
+    dev_free(b->ms_ctl);
+    dev_free(b->ms_gdesc);
+    dev_free(b->ms_reached);
+    dev_free(b->ms_chunks);
+    if (b->h_ms_ctl)
+        cudaFreeHost(b->h_ms_ctl);
+    b->h_ms_ctl = nullptr;
+    b->ms_cap = 0;
+    b->ms_gcap = 0;
+}
+
+// Multi-source BFS of graphs[0..k) with nsrc[i] sources each. Levels (when
+// levels != NULL) are written through device staging and copied to the
+// caller's pointers; reached receives sum(nsrc) counts. Also returns the
+// traversed-edge total through *traversed_out when non-null.
+gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs, const uint32_t *nsrc,
+                          uint32_t k, uint32_t *const *levels, uint64_t *reached, cudaStream_t s) {
+    const int grid = ms_grid_size(b->sms);
+    if (grid == 0) {
+        set_error("multi-source BFS kernel cannot be resident");
+        return GPMA_ERR_CUDA;
+    }
+    std::vector<uint32_t> voff(k + 1, 0);
+    for (uint32_t i = 0; i < k; ++i)
+        voff[i + 1] = voff[i] + graphs[i]->row_num;
+    const uint64_t N = voff[k];
+    if (N > b->ms_cap || !b->ms_mask[0]) {
+        for (int i = 0; i < 3; ++i)
+            dev_free(b->ms_mask[i]);
+        b->ms_cap = 0;
+        for (int i = 0; i < 3; ++i)
+            GPMA_TRY(dev_alloc(&b->ms_mask[i], std::max<uint64_t>(N, 1)));
+        b->ms_cap = std::max<uint64_t>(N, 1);
+    }
+    if (k > b->ms_gcap || !b->ms_voff) {
+        dev_free(b->ms_voff);
+        dev_free(b->ms_src);
+        dev_free(b->ms_gdesc);
+        dev_free(b->ms_reached);
+        b->ms_gcap = 0;
+        GPMA_TRY(dev_alloc(&b->ms_voff, k + 1));
+        GPMA_TRY(dev_alloc(&b->ms_src, 64ull * k));
+        uint8_t *gd = nullptr;
+        GPMA_TRY(dev_alloc(&gd, sizeof(MsGraph) * k));
+        b->ms_gdesc = gd;
+        GPMA_TRY(dev_alloc(&b->ms_reached, 64ull * k + 1));
+        b->ms_gcap = k;
+    }
+    if (!b->ms_ctl) {
+        GPMA_TRY(dev_alloc(&b->ms_ctl, MS_CTL_WORDS));
+        GPMA_TRY(dev_alloc(&b->ms_chunks, MS_CHUNK_CAP * 2));  // uint4 = 2 x uint2
+        cudaError_t e = cudaMallocHost((void **)&b->h_ms_ctl, sizeof(uint32_t) * MS_CTL_WORDS);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaMallocHost(ms ctl)");
+    }
+    // per-graph level staging, only when levels are requested
+    std::vector<uint32_t *> stage(k, nullptr);
+    std::vector<MsGraph> gr(k);
+    std::vector<uint32_t> hsrc(64ull * k, 0);
+    gpma_status st = GPMA_OK;
+    for (uint32_t i = 0; i < k; ++i) {
+        gpma_graph *g = graphs[i];
+        gr[i].keys = g->keys;
+        gr[i].vals = g->values;
+        gr[i].ro = g->row_offset;
+        gr[i].n = g->row_num;
+        gr[i].size = g->geo.size;
+        gr[i].nsrc = nsrc[i];
+        gr[i].levels = nullptr;
+        if (levels && levels[i]) {
+            st = dev_alloc(&stage[i], (uint64_t)nsrc[i] * g->row_num);
+            if (st != GPMA_OK)
+                break;
+            gr[i].levels = stage[i];
+            cudaMemsetAsync(stage[i], 0, sizeof(uint32_t) * nsrc[i] * (uint64_t)g->row_num, s);
+        }
+        for (uint32_t j = 0; j < nsrc[i]; ++j)
+            hsrc[64ull * i + j] = srcs[i][j];
+    }
+    auto cleanup = [&]() {
+        for (auto *p : stage)
+            if (p)
+                cudaFree(p);
+    };
+    if (st != GPMA_OK) {
+        cleanup();
+        return st;
+    }
+    auto step = [&]() -> gpma_status {
+        GPMA_CUDA(cudaMemcpyAsync(b->ms_voff, voff.data(), sizeof(uint32_t) * (k + 1), cudaMemcpyHostToDevice, s));
+        GPMA_CUDA(cudaMemcpyAsync(b->ms_src, hsrc.data(), sizeof(uint32_t) * 64 * k, cudaMemcpyHostToDevice, s));
+        GPMA_CUDA(cudaMemcpyAsync(b->ms_gdesc, gr.data(), sizeof(MsGraph) * k, cudaMemcpyHostToDevice, s));
+        for (int i = 0; i < 3; ++i)
+            GPMA_CUDA(cudaMemsetAsync(b->ms_mask[i], 0, sizeof(uint64_t) * N, s));
+        GPMA_CUDA(cudaMemsetAsync(b->ms_ctl, 0, sizeof(uint32_t) * MS_CTL_WORDS, s));
+        GPMA_CUDA(cudaMemsetAsync(b->ms_reached, 0, sizeof(unsigned long long) * (64ull * k + 1), s));
+        MsArgs A;
+        A.gr = static_cast<const MsGraph *>(b->ms_gdesc);
+        A.G = k;
+        A.voff = b->ms_voff;
+        A.src = b->ms_src;
+        A.visited = b->ms_mask[0];
+        A.frontier = b->ms_mask[1];
+        A.next = b->ms_mask[2];
+        A.chunks = reinterpret_cast<uint4 *>(b->ms_chunks);
+        A.chunk_cap = MS_CHUNK_CAP;
+        A.ctl = b->ms_ctl;
+        A.reached = reinterpret_cast<unsigned long long *>(b->ms_reached);
+        A.traversed = reinterpret_cast<unsigned long long *>(b->ms_reached) + 64ull * k;
+        void *params[] = {&A};
+        prof_mark(b->profiling, b->ev, 0, s);
+        GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)msbfs_kernel, dim3(grid), dim3(BLOCK), params, 0, s));
+        prof_mark(b->profiling, b->ev, 1, s);
+        GPMA_CUDA(cudaMemcpyAsync(b->h_ms_ctl, b->ms_ctl, sizeof(uint32_t) * MS_CTL_WORDS, cudaMemcpyDeviceToHost, s));
+        std::vector<unsigned long long> r(64ull * k + 1);
+        GPMA_CUDA(cudaMemcpyAsync(r.data(), b->ms_reached, sizeof(unsigned long long) * r.size(),
+                                  cudaMemcpyDeviceToHost, s));
+        for (uint32_t i = 0; i < k; ++i)
+            if (stage[i])
+                GPMA_TRY(copy_any(levels[i], stage[i], sizeof(uint32_t) * nsrc[i] * (uint64_t)graphs[i]->row_num, s));
+        GPMA_CUDA(cudaStreamSynchronize(s));
+        b->prof.kernel_launches += 1;
+        b->prof.bfs_kernels++;
+        b->prof.bfs_ms += prof_elapsed(b->profiling, b->ev, 0, 1);
+        if (b->h_ms_ctl[MS_ERR]) {
+            set_error("device-side wait gave up in the multi-source BFS kernel (code %u)", b->h_ms_ctl[MS_ERR]);
+            return GPMA_ERR_TIMEOUT;
+        }
+        if (reached) {
+            uint64_t o = 0;
+            for (uint32_t i = 0; i < k; ++i)
+                for (uint32_t j = 0; j < nsrc[i]; ++j)
+                    reached[o++] = r[64ull * i + j];
+        }
+        b->last_traversed = r[64ull * k];
+        b->prof.bfs_edges += r[64ull * k];
+        return GPMA_OK;
+    };
+    st = step();
+    cleanup();
+    return st;
+}
+
+}  // namespace gpma

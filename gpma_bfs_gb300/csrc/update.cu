@@ -1,29 +1,36 @@
-// update.cu - GPMA+ batch update on one GB300.
+// update.cu - GPMA+ batch update on one GB300, for one graph or many.
 //
-// Replaces update_gpma (gpma.cuh:968-1050). After the batch sort (sort.cu)
-// one persistent cooperative kernel runs every remaining step on the device,
-// separated by bounded grid barriers instead of host round trips:
-//   P1 locate: the reference's top-down search over segment first keys, then
+// Replaces update_gpma (gpma.cuh:968-1050). One persistent cooperative kernel
+// runs every step of the update of one or more independent graphs, with
+// bounded grid barriers instead of host round trips:
+//   S  stable radix sort of each graph's batch (sort.cuh, gpma.cuh:977);
+//   P1 locate: the reference's top-down search over segment first keys (its
+//      upper levels from a shared-memory copy when one graph is updated), then
 //      an equality scan of the leaf with 16-byte loads; hits store the
 //      update's value in place (delete/modify/revive, gpma.cuh:188-220);
 //   P2 keep the insertions in sorted order (compact_insertions, :836-844);
-//   P3 group them by leaf into level-0 windows (group_insertion_by_node,
-//      :846-873). A window is (node, [a, b)) into the sorted insertions;
+//   P3 group them by (graph, leaf) into level-0 windows
+//      (group_insertion_by_node, :846-873). A window is (graph, node, [a, b))
+//      into the current insertion buffer;
 //   level loop (:1012-1029): each window of width W = seg << level counts its
-//      live slots, is accepted iff lower <= live + pending <= upper, and an
-//      accepted window is rewritten as the stable merge of its live entries
-//      and its insertions, redispatched evenly (:636-654) in one coalesced
-//      pass. Rejected windows whose parents coincide merge into one parent
-//      window (their insertion ranges are adjacent), so insertions are never
-//      moved between levels. Windows up to 256 slots go to warp groups, up to
-//      2048 slots to one CTA in shared memory, wider ones to the whole grid.
-// The host reads one status block at the end. Only the root resize
-// (:1034-1044) and the >= 5M-insertion rebuild (:936-966) run host-driven.
+//      live slots, is accepted iff lower <= live + pending <= upper (the
+//      graph's thresholds), and an accepted window is rewritten as the stable
+//      merge of its live entries and its insertions, redispatched evenly
+//      (:636-654) in one coalesced pass. The insertions of rejected windows
+//      are compacted into the other buffer (one scan over windows) and a
+//      rejected right sibling joins its rejected left sibling in the parent.
+//      Windows are ordered by graph and graphs by segment length, so the list
+//      splits into one contiguous run per segment length and each run has one
+//      window width: up to 256 slots per warp group, up to 2048 per CTA in
+//      shared memory, wider ones chunk by chunk over the whole grid.
+// The host reads the status blocks once. Only the root resize (:1034-1044)
+// and the >= 5M-insertion rebuild (:936-966) run host-driven, per graph.
 #include "gpma_internal.cuh"
 #include "sort.cuh"
 
 #include <algorithm>
 #include <cmath>
+#include <numeric>
 
 namespace gpma {
 
@@ -60,69 +67,81 @@ void recalculate_density(Geometry &geo) {
 namespace {
 
 struct UpdateArgs {
-    uint64_t *keys;
-    uint8_t *vals;
-    uint32_t *row_offset;
-    uint32_t row_num;
-    uint32_t size, seg, log2seg, height;
-    const uint32_t *lower;
-    const uint32_t *upper;
-    uint64_t *bk[2];  // batch, ping-pong buffers of the radix sort (input in [0])
+    const GraphDesc *gd;
+    GraphStatus *gs;
+    uint32_t G;
+    uint32_t max_height;
+    const uint32_t *boff;   // batch offsets, G + 1
+    const uint32_t *toff;   // sort tile offsets, G + 1
+    uint32_t n;
+    uint64_t *bk[2];        // batches, ping-pong buffers of the radix sort (input in [0])
     uint8_t *bv[2];
-    uint32_t *sort_hist;    // 8 x 256 digit counts (zeroed per update)
+    uint32_t *sort_hist;    // [G + 1][8][256] digit counts (zeroed per update)
     uint32_t *sort_tiles;   // 8 tile counters (zeroed per update)
     uint32_t *sort_status;  // look-back words, 8 x tiles x 256 (zeroed per update)
     bool check_keys;
-    uint32_t n;
     uint32_t *leaf;
     uint64_t *ikeys[2];
     uint8_t *ivals[2];
     uint32_t *ileaf;
+    uint32_t *igraph;
     uint32_t *wnode[2];
+    uint32_t *wgraph[2];
     uint32_t *wa[2];
     uint32_t *wb[2];
     uint32_t *wflag;
     uint32_t *wlive;
-    uint64_t *skeys;
-    uint8_t *svals;
+    uint64_t *rkeys;
+    uint8_t *rvals;
     uint32_t *chunk_cnt;
     uint32_t *cta_cnt;
     DeviceStatus *st;
 };
 
+// Current window list of a level.
+struct Windows {
+    const uint32_t *node, *graph, *a, *b;
+};
+
+__device__ __forceinline__ uint32_t graph_of(const UpdateArgs &A, uint32_t i) {
+    return A.G == 1 ? 0u : segment_of(A.boff, A.G, i);
+}
+
 // ---- P1: locate ------------------------------------------------------------
 
 // The top levels of the descent read segment first keys at multiples of
-// `stride` slots; each CTA copies those (at most LOCATE_CACHE of them) into
-// shared memory once, so a key walks the upper levels in shared memory and
-// only the last log2(stride/seg) levels in HBM. The comparisons and their
-// order are the reference's bit-by-bit descent (gpma.cuh:209-216).
+// `stride` slots; with one graph each CTA copies those (at most LOCATE_CACHE
+// of them) into shared memory once, so a key walks the upper levels in shared
+// memory and only the last log2(stride/seg) levels in HBM. The comparisons and
+// their order are the reference's bit-by-bit descent (gpma.cuh:209-216).
 constexpr uint32_t LOCATE_CACHE = 4096;
 
-__device__ __forceinline__ uint32_t locate_one(const UpdateArgs &A, uint64_t key, uint8_t value, const uint64_t *fk,
+__device__ __forceinline__ uint32_t locate_one(const GraphDesc &D, uint64_t key, uint8_t value, const uint64_t *fk,
                                                uint32_t log2stride) {
-    const uint32_t seg = A.seg;
-    const uint32_t stride = 1u << log2stride;
+    const uint32_t seg = D.seg;
     uint32_t prefix = 0;
-    uint32_t bit = (seg << A.height) >> 1;
-    while (stride <= bit) {
-        if (fk[(prefix | bit) >> log2stride] <= key)
-            prefix |= bit;
-        bit >>= 1;
+    uint32_t bit = (seg << D.height) >> 1;
+    if (fk) {
+        const uint32_t stride = 1u << log2stride;
+        while (stride <= bit) {
+            if (fk[(prefix | bit) >> log2stride] <= key)
+                prefix |= bit;
+            bit >>= 1;
+        }
     }
     while (seg <= bit) {
-        if (A.keys[prefix | bit] <= key)
+        if (D.keys[prefix | bit] <= key)
             prefix |= bit;
         bit >>= 1;
     }
     uint32_t leaf = value == 0 ? SIZE_NONE : prefix;
     // first equal key of the leaf (handle_del_mod scans all seg slots)
-    const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(A.keys + prefix);
+    const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(D.keys + prefix);
     for (uint32_t j = 0; j < (seg >> 1); ++j) {
         ulonglong2 q = p[j];
         uint32_t hit = q.x == key ? 2 * j : (q.y == key ? 2 * j + 1 : SIZE_NONE);
         if (hit != SIZE_NONE) {
-            A.vals[prefix + hit] = value;
+            D.vals[prefix + hit] = value;
             leaf = SIZE_NONE;
             break;
         }
@@ -286,9 +305,8 @@ __device__ __forceinline__ void store_slots(uint64_t *keys, uint8_t *vals, uint3
 }
 
 template <uint32_t W>
-__device__ void warp_windows(const UpdateArgs &A, const uint32_t *wn, const uint32_t *wa, const uint32_t *wb,
-                             uint32_t nw, uint32_t lo, uint32_t hi, const uint64_t *pk, const uint8_t *pv,
-                             unsigned char *smem, unsigned long long &acc) {
+__device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32_t r1, uint32_t level,
+                             const uint64_t *pk, const uint8_t *pv, unsigned char *smem, unsigned long long &acc) {
     constexpr uint32_t G = W >= 128 ? 32 : (W >= 4 ? W / 4 : 1);  // lanes per window
     constexpr uint32_t GPW = 32 / G;                                // windows per warp
     constexpr uint32_t K = W / G;                                   // slots per lane
@@ -302,19 +320,21 @@ __device__ void warp_windows(const UpdateArgs &A, const uint32_t *wn, const uint
     uint8_t *pend_v = reinterpret_cast<uint8_t *>(mk + W);
     uint8_t *cv = pend_v + W;
     uint8_t *mv = cv + W;
-    const uint32_t seg_mask = A.seg - 1, log2seg = A.log2seg;
-    const uint32_t log2F = (31 - __clz(W)) - log2seg;
     const uint32_t total_warps = gridDim.x * (BLOCK / 32);
-    for (uint32_t wbase = (blockIdx.x * (BLOCK / 32) + warp) * GPW; wbase < nw; wbase += total_warps * GPW) {
+    for (uint32_t wbase = r0 + (blockIdx.x * (BLOCK / 32) + warp) * GPW; wbase < r1; wbase += total_warps * GPW) {
         const uint32_t w = wbase + grp;
-        const bool has = w < nw;
-        const uint32_t node = has ? wn[w] : 0, a = has ? wa[w] : 0, b = has ? wb[w] : 0;
+        const bool has = w < r1;
+        const GraphDesc &D = A.gd[has ? L.graph[w] : L.graph[r0]];
+        const uint32_t node = has ? L.node[w] : 0, a = has ? L.a[w] : 0, b = has ? L.b[w] : 0;
+        const uint32_t log2seg = D.log2seg, seg_mask = D.seg - 1;
+        const uint32_t log2F = (31 - __clz(W)) - log2seg;
+        const uint32_t lo = D.lower[level], hi = D.upper[level];
         const uint32_t t0 = node + gl * K;
         uint64_t k[K];
         uint8_t v[K];
         uint32_t c_l = 0;
         if (has) {
-            load_slots<K>(A.keys, A.vals, t0, k, v);
+            load_slots<K>(D.keys, D.vals, t0, k, v);
 #pragma unroll
             for (uint32_t j = 0; j < K; ++j)
                 c_l += (k[j] != KEY_NONE && v[j] != 0);
@@ -367,11 +387,11 @@ __device__ void warp_windows(const UpdateArgs &A, const uint32_t *wn, const uint
                 }
                 if (is_guard(k[j])) {
                     const uint32_t row = (uint32_t)(k[j] >> 32);
-                    if (row < A.row_num)
-                        A.row_offset[row + 1] = node + t;
+                    if (row < D.row_num)
+                        D.row_offset[row + 1] = node + t;
                 }
             }
-            store_slots<K>(A.keys, A.vals, t0, k, v);
+            store_slots<K>(D.keys, D.vals, t0, k, v);
             if (gl == 0)
                 ++acc;
         }
@@ -383,9 +403,9 @@ __device__ void warp_windows(const UpdateArgs &A, const uint32_t *wn, const uint
 
 // ---- windows of 512..CTA_WINDOW_MAX slots: one CTA each ---------------------
 template <uint32_t W>
-__device__ void cta_windows(const UpdateArgs &A, const uint32_t *wn, const uint32_t *wa, const uint32_t *wb,
-                            uint32_t nw, uint32_t lo, uint32_t hi, const uint64_t *pk, const uint8_t *pv,
-                            unsigned char *smem, uint32_t *tmp, unsigned long long &acc) {
+__device__ void cta_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32_t r1, uint32_t level,
+                            const uint64_t *pk, const uint8_t *pv, unsigned char *smem, uint32_t *tmp,
+                            unsigned long long &acc) {
     constexpr uint32_t K = W / BLOCK;
     uint64_t *sk = reinterpret_cast<uint64_t *>(smem);
     uint64_t *ck = sk + W;
@@ -394,15 +414,17 @@ __device__ void cta_windows(const UpdateArgs &A, const uint32_t *wn, const uint3
     uint8_t *cv = sv + W;
     uint8_t *mv = cv + W;
     const uint32_t tid = threadIdx.x;
-    const uint32_t seg_mask = A.seg - 1, log2seg = A.log2seg;
-    const uint32_t log2F = (31 - __clz(W)) - log2seg;
-    for (uint32_t w = blockIdx.x; w < nw; w += gridDim.x) {
-        const uint32_t node = wn[w], a = wa[w], b = wb[w];
+    for (uint32_t w = r0 + blockIdx.x; w < r1; w += gridDim.x) {
+        const GraphDesc &D = A.gd[L.graph[w]];
+        const uint32_t node = L.node[w], a = L.a[w], b = L.b[w];
+        const uint32_t log2seg = D.log2seg, seg_mask = D.seg - 1;
+        const uint32_t log2F = (31 - __clz(W)) - log2seg;
+        const uint32_t lo = D.lower[level], hi = D.upper[level];
 #pragma unroll
         for (uint32_t j = 0; j < K; ++j) {
             uint32_t t = tid + j * BLOCK;
-            sk[t] = A.keys[node + t];
-            sv[t] = A.vals[node + t];
+            sk[t] = D.keys[node + t];
+            sv[t] = D.vals[node + t];
         }
         __syncthreads();
         uint32_t c_l = 0;
@@ -461,12 +483,12 @@ __device__ void cta_windows(const UpdateArgs &A, const uint32_t *wn, const uint3
                     k = mk[f0 + ln];
                     v = mv[f0 + ln];
                 }
-                A.keys[node + t] = k;
-                A.vals[node + t] = v;
+                D.keys[node + t] = k;
+                D.vals[node + t] = v;
                 if (is_guard(k)) {
                     uint32_t row = (uint32_t)(k >> 32);
-                    if (row < A.row_num)
-                        A.row_offset[row + 1] = node + t;
+                    if (row < D.row_num)
+                        D.row_offset[row + 1] = node + t;
                 }
             }
             if (tid == 0)
@@ -479,20 +501,21 @@ __device__ void cta_windows(const UpdateArgs &A, const uint32_t *wn, const uint3
 }
 
 // ---- windows wider than one CTA: the whole grid, chunk by chunk -------------
-__device__ bool grid_windows(const UpdateArgs &A, const uint32_t *wn, const uint32_t *wa, const uint32_t *wb,
-                             uint32_t nw, uint32_t W, uint32_t lo, uint32_t hi, const uint64_t *pk,
-                             const uint8_t *pv, unsigned char *smem, uint32_t *tmp, unsigned long long &acc) {
+__device__ bool grid_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32_t r1, uint32_t W, uint32_t level,
+                             const uint64_t *pk, const uint8_t *pv, unsigned char *smem, uint32_t *tmp,
+                             unsigned long long &acc) {
     const uint32_t cpw = W / CHUNK;
-    const uint32_t total = nw * cpw;
+    const uint32_t total = (r1 - r0) * cpw;
     constexpr uint32_t K = CHUNK / BLOCK;
     // B1: live count of every chunk
     for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
-        uint32_t w = c / cpw, k = c % cpw;
-        uint32_t base = wn[w] + k * CHUNK + threadIdx.x * K;
+        const uint32_t w = r0 + c / cpw, k = c % cpw;
+        const GraphDesc &D = A.gd[L.graph[w]];
+        const uint32_t base = L.node[w] + k * CHUNK + threadIdx.x * K;
         uint32_t cl = 0;
 #pragma unroll
         for (uint32_t j = 0; j < K; ++j)
-            cl += (A.keys[base + j] != KEY_NONE && A.vals[base + j] != 0);
+            cl += (D.keys[base + j] != KEY_NONE && D.vals[base + j] != 0);
         uint32_t t = block_sum(cl, tmp);
         if (threadIdx.x == 0)
             A.chunk_cnt[c] = t;
@@ -500,19 +523,21 @@ __device__ bool grid_windows(const UpdateArgs &A, const uint32_t *wn, const uint
     if (!grid_barrier(&A.st->bar, &A.st->err))
         return false;
     // B2: per window, chunk offsets, live total and the density decision
-    for (uint32_t w = blockIdx.x; w < nw; w += gridDim.x) {
+    for (uint32_t w = r0 + blockIdx.x; w < r1; w += gridDim.x) {
+        const GraphDesc &D = A.gd[L.graph[w]];
+        uint32_t *cc = A.chunk_cnt + (w - r0) * cpw;
         uint32_t run = 0;
         for (uint32_t k0 = 0; k0 < cpw; k0 += BLOCK) {
             uint32_t k = k0 + threadIdx.x;
-            uint32_t v = k < cpw ? A.chunk_cnt[w * cpw + k] : 0;
+            uint32_t v = k < cpw ? cc[k] : 0;
             uint32_t tot;
             uint32_t ex = block_excl_scan(v, &tot, tmp);
             if (k < cpw)
-                A.chunk_cnt[w * cpw + k] = run + ex;
+                cc[k] = run + ex;
             run += tot;
         }
-        uint32_t M = run + (wb[w] - wa[w]);
-        bool accept = lo <= M && M <= hi;
+        uint32_t M = run + (L.b[w] - L.a[w]);
+        bool accept = D.lower[level] <= M && M <= D.upper[level];
         if (threadIdx.x == 0) {
             A.wflag[w] = accept ? 1u : 0u;
             A.wlive[w] = run;
@@ -522,20 +547,21 @@ __device__ bool grid_windows(const UpdateArgs &A, const uint32_t *wn, const uint
     }
     if (!grid_barrier(&A.st->bar, &A.st->err))
         return false;
-    // B3: stable compaction of accepted windows into the scratch arrays
+    // B3: stable compaction of accepted windows into the graph's scratch arrays
     for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
-        uint32_t w = c / cpw, k = c % cpw;
+        const uint32_t w = r0 + c / cpw, k = c % cpw;
         if (!A.wflag[w])
             continue;
-        uint32_t node = wn[w];
-        uint32_t base = node + k * CHUNK + threadIdx.x * K;
+        const GraphDesc &D = A.gd[L.graph[w]];
+        const uint32_t node = L.node[w];
+        const uint32_t base = node + k * CHUNK + threadIdx.x * K;
         uint64_t kk[K];
         uint8_t vv[K];
         uint32_t cl = 0;
 #pragma unroll
         for (uint32_t j = 0; j < K; ++j) {
-            kk[j] = A.keys[base + j];
-            vv[j] = A.vals[base + j];
+            kk[j] = D.keys[base + j];
+            vv[j] = D.vals[base + j];
             cl += (kk[j] != KEY_NONE && vv[j] != 0);
         }
         uint32_t tot;
@@ -543,8 +569,8 @@ __device__ bool grid_windows(const UpdateArgs &A, const uint32_t *wn, const uint
 #pragma unroll
         for (uint32_t j = 0; j < K; ++j) {
             if (kk[j] != KEY_NONE && vv[j] != 0) {
-                A.skeys[o] = kk[j];
-                A.svals[o] = vv[j];
+                D.skeys[o] = kk[j];
+                D.svals[o] = vv[j];
                 ++o;
             }
         }
@@ -554,28 +580,42 @@ __device__ bool grid_windows(const UpdateArgs &A, const uint32_t *wn, const uint
     // B4: merge with the window's insertions and redispatch chunk by chunk
     uint64_t *mk = reinterpret_cast<uint64_t *>(smem);
     uint8_t *mv = reinterpret_cast<uint8_t *>(mk + CHUNK);
-    const uint32_t log2F = (31 - __clz(W)) - A.log2seg;
     for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
-        uint32_t w = c / cpw, k = c % cpw;
+        const uint32_t w = r0 + c / cpw, k = c % cpw;
         if (!A.wflag[w])
             continue;
-        uint32_t node = wn[w], a = wa[w];
-        redispatch_chunk(A.keys, A.vals, A.row_offset, A.row_num, node, A.log2seg, log2F, k * CHUNK, CHUNK,
-                         A.skeys + node, A.svals + node, A.wlive[w], pk + a, pv + a, wb[w] - a, KEY_NONE,
-                         mk, mv);
+        const GraphDesc &D = A.gd[L.graph[w]];
+        const uint32_t node = L.node[w], a = L.a[w];
+        const uint32_t log2F = (31 - __clz(W)) - D.log2seg;
+        redispatch_chunk(D.keys, D.vals, D.row_offset, D.row_num, node, D.log2seg, log2F, k * CHUNK, CHUNK,
+                         D.skeys + node, D.svals + node, A.wlive[w], pk + a, pv + a, L.b[w] - a, KEY_NONE, mk, mv);
     }
     return true;
 }
 
 template <uint32_t W>
-__device__ __forceinline__ void small_dispatch(const UpdateArgs &A, const uint32_t *wn, const uint32_t *wa,
-                                               const uint32_t *wb, uint32_t nw, uint32_t lo, uint32_t hi,
-                                               const uint64_t *pk, const uint8_t *pv, unsigned char *smem,
-                                               uint32_t *tmp, unsigned long long &acc) {
+__device__ __forceinline__ void small_dispatch(const UpdateArgs &A, Windows L, uint32_t r0, uint32_t r1,
+                                               uint32_t level, const uint64_t *pk, const uint8_t *pv,
+                                               unsigned char *smem, uint32_t *tmp, unsigned long long &acc) {
     if constexpr (W <= WARP_WINDOW_MAX)
-        warp_windows<W>(A, wn, wa, wb, nw, lo, hi, pk, pv, smem, acc);
+        warp_windows<W>(A, L, r0, r1, level, pk, pv, smem, acc);
     else
-        cta_windows<W>(A, wn, wa, wb, nw, lo, hi, pk, pv, smem, tmp, acc);
+        cta_windows<W>(A, L, r0, r1, level, pk, pv, smem, tmp, acc);
+}
+
+// First window in [0, nw) whose graph has segment length >= s (windows are
+// ordered by graph, graphs by segment length).
+__device__ __forceinline__ uint32_t first_window_of_seg(const UpdateArgs &A, const uint32_t *wg, uint32_t nw,
+                                                        uint32_t s) {
+    uint32_t lo = 0, hi = nw;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (A.gd[wg[mid]].seg < s)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
 }
 
 // Minimum resident CTAs per SM the register allocation must allow (build
@@ -588,18 +628,21 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint32_t tmp[BLOCK / 32 + 1];
     DeviceStatus *st = A.st;
+    const bool stamper = blockIdx.x == 0 && threadIdx.x == 0;
+    if (stamper)
+        st->stamp[0] = globaltimer_ns();
 
-    // S: stable radix sort of the batch (gpma.cuh:977); digit passes are
-    // separated by grid barriers, constant digits skipped.
-    sort_histogram(A.bk[0], A.n, A.sort_hist, st, A.check_keys, reinterpret_cast<uint32_t *>(smem));
+    // S: stable radix sort of each graph's batch (gpma.cuh:977); digit passes
+    // are separated by grid barriers, digits constant over all batches skipped.
+    sort_histogram(A.bk[0], A.boff, A.G, A.sort_hist, st, A.check_keys, reinterpret_cast<uint32_t *>(smem));
     if (!grid_barrier(&st->bar, &st->err))
         return;
     if (ld_volatile(&st->invalid_keys) != 0)
         return;  // reserved-column keys: reject the batch before any change
     uint32_t sel = 0;
     {
-        const uint32_t trivial = sort_trivial_mask(A.sort_hist, A.n);
-        const uint32_t tiles = (A.n + SORT_TILE - 1) / SORT_TILE;
+        const uint32_t trivial = sort_trivial_mask(A.sort_hist + (size_t)(A.G == 1 ? 0 : A.G) * 2048, A.n);
+        const uint32_t tiles = A.toff[A.G];
         __shared__ uint32_t s_tile;
         for (int p = 0; p < 8; ++p) {
             if (trivial & (1u << p))
@@ -616,7 +659,8 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
                 __syncthreads();
                 if (tile >= tiles)
                     break;
-                sort_tile(p, tile, ink, inv, outk, outv, A.n, A.sort_hist, A.sort_status, st, smem, tmp);
+                sort_tile(p, tile, ink, inv, outk, outv, A.boff, A.toff, A.G, A.sort_hist, A.sort_status, st, smem,
+                          tmp);
             }
             sel ^= 1u;
             if (!grid_barrier(&st->bar, &st->err))
@@ -630,26 +674,36 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
 #define CNT(id) ((id) ? A.cta_cnt + G : A.cta_cnt)
 #define CNTI(id) ((id) ? A.cta_cnt + 3 * G : A.cta_cnt + 2 * G)
     unsigned long long acc = 0, acc_slots = 0;
+    if (stamper)
+        st->stamp[1] = globaltimer_ns();
 
-    // P1: locate every update, applying deletes / modifies in place. The top
-    // of the descent comes from a shared-memory copy of the first keys at
-    // every `stride`-th slot.
+    // P1: locate every update, applying deletes / modifies in place. With one
+    // graph, the top of the descent comes from a shared-memory copy of the
+    // first keys at every `stride`-th slot.
     {
-        const uint32_t segs = A.size >> A.log2seg;
-        const uint32_t cached = segs < LOCATE_CACHE ? segs : LOCATE_CACHE;
-        const uint32_t log2stride = (31 - __clz(A.size / cached));
-        uint64_t *fk = reinterpret_cast<uint64_t *>(smem);
-        for (uint32_t j = threadIdx.x; j < cached; j += BLOCK)
-            fk[j] = A.keys[(size_t)j << log2stride];
-        __syncthreads();
+        const uint64_t *fk = nullptr;
+        uint32_t log2stride = 0;
+        if (A.G == 1) {
+            const GraphDesc &D = A.gd[0];
+            const uint32_t segs = D.size >> D.log2seg;
+            const uint32_t cached = segs < LOCATE_CACHE ? segs : LOCATE_CACHE;
+            log2stride = 31 - __clz(D.size / cached);
+            uint64_t *f = reinterpret_cast<uint64_t *>(smem);
+            for (uint32_t j = threadIdx.x; j < cached; j += BLOCK)
+                f[j] = D.keys[(size_t)j << log2stride];
+            __syncthreads();
+            fk = f;
+        }
         for (uint32_t i = blockIdx.x * BLOCK + threadIdx.x; i < A.n; i += G * BLOCK)
-            A.leaf[i] = locate_one(A, bk[i], bv[i], fk, log2stride);
+            A.leaf[i] = locate_one(A.gd[graph_of(A, i)], bk[i], bv[i], fk, log2stride);
         __syncthreads();
     }
     if (!grid_barrier(&st->bar, &st->err))
         return;
+    if (stamper)
+        st->stamp[2] = globaltimer_ns();
 
-    // P2: stable compaction of the insertions.
+    // P2: stable compaction of the insertions (with their graph).
     uint32_t lo, hi;
     cta_range(A.n, lo, hi);
     {
@@ -673,26 +727,30 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
             A.ikeys[0][base + ex] = bk[i];
             A.ivals[0][base + ex] = bv[i];
             A.ileaf[base + ex] = A.leaf[i];
+            A.igraph[base + ex] = graph_of(A, i);
         }
         base += tot;
     }
     scan_id ^= 1;
     if (!grid_barrier(&st->bar, &st->err))
         return;
-    if (m >= SIGNIFICANT_INSERTS) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (A.G == 1 && m >= SIGNIFICANT_INSERTS) {
+        if (stamper) {
             st->significant = 1;
             st->inserts = m;
+            A.gs[0].inserts = m;
+            A.gs[0].ins_base = 0;
         }
         return;
     }
 
-    // P3: run-length grouping of the insertions by leaf -> level-0 windows.
+    // P3: run-length grouping of the insertions by (graph, leaf) -> level-0
+    // windows; also each graph's first insertion and its count.
     cta_range(m, lo, hi);
     {
         uint32_t cl = 0;
         for (uint32_t j = lo + threadIdx.x; j < hi; j += BLOCK)
-            cl += (j == 0 || A.ileaf[j] != A.ileaf[j - 1]);
+            cl += (j == 0 || A.ileaf[j] != A.ileaf[j - 1] || A.igraph[j] != A.igraph[j - 1]);
         uint32_t t = block_sum(cl, tmp);
         if (threadIdx.x == 0)
             CNT(scan_id)[blockIdx.x] = t;
@@ -704,16 +762,27 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
     for (uint32_t j0 = lo; j0 < hi; j0 += BLOCK) {
         uint32_t j = j0 + threadIdx.x;
         bool in = j < hi;
-        uint32_t head = (in && (j == 0 || A.ileaf[j] != A.ileaf[j - 1])) ? 1u : 0u;
+        uint32_t head = 0;
+        if (in) {
+            const uint32_t gj = A.igraph[j];
+            const bool new_graph = j == 0 || A.igraph[j - 1] != gj;
+            head = (new_graph || A.ileaf[j] != A.ileaf[j - 1]) ? 1u : 0u;
+            if (new_graph)
+                A.gs[gj].ins_base = j;
+            if (j + 1 == m || A.igraph[j + 1] != gj)
+                A.gs[gj].inserts = j + 1;  // end for now; made a count by the host
+        }
         uint32_t tot;
         uint32_t ex = block_excl_scan(head, &tot, tmp);
         if (in) {
             uint32_t e = base + ex;
             if (head) {
                 A.wnode[0][e] = A.ileaf[j];
+                A.wgraph[0][e] = A.igraph[j];
                 A.wa[0][e] = j;
             }
-            if (j + 1 == m || A.ileaf[j + 1] != A.ileaf[j])
+            const bool last = j + 1 == m || A.ileaf[j + 1] != A.ileaf[j] || A.igraph[j + 1] != A.igraph[j];
+            if (last)
                 A.wb[0][e + head - 1] = j + 1;
         }
         base += tot;
@@ -721,47 +790,65 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
     scan_id ^= 1;
     if (!grid_barrier(&st->bar, &st->err))
         return;
+    if (stamper)
+        st->stamp[3] = globaltimer_ns();
 
     // Level loop. Windows and their pending insertions live in ping-pong
     // buffers selected by `cur`; each window's insertions are the contiguous
     // range [wa, wb) of the current insertion buffer.
     uint32_t cur = 0, level = 0;
-    __shared__ uint32_t s_nb[BLOCK], s_src[BLOCK], s_cnt[BLOCK];
-    for (; level <= A.height && nw > 0; ++level) {
-        const uint32_t W = A.seg << level;
-        const uint32_t lob = A.lower[level], hib = A.upper[level];
-        const uint32_t *wn = cur ? A.wnode[1] : A.wnode[0];
-        const uint32_t *wa = cur ? A.wa[1] : A.wa[0];
-        const uint32_t *wb = cur ? A.wb[1] : A.wb[0];
+    __shared__ uint32_t s_nb[BLOCK], s_src[BLOCK], s_cnt[BLOCK], s_dst[BLOCK];
+    for (; level <= A.max_height && nw > 0; ++level) {
+        Windows L;
+        L.node = cur ? A.wnode[1] : A.wnode[0];
+        L.graph = cur ? A.wgraph[1] : A.wgraph[0];
+        L.a = cur ? A.wa[1] : A.wa[0];
+        L.b = cur ? A.wb[1] : A.wb[0];
         const uint64_t *pk = cur ? A.ikeys[1] : A.ikeys[0];
         const uint8_t *pv = cur ? A.ivals[1] : A.ivals[0];
-        const unsigned long long before = acc;
-        switch (W) {
-        case 2: small_dispatch<2>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
-        case 4: small_dispatch<4>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
-        case 8: small_dispatch<8>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
-        case 16: small_dispatch<16>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
-        case 32: small_dispatch<32>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
-        case 64: small_dispatch<64>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
-        case 128: small_dispatch<128>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
-        case 256: small_dispatch<256>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
-        case 512: small_dispatch<512>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
-        case 1024: small_dispatch<1024>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
-        case 2048: small_dispatch<2048>(A, wn, wa, wb, nw, lob, hib, pk, pv, smem, tmp, acc); break;
-        default:
-            if (!grid_windows(A, wn, wa, wb, nw, W, lob, hib, pk, pv, smem, tmp, acc))
-                return;
+        // one run of windows per segment length (a single run for one graph)
+        for (uint32_t s = 2; s <= 32; s <<= 1) {
+            uint32_t r0 = 0, r1 = nw;
+            if (A.G > 1) {
+                r0 = first_window_of_seg(A, L.graph, nw, s);
+                r1 = first_window_of_seg(A, L.graph, nw, 2 * s);
+            } else if (A.gd[0].seg != s) {
+                continue;
+            }
+            if (r0 >= r1)
+                continue;
+            const uint32_t W = s << level;
+            const unsigned long long before = acc;
+            switch (W) {
+            case 2: small_dispatch<2>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
+            case 4: small_dispatch<4>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
+            case 8: small_dispatch<8>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
+            case 16: small_dispatch<16>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
+            case 32: small_dispatch<32>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
+            case 64: small_dispatch<64>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
+            case 128: small_dispatch<128>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
+            case 256: small_dispatch<256>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
+            case 512: small_dispatch<512>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
+            case 1024: small_dispatch<1024>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
+            case 2048: small_dispatch<2048>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
+            default:
+                if (!grid_windows(A, L, r0, r1, W, level, pk, pv, smem, tmp, acc))
+                    return;
+            }
+            acc_slots += (acc - before) * (unsigned long long)W;
         }
-        acc_slots += (acc - before) * (unsigned long long)W;
         if (!grid_barrier(&st->bar, &st->err))
             return;
         // Next level. Rejected windows keep their insertions, which are
         // compacted into the other buffer (new offsets from one scan over the
         // windows, as compact_insertions does over insertions, gpma.cuh:1022);
         // a rejected right sibling joins its rejected left sibling in the
-        // parent window (up_level, gpma.cuh:881-889 + regrouping).
+        // parent window (up_level, gpma.cuh:881-889 + regrouping). A rejected
+        // root window leaves its insertions to the root rebalance: they go to
+        // the graph's area of the remaining-insertion buffer.
         const uint32_t nxt = cur ^ 1;
         uint32_t *nwn = nxt ? A.wnode[1] : A.wnode[0];
+        uint32_t *nwg = nxt ? A.wgraph[1] : A.wgraph[0];
         uint32_t *nwa = nxt ? A.wa[1] : A.wa[0];
         uint32_t *nwb = nxt ? A.wb[1] : A.wb[0];
         uint64_t *nk = nxt ? A.ikeys[1] : A.ikeys[0];
@@ -772,9 +859,14 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
             for (uint32_t w = lo + threadIdx.x; w < hi; w += BLOCK) {
                 if (A.wflag[w])
                     continue;
-                ci += wb[w] - wa[w];
-                uint32_t par = wn[w] & ~W;
-                bool merged = w > 0 && !A.wflag[w - 1] && (wn[w - 1] & ~W) == par;
+                const uint32_t g = L.graph[w];
+                if (level >= A.gd[g].height)
+                    continue;  // root window: to the remaining buffer
+                const uint32_t W = A.gd[g].seg << level;
+                ci += L.b[w] - L.a[w];
+                const uint32_t par = L.node[w] & ~W;
+                const bool merged =
+                    w > 0 && !A.wflag[w - 1] && L.graph[w - 1] == g && (L.node[w - 1] & ~W) == par;
                 ch += merged ? 0u : 1u;
             }
             uint32_t th = block_sum(ch, tmp);
@@ -792,34 +884,48 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
         for (uint32_t w0 = lo; w0 < hi; w0 += BLOCK) {
             const uint32_t w = w0 + threadIdx.x;
             const bool rej = w < hi && !A.wflag[w];
-            const uint32_t c = rej ? wb[w] - wa[w] : 0u;
+            const uint32_t g = rej ? L.graph[w] : 0u;
+            const bool root = rej && level >= A.gd[g].height;
+            const bool carry = rej && !root;
+            const uint32_t c = rej ? L.b[w] - L.a[w] : 0u;
             uint32_t tot_i;
-            const uint32_t nb = base_i + block_excl_scan(c, &tot_i, tmp);
-            uint32_t head = 0, par = 0;
-            if (rej) {
-                par = wn[w] & ~W;
-                bool merged = w > 0 && !A.wflag[w - 1] && (wn[w - 1] & ~W) == par;
+            const uint32_t nb = base_i + block_excl_scan(carry ? c : 0u, &tot_i, tmp);
+            uint32_t head = 0, par = 0, W = 0;
+            if (carry) {
+                W = A.gd[g].seg << level;
+                par = L.node[w] & ~W;
+                const bool merged =
+                    w > 0 && !A.wflag[w - 1] && L.graph[w - 1] == g && (L.node[w - 1] & ~W) == par;
                 head = merged ? 0u : 1u;
             }
             uint32_t tot_h;
             const uint32_t ex = block_excl_scan(head, &tot_h, tmp);
             if (head) {
                 const uint32_t e = base + ex;
-                const bool right = w + 1 < nw && !A.wflag[w + 1] && (wn[w + 1] & ~W) == par;
+                const bool right =
+                    w + 1 < nw && !A.wflag[w + 1] && L.graph[w + 1] == g && (L.node[w + 1] & ~W) == par;
                 nwn[e] = par;
+                nwg[e] = g;
                 nwa[e] = nb;
-                nwb[e] = nb + c + (right ? wb[w + 1] - wa[w + 1] : 0u);
+                nwb[e] = nb + c + (right ? L.b[w + 1] - L.a[w + 1] : 0u);
             }
-            s_nb[threadIdx.x] = nb;
-            s_src[threadIdx.x] = rej ? wa[w] : 0u;
-            s_cnt[threadIdx.x] = c;
+            if (root)
+                A.gs[g].remaining = c;
+            // copy plan: carried windows to the next buffer, root windows to
+            // the remaining-insertion buffer at the graph's first insertion
+            s_src[threadIdx.x] = rej ? L.a[w] : 0u;
+            s_cnt[threadIdx.x] = rej ? c : 0u;
+            s_nb[threadIdx.x] = carry ? nb : (root ? A.gs[g].ins_base : 0u);
+            s_dst[threadIdx.x] = root ? 1u : 0u;
             __syncthreads();
             // copy the kept insertions, one warp per window of this tile
             for (uint32_t t = threadIdx.x >> 5; t < BLOCK; t += BLOCK / 32) {
                 const uint32_t cc = s_cnt[t], from = s_src[t], to = s_nb[t];
+                uint64_t *dk = s_dst[t] ? A.rkeys : nk;
+                uint8_t *dv = s_dst[t] ? A.rvals : nv;
                 for (uint32_t e = threadIdx.x & 31; e < cc; e += 32) {
-                    nk[to + e] = pk[from + e];
-                    nv[to + e] = pv[from + e];
+                    dk[to + e] = pk[from + e];
+                    dv[to + e] = pv[from + e];
                 }
             }
             __syncthreads();
@@ -832,8 +938,9 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
         nw = nw_next;
         cur = nxt;
     }
+    if (stamper)
+        st->stamp[4] = globaltimer_ns();
 
-    unsigned long long acc_b = acc;
     // one atomic per CTA for the statistics
     __shared__ unsigned long long s_acc[2];
     if (threadIdx.x == 0) {
@@ -841,8 +948,8 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
         s_acc[1] = 0;
     }
     __syncthreads();
-    if (acc_b)
-        atomicAdd(&s_acc[0], acc_b);
+    if (acc)
+        atomicAdd(&s_acc[0], acc);
     if (acc_slots)
         atomicAdd(&s_acc[1], acc_slots);
     __syncthreads();
@@ -852,18 +959,12 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
         if (s_acc[1])
             atomicAdd(&st->accepted_slots, s_acc[1]);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (stamper) {
         st->levels = level;
         st->inserts = m;
-        if (nw > 0) {
-            const uint32_t ra = (cur ? A.wa[1] : A.wa[0])[0], rb = (cur ? A.wb[1] : A.wb[0])[0];
-            st->remaining = rb - ra;
-            st->rem_a = ra;
-            st->rem_buf = cur;
-        }
+    }
 #undef CNT
 #undef CNTI
-    }
 }
 
 // ---- whole-array kernels for the root resize and the bulk rebuild ----------
@@ -959,11 +1060,9 @@ int grid_for(uint64_t work, int sms, int per_sm) {
     return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, (uint64_t)sms * per_sm));
 }
 
-// resize_gpma + (root rebalance | significant_insert) on the device.
-gpma_status root_rebuild(gpma_graph *g, bool significant, uint32_t pend_buf, uint32_t pend_a, uint32_t pend_n,
-                         cudaStream_t s) {
-    const uint64_t *pend_k = g->ikeys[pend_buf] + pend_a;
-    const uint8_t *pend_v = g->ivals[pend_buf] + pend_a;
+// resize_gpma + (root rebalance | significant_insert) of one graph.
+gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k, const uint8_t *pend_v,
+                         uint32_t pend_n, cudaStream_t s) {
     const uint32_t size = g->geo.size;
     const uint32_t chunks = (size + CHUNK - 1) / CHUNK;
     prof_mark(g, 0, s);
@@ -971,7 +1070,7 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, uint32_t pend_buf, uin
     // 1. stable compaction of the live slots (resize_gpma, gpma.cuh:909-915)
     chunk_live_kernel<<<grid_for((uint64_t)chunks * BLOCK, g->sms, 8), BLOCK, 0, s>>>(g->keys, g->values, size,
                                                                                        g->chunk_cnt);
-    uint32_t *d_total = reinterpret_cast<uint32_t *>(&g->status->pad);
+    uint32_t *d_total = g->chunk_cnt + chunks;
     chunk_scan_kernel<<<1, BLOCK, 0, s>>>(g->chunk_cnt, chunks, d_total);
     chunk_compact_kernel<<<grid_for((uint64_t)chunks * BLOCK, g->sms, 8), BLOCK, 0, s>>>(g->keys, g->values, size,
                                                                                           g->chunk_cnt, g->skeys,
@@ -1043,7 +1142,6 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, uint32_t pend_buf, uin
     GPMA_CUDA(cudaGetLastError());
     prof_mark(g, 1, s);
     g->geo = geo;
-    GPMA_TRY(upload_geometry(g, s));
     GPMA_CUDA(cudaStreamSynchronize(s));
     g->prof.rebuild_ms += prof_elapsed(g, 0, 1);
     // the scratch must cover the whole array for later wide windows
@@ -1051,19 +1149,44 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, uint32_t pend_buf, uin
     return GPMA_OK;
 }
 
+GraphDesc describe(const gpma_graph *g) {
+    GraphDesc d{};
+    d.keys = g->keys;
+    d.vals = g->values;
+    d.row_offset = g->row_offset;
+    d.skeys = g->skeys;
+    d.svals = g->svals;
+    d.row_num = g->row_num;
+    d.size = g->geo.size;
+    d.seg = g->geo.seg;
+    d.log2seg = fls32(g->geo.seg) - 1;
+    d.height = g->geo.height;
+    for (uint32_t i = 0; i <= g->geo.height && i < MAX_LEVELS; ++i) {
+        d.lower[i] = g->geo.lower[i];
+        d.upper[i] = g->geo.upper[i];
+    }
+    return d;
+}
+
+int g_update_grid[64] = {};
+
 }  // namespace
 
-gpma_status upload_geometry(gpma_graph *g, cudaStream_t s) {
-    uint32_t buf[64] = {0};
-    for (uint32_t i = 0; i <= g->geo.height && i < 32; ++i) {
-        buf[i] = g->geo.lower[i];
-        buf[32 + i] = g->geo.upper[i];
+int update_grid_size(int sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64)
+        dev = 0;
+    if (g_update_grid[dev] == 0) {
+        if (cudaFuncSetAttribute(update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)UPDATE_SMEM) !=
+            cudaSuccess)
+            return 0;
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, update_kernel, BLOCK, UPDATE_SMEM) != cudaSuccess)
+            return 0;
+        g_update_grid[dev] = sms * std::min(per_sm, 4);
     }
-    GPMA_CUDA(cudaMemcpyAsync(g->d_lower, buf, 32 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    GPMA_CUDA(cudaMemcpyAsync(g->d_upper, buf + 32, 32 * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    // the host buffer is on the stack: wait for the copies
-    GPMA_CUDA(cudaStreamSynchronize(s));
-    return GPMA_OK;
+    return g_update_grid[dev];
 }
 
 gpma_status ensure_scratch(gpma_graph *g, uint32_t slots) {
@@ -1080,119 +1203,230 @@ gpma_status ensure_scratch(gpma_graph *g, uint32_t slots) {
     return GPMA_OK;
 }
 
-gpma_status ensure_batch(gpma_graph *g, uint64_t n) {
-    if (n <= g->batch_cap && g->bkeys[0])
-        return GPMA_OK;
-    uint64_t cap = std::max<uint64_t>(n, 1024);
+void free_buffers(BatchBuffers &b) {
     for (int i = 0; i < 2; ++i) {
-        dev_free(g->bkeys[i]);
-        dev_free(g->bvals[i]);
-        dev_free(g->wnode[i]);
-        dev_free(g->wa[i]);
-        dev_free(g->wb[i]);
+        dev_free(b.bkeys[i]);
+        dev_free(b.bvals[i]);
+        dev_free(b.ikeys[i]);
+        dev_free(b.ivals[i]);
+        dev_free(b.wnode[i]);
+        dev_free(b.wgraph[i]);
+        dev_free(b.wa[i]);
+        dev_free(b.wb[i]);
     }
-    dev_free(g->leaf);
-    for (int i = 0; i < 2; ++i) {
-        dev_free(g->ikeys[i]);
-        dev_free(g->ivals[i]);
+    dev_free(b.leaf);
+    dev_free(b.ileaf);
+    dev_free(b.igraph);
+    dev_free(b.wflag);
+    dev_free(b.wlive);
+    dev_free(b.rkeys);
+    dev_free(b.rvals);
+    dev_free(b.sort_tiles);
+    dev_free(b.sort_status);
+    dev_free(b.sort_hist);
+    dev_free(b.gd);
+    dev_free(b.gs);
+    dev_free(b.boff);
+    dev_free(b.toff);
+    dev_free(b.chunk_cnt);
+    dev_free(b.cta_cnt);
+    dev_free(b.status);
+    if (b.h_status)
+        cudaFreeHost(b.h_status);
+    if (b.h_gs)
+        cudaFreeHost(b.h_gs);
+    b.h_status = nullptr;
+    b.h_gs = nullptr;
+    b.cap = 0;
+    b.gcap = 0;
+    b.hist_cap = 0;
+    b.chunk_cap = 0;
+    b.sort_status_cap = 0;
+}
+
+gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
+    if (!b.status) {
+        GPMA_TRY(dev_alloc(&b.status, 1));
+        GPMA_TRY(dev_alloc(&b.sort_tiles, 8));
+        cudaError_t e = cudaMallocHost((void **)&b.h_status, sizeof(DeviceStatus));
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaMallocHost(status)");
     }
-    dev_free(g->ileaf);
-    dev_free(g->wflag);
-    dev_free(g->wlive);
-    g->batch_cap = 0;
-    for (int i = 0; i < 2; ++i) {
-        GPMA_TRY(dev_alloc(&g->bkeys[i], cap));
-        GPMA_TRY(dev_alloc(&g->bvals[i], cap));
-        GPMA_TRY(dev_alloc(&g->wnode[i], cap));
-        GPMA_TRY(dev_alloc(&g->wa[i], cap));
-        GPMA_TRY(dev_alloc(&g->wb[i], cap));
+    if (n > b.cap || !b.bkeys[0]) {
+        uint64_t cap = std::max<uint64_t>(n, 1024);
+        for (int i = 0; i < 2; ++i) {
+            dev_free(b.bkeys[i]);
+            dev_free(b.bvals[i]);
+            dev_free(b.ikeys[i]);
+            dev_free(b.ivals[i]);
+            dev_free(b.wnode[i]);
+            dev_free(b.wgraph[i]);
+            dev_free(b.wa[i]);
+            dev_free(b.wb[i]);
+        }
+        dev_free(b.leaf);
+        dev_free(b.ileaf);
+        dev_free(b.igraph);
+        dev_free(b.wflag);
+        dev_free(b.wlive);
+        dev_free(b.rkeys);
+        dev_free(b.rvals);
+        b.cap = 0;
+        for (int i = 0; i < 2; ++i) {
+            GPMA_TRY(dev_alloc(&b.bkeys[i], cap));
+            GPMA_TRY(dev_alloc(&b.bvals[i], cap));
+            GPMA_TRY(dev_alloc(&b.ikeys[i], cap));
+            GPMA_TRY(dev_alloc(&b.ivals[i], cap));
+            GPMA_TRY(dev_alloc(&b.wnode[i], cap));
+            GPMA_TRY(dev_alloc(&b.wgraph[i], cap));
+            GPMA_TRY(dev_alloc(&b.wa[i], cap));
+            GPMA_TRY(dev_alloc(&b.wb[i], cap));
+        }
+        GPMA_TRY(dev_alloc(&b.leaf, cap));
+        GPMA_TRY(dev_alloc(&b.ileaf, cap));
+        GPMA_TRY(dev_alloc(&b.igraph, cap));
+        GPMA_TRY(dev_alloc(&b.wflag, cap));
+        GPMA_TRY(dev_alloc(&b.wlive, cap));
+        GPMA_TRY(dev_alloc(&b.rkeys, cap));
+        GPMA_TRY(dev_alloc(&b.rvals, cap));
+        b.cap = cap;
     }
-    GPMA_TRY(dev_alloc(&g->leaf, cap));
-    for (int i = 0; i < 2; ++i) {
-        GPMA_TRY(dev_alloc(&g->ikeys[i], cap));
-        GPMA_TRY(dev_alloc(&g->ivals[i], cap));
+    if (graphs > b.gcap || !b.gd) {
+        uint32_t gc = std::max<uint32_t>(graphs, 1);
+        dev_free(b.gd);
+        dev_free(b.gs);
+        dev_free(b.boff);
+        dev_free(b.toff);
+        if (b.h_gs)
+            cudaFreeHost(b.h_gs);
+        b.h_gs = nullptr;
+        b.gcap = 0;
+        GPMA_TRY(dev_alloc(&b.gd, gc));
+        GPMA_TRY(dev_alloc(&b.gs, gc));
+        GPMA_TRY(dev_alloc(&b.boff, gc + 1));
+        GPMA_TRY(dev_alloc(&b.toff, gc + 1));
+        cudaError_t e = cudaMallocHost((void **)&b.h_gs, sizeof(GraphStatus) * gc);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaMallocHost(graph status)");
+        b.gcap = gc;
     }
-    GPMA_TRY(dev_alloc(&g->ileaf, cap));
-    GPMA_TRY(dev_alloc(&g->wflag, cap));
-    GPMA_TRY(dev_alloc(&g->wlive, cap));
-    g->batch_cap = cap;
     return GPMA_OK;
 }
 
-// Runs the update of the n-key batch already staged in bkeys[0]/bvals[0].
-gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys) {
-    if (g->update_grid == 0) {
-        GPMA_CUDA(cudaFuncSetAttribute(update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)UPDATE_SMEM));
-        GPMA_CUDA(cudaFuncSetAttribute(rebuild_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(CHUNK * 9)));
-        int per_sm = 0;
-        GPMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, update_kernel, BLOCK, UPDATE_SMEM));
-        if (per_sm < 1) {
-            set_error("update kernel cannot be resident (occupancy 0)");
-            return GPMA_ERR_CUDA;
+gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32_t k, BatchBuffers &buf, int sms,
+                          cudaStream_t s, bool check_keys, bool profiling, cudaEvent_t *ev, gpma_profile *prof) {
+    const uint64_t n = off[k];
+    if (n == 0)
+        return GPMA_OK;
+    const int grid = update_grid_size(sms);
+    if (grid == 0) {
+        set_error("update kernel cannot be resident");
+        return GPMA_ERR_CUDA;
+    }
+    GPMA_TRY(ensure_buffers(buf, n, k));
+    if (!buf.cta_cnt)
+        GPMA_TRY(dev_alloc(&buf.cta_cnt, 4ull * grid));
+    // per-graph tables: descriptors, batch offsets, sort tile offsets
+    buf.h_gd.resize(k);
+    buf.h_off.assign(2ull * (k + 1), 0);
+    uint32_t max_height = 0;
+    uint64_t chunk_need = 1;
+    for (uint32_t i = 0; i < k; ++i) {
+        buf.h_gd[i] = describe(graphs[i]);
+        max_height = std::max(max_height, graphs[i]->geo.height);
+        chunk_need += graphs[i]->geo.size / CHUNK + 1;
+        if (i > 0 && graphs[i]->geo.seg < graphs[i - 1]->geo.seg) {
+            set_error("update_graphs: graphs must be ordered by segment length");
+            return GPMA_ERR_INVALID;
         }
-        g->update_grid = g->sms * std::min(per_sm, 4);
-        GPMA_TRY(dev_alloc(&g->cta_cnt, 4ull * g->update_grid));
     }
-    const uint32_t tiles = (uint32_t)((n + SORT_TILE - 1) / SORT_TILE);
+    for (uint32_t i = 0; i <= k; ++i) {
+        buf.h_off[i] = (uint32_t)off[i];
+        if (i > 0) {
+            const uint64_t ni = off[i] - off[i - 1];
+            buf.h_off[k + 1 + i] = buf.h_off[k + i] + (uint32_t)((ni + SORT_TILE - 1) / SORT_TILE);
+        }
+    }
+    const uint32_t tiles = buf.h_off[2 * k + 1];
     const uint64_t status_words = 8ull * tiles * 256;
-    if (status_words > g->sort_status_cap) {
-        dev_free(g->sort_status);
-        GPMA_TRY(dev_alloc(&g->sort_status, status_words));
-        g->sort_status_cap = status_words;
+    if (status_words > buf.sort_status_cap) {
+        dev_free(buf.sort_status);
+        GPMA_TRY(dev_alloc(&buf.sort_status, status_words));
+        buf.sort_status_cap = status_words;
     }
-    GPMA_CUDA(cudaMemsetAsync(g->status, 0, sizeof(DeviceStatus), s));
-    GPMA_CUDA(cudaMemsetAsync(g->sort_hist, 0, 8 * 256 * sizeof(uint32_t), s));
-    GPMA_CUDA(cudaMemsetAsync(g->sort_tiles, 0, 8 * sizeof(uint32_t), s));
-    GPMA_CUDA(cudaMemsetAsync(g->sort_status, 0, status_words * sizeof(uint32_t), s));
-    prof_mark(g, 1, s);
+    const uint32_t hist_rows = k == 1 ? 1 : k + 1;
+    if (hist_rows > buf.hist_cap) {
+        dev_free(buf.sort_hist);
+        GPMA_TRY(dev_alloc(&buf.sort_hist, (size_t)hist_rows * 2048));
+        buf.hist_cap = hist_rows;
+    }
+    if (chunk_need > buf.chunk_cap) {
+        dev_free(buf.chunk_cnt);
+        GPMA_TRY(dev_alloc(&buf.chunk_cnt, chunk_need));
+        buf.chunk_cap = chunk_need;
+    }
+    GPMA_CUDA(cudaMemcpyAsync(buf.gd, buf.h_gd.data(), sizeof(GraphDesc) * k, cudaMemcpyHostToDevice, s));
+    GPMA_CUDA(cudaMemcpyAsync(buf.boff, buf.h_off.data(), sizeof(uint32_t) * (k + 1), cudaMemcpyHostToDevice, s));
+    GPMA_CUDA(cudaMemcpyAsync(buf.toff, buf.h_off.data() + k + 1, sizeof(uint32_t) * (k + 1), cudaMemcpyHostToDevice,
+                              s));
+    GPMA_CUDA(cudaMemsetAsync(buf.status, 0, sizeof(DeviceStatus), s));
+    GPMA_CUDA(cudaMemsetAsync(buf.gs, 0, sizeof(GraphStatus) * k, s));
+    GPMA_CUDA(cudaMemsetAsync(buf.sort_hist, 0, sizeof(uint32_t) * hist_rows * 2048, s));
+    GPMA_CUDA(cudaMemsetAsync(buf.sort_tiles, 0, 8 * sizeof(uint32_t), s));
+    GPMA_CUDA(cudaMemsetAsync(buf.sort_status, 0, status_words * sizeof(uint32_t), s));
+    prof_mark(profiling, ev, 1, s);
     UpdateArgs A;
-    A.keys = g->keys;
-    A.vals = g->values;
-    A.row_offset = g->row_offset;
-    A.row_num = g->row_num;
-    A.size = g->geo.size;
-    A.seg = g->geo.seg;
-    A.log2seg = fls32(g->geo.seg) - 1;
-    A.height = g->geo.height;
-    A.lower = g->d_lower;
-    A.upper = g->d_upper;
-    A.bk[0] = g->bkeys[0];
-    A.bk[1] = g->bkeys[1];
-    A.bv[0] = g->bvals[0];
-    A.bv[1] = g->bvals[1];
-    A.sort_hist = g->sort_hist;
-    A.sort_tiles = g->sort_tiles;
-    A.sort_status = g->sort_status;
-    A.check_keys = check_keys;
+    A.gd = buf.gd;
+    A.gs = buf.gs;
+    A.G = k;
+    A.max_height = max_height;
+    A.boff = buf.boff;
+    A.toff = buf.toff;
     A.n = (uint32_t)n;
-    A.leaf = g->leaf;
     for (int i = 0; i < 2; ++i) {
-        A.ikeys[i] = g->ikeys[i];
-        A.ivals[i] = g->ivals[i];
+        A.bk[i] = buf.bkeys[i];
+        A.bv[i] = buf.bvals[i];
+        A.ikeys[i] = buf.ikeys[i];
+        A.ivals[i] = buf.ivals[i];
+        A.wnode[i] = buf.wnode[i];
+        A.wgraph[i] = buf.wgraph[i];
+        A.wa[i] = buf.wa[i];
+        A.wb[i] = buf.wb[i];
     }
-    A.ileaf = g->ileaf;
-    for (int i = 0; i < 2; ++i) {
-        A.wnode[i] = g->wnode[i];
-        A.wa[i] = g->wa[i];
-        A.wb[i] = g->wb[i];
-    }
-    A.wflag = g->wflag;
-    A.wlive = g->wlive;
-    A.skeys = g->skeys;
-    A.svals = g->svals;
-    A.chunk_cnt = g->chunk_cnt;
-    A.cta_cnt = g->cta_cnt;
-    A.st = g->status;
+    A.sort_hist = buf.sort_hist;
+    A.sort_tiles = buf.sort_tiles;
+    A.sort_status = buf.sort_status;
+    A.check_keys = check_keys;
+    A.leaf = buf.leaf;
+    A.ileaf = buf.ileaf;
+    A.igraph = buf.igraph;
+    A.wflag = buf.wflag;
+    A.wlive = buf.wlive;
+    A.rkeys = buf.rkeys;
+    A.rvals = buf.rvals;
+    A.chunk_cnt = buf.chunk_cnt;
+    A.cta_cnt = buf.cta_cnt;
+    A.st = buf.status;
     void *params[] = {&A};
-    GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)update_kernel, dim3(g->update_grid), dim3(BLOCK), params,
-                                          UPDATE_SMEM, s));
-    prof_mark(g, 2, s);
-    GPMA_CUDA(cudaMemcpyAsync(g->h_status, g->status, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
+    GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)update_kernel, dim3(grid), dim3(BLOCK), params, UPDATE_SMEM,
+                                          s));
+    prof_mark(profiling, ev, 2, s);
+    GPMA_CUDA(cudaMemcpyAsync(buf.h_status, buf.status, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
+    GPMA_CUDA(cudaMemcpyAsync(buf.h_gs, buf.gs, sizeof(GraphStatus) * k, cudaMemcpyDeviceToHost, s));
     GPMA_CUDA(cudaStreamSynchronize(s));
-    g->prof.kernel_launches += 1;  // the sort runs inside the update kernel
-    g->prof.update_kernels++;
-    g->prof.update_kernel_ms += prof_elapsed(g, 1, 2);
-    const DeviceStatus &h = *g->h_status;
+    const DeviceStatus &h = *buf.h_status;
+    if (prof) {
+        prof->kernel_launches += 1;  // the sort runs inside the update kernel
+        prof->update_kernels++;
+        prof->update_kernel_ms += prof_elapsed(profiling, ev, 1, 2);
+        // phase split from the kernel's own timeline (stamps of an early exit stay 0)
+        const unsigned long long *t = h.stamp;
+        auto span = [&](int a, int b) { return (t[a] && t[b] && t[b] >= t[a]) ? (t[b] - t[a]) * 1e-6 : 0.0; };
+        prof->sort_ms += span(0, 1);
+        prof->locate_ms += span(1, 2);
+        prof->group_ms += span(2, 3);
+        prof->levels_ms += span(3, 4);
+    }
     if (h.invalid_keys) {
         set_error("update batch holds keys whose column is 0xFFFFFFFF (reserved for row guards and empty slots)");
         return GPMA_ERR_INVALID;
@@ -1201,15 +1435,33 @@ gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_
         set_error("device-side wait gave up in the update kernel (code %u)", h.err);
         return h.err == DERR_BOUNDS ? GPMA_ERR_DEVICE : GPMA_ERR_TIMEOUT;
     }
-    g->stats.levels_visited += h.levels;
-    g->stats.accepted_windows += h.accepted_windows;
-    g->stats.accepted_slots += h.accepted_slots;
-    g->stats.last_inserts = h.inserts;
+    for (uint32_t i = 0; i < k; ++i) {
+        gpma_graph *g = graphs[i];
+        const GraphStatus &gs = buf.h_gs[i];
+        const uint32_t inserts = gs.inserts ? gs.inserts - gs.ins_base : 0;  // end - first
+        g->stats.last_inserts = h.significant ? h.inserts : inserts;
+        g->stats.levels_visited += h.levels;
+        if (k == 1) {
+            g->stats.accepted_windows += h.accepted_windows;
+            g->stats.accepted_slots += h.accepted_slots;
+        }
+    }
     if (h.significant)
-        return root_rebuild(g, true, 0, 0, h.inserts, s);
-    if (h.remaining > 0)
-        return root_rebuild(g, false, h.rem_buf, h.rem_a, h.remaining, s);
+        return root_rebuild(graphs[0], true, buf.ikeys[0], buf.ivals[0], h.inserts, s);
+    for (uint32_t i = 0; i < k; ++i) {
+        const GraphStatus &gs = buf.h_gs[i];
+        if (gs.remaining > 0)
+            GPMA_TRY(root_rebuild(graphs[i], false, buf.rkeys + gs.ins_base, buf.rvals + gs.ins_base, gs.remaining,
+                                  s));
+    }
     return GPMA_OK;
+}
+
+// Single-graph update of the n-key batch staged in g->buf.bkeys[0]/bvals[0].
+gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys) {
+    const uint64_t off[2] = {0, n};
+    gpma_graph *gs[1] = {g};
+    return update_graphs(gs, off, 1, g->buf, g->sms, s, check_keys, g->profiling, g->ev, &g->prof);
 }
 
 }  // namespace gpma

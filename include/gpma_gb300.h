@@ -117,6 +117,32 @@ GPMA_API gpma_status gpma_bfs_multi(gpma_graph *g, const uint32_t *srcs, uint32_
 GPMA_API gpma_status gpma_bfs_noalloc(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached,
                                       void *stream);
 
+/* ---- many graphs per launch -------------------------------------------------
+ * No reference counterpart: the reference updates one GPMA per call. A
+ * gpma_batch owns the update buffers shared by the graphs of one call. All
+ * graphs of a call must live on the current device and be distinct. */
+typedef struct gpma_batch gpma_batch;
+GPMA_API gpma_status gpma_batch_create(gpma_batch **out);
+GPMA_API gpma_status gpma_batch_destroy(gpma_batch *b);
+
+/* Applies k independent update batches, batch i (keys[i], values[i],
+ * counts[i] entries, host or device) to graphs[i], in one persistent kernel
+ * launch; each graph ends exactly as gpma_update(graphs[i], ...) would leave
+ * it. Batches of 5,000,000 keys or more take the single-graph path. */
+GPMA_API gpma_status gpma_batch_update(gpma_batch *b, gpma_graph *const *graphs, const uint64_t *const *keys,
+                                       const uint8_t *const *values, const uint64_t *counts, uint32_t k,
+                                       void *stream);
+
+/* Multi-source BFS on k graphs in one persistent launch: graph i searches
+ * from nsrc[i] (1..64) sources srcs[i][0..nsrc[i]), one bit lane per source.
+ * levels (optional; NULL or per-graph pointers, host or device, each
+ * [nsrc[i]][row_num]) receives the levels; reached (optional, host) receives
+ * sum(nsrc) counts, graph by graph. Each search equals gpma_bfs from that
+ * source. */
+GPMA_API gpma_status gpma_batch_bfs_multi(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs,
+                                          const uint32_t *nsrc, uint32_t k, uint32_t *const *levels,
+                                          uint64_t *reached, void *stream);
+
 /* ---- views ---------------------------------------------------------------
  * GPMA's public members (gpma.cuh:31-52) as read-only views. */
 GPMA_API gpma_status gpma_get_geometry(const gpma_graph *g, gpma_geometry *out);
@@ -150,17 +176,25 @@ GPMA_API gpma_status gpma_get_stats(const gpma_graph *g, gpma_stats *out);
  * No reference counterpart (the reference printed wall-clock deltas,
  * rdebug.hpp:8-17). */
 typedef struct gpma_profile {
-    double sort_ms;          /* batch radix sort (histogram, plan, digit passes) */
-    double update_kernel_ms; /* persistent update kernel: locate .. level loop */
+    double sort_ms;          /* inside the update kernel: batch radix sort */
+    double locate_ms;        /* inside the update kernel: leaf locate + delete/modify */
+    double group_ms;         /* inside the update kernel: insertion compaction + grouping */
+    double levels_ms;        /* inside the update kernel: the level loop */
+    double update_kernel_ms; /* whole persistent update kernel (events on the stream) */
     double rebuild_ms;       /* root resize / bulk rebuild kernels */
     double bfs_ms;           /* BFS kernels (single- and multi-source) */
     uint64_t update_kernels; /* launches of the persistent update kernel */
     uint64_t bfs_kernels;    /* launches of BFS traversal kernels */
     uint64_t kernel_launches;
+    uint64_t bfs_edges;      /* edges scanned from reached nodes by multi-source BFS, summed over sources */
 } gpma_profile;
 GPMA_API gpma_status gpma_set_profiling(gpma_graph *g, int enabled);
 GPMA_API gpma_status gpma_get_profile(const gpma_graph *g, gpma_profile *out);
 GPMA_API gpma_status gpma_reset_profile(gpma_graph *g);
+/* The same for the launches of a gpma_batch. */
+GPMA_API gpma_status gpma_batch_set_profiling(gpma_batch *b, int enabled);
+GPMA_API gpma_status gpma_batch_get_profile(const gpma_batch *b, gpma_profile *out);
+GPMA_API gpma_status gpma_batch_reset_profile(gpma_batch *b);
 
 /* ---- diagnostics ---------------------------------------------------------- */
 GPMA_API const char *gpma_status_string(gpma_status s);
