@@ -274,6 +274,11 @@ def run_gpu(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(n, keys, half, slide, args.cpu_sample_steps)
+    g.close()
+    del dk, dv, hk, hv
+    batched = None
+    if args.batched_graphs > 0:
+        batched = run_batched(args, stream)
 
     if rank == 0:
         line = {
@@ -303,10 +308,116 @@ def run_gpu(args):
         }
         if cpu:
             line["cpu_baseline"] = cpu
+        if batched:
+            line["batched"] = batched
         print(json.dumps(line), flush=True)
-    g.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_batched(args, stream):
+    """Batched configuration: many independent R-MAT graphs (edge counts
+    log-uniform in [10k, 2M], ~edges/16 nodes), each updated every step by a
+    sliding-window batch of log-uniform [100, 200k] keys (half inserts, half
+    deletes), all graphs in ONE launch per step; then 64-source BFS on every
+    graph in one launch. The plain drop-in (one gpma_update / gpma_bfs_multi
+    per graph, same device-resident batches) is timed on the same stream."""
+    import torch
+
+    import gpma_bfs_gb300 as G
+    from gpma_bfs_gb300.workloads import SlidingStream, batched_graphs
+
+    t0 = time.time()
+    specs = batched_graphs(args.batched_graphs, seed=4)
+    gen_s = time.time() - t0
+    rng = np.random.default_rng(44)
+    graphs_b = [G.GPMA(nn) for nn, _ in specs]  # batched form
+    graphs_p = [G.GPMA(nn) for nn, _ in specs]  # plain drop-in, same stream of updates
+    streams = [SlidingStream(kk) for _, kk in specs]
+    streams_p = [SlidingStream(kk) for _, kk in specs]
+    b = G.Batch()
+    k = len(specs)
+    loads = [s.load() for s in streams]
+    off = np.concatenate([[0], np.cumsum([len(x[0]) for x in loads])]).astype(np.uint64)
+    b.update_packed(graphs_b, np.concatenate([x[0] for x in loads]), np.concatenate([x[1] for x in loads]), off,
+                    stream)
+    for gp, sp in zip(graphs_p, streams_p):
+        G.update_gpma(gp, *sp.load(), stream=stream)
+    total_steps = args.warmup + args.batched_steps
+    staged = []
+    for _ in range(total_steps):
+        sizes = np.exp(rng.uniform(np.log(100), np.log(200_000), k)).astype(np.int64)
+        parts = [s.step(int(z)) for s, z in zip(streams, sizes)]
+        for sp, z in zip(streams_p, sizes):
+            sp.step(int(z))  # keep the plain copy's window in step (same batches)
+        o = np.concatenate([[0], np.cumsum([len(p[0]) for p in parts])]).astype(np.uint64)
+        staged.append((torch.from_numpy(np.concatenate([p[0] for p in parts]).view(np.int64)).cuda(),
+                       torch.from_numpy(np.concatenate([p[1] for p in parts])).cuda(), o))
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    def timed(fn):
+        flush.fill_(1)
+        a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        c.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(c)
+
+    bt, pt, nupd = [], [], 0
+    for j, (dk, dv, o) in enumerate(staged):
+        tb = timed(lambda: b.update_packed(graphs_b, dk, dv, o, stream))
+
+        def plain():
+            for i, gp in enumerate(graphs_p):
+                lo, hi = int(o[i]), int(o[i + 1])
+                G.update_gpma(gp, dk[lo:hi], dv[lo:hi], stream)
+
+        tp = timed(plain)
+        if j >= args.warmup:
+            bt.append(tb)
+            pt.append(tp)
+            nupd += int(o[-1])
+    # the two copies must agree (same batches, same algorithm)
+    same = all(np.array_equal(x.export_layout()[0], y.export_layout()[0]) for x, y in zip(graphs_b, graphs_p))
+    # 64-source BFS on every graph
+    sources = []
+    for (nn, kk) in specs:
+        cand = np.unique((kk >> np.uint64(32)).astype(np.uint32))
+        sources.append(rng.choice(cand, min(64, len(cand)), replace=False).astype(np.uint32))
+    b.set_profiling(True)
+    b.bfs_multi(graphs_b, sources)  # warm-up
+    b.reset_profile()
+    tbb = timed(lambda: b.bfs_multi(graphs_b, sources, stream=stream))
+    edges_b = b.profile()["bfs_edges"]
+
+    # the plain call writes 64 level arrays per graph: keep them on the device
+    lv = torch.empty(64 * max(nn for nn, _ in specs), dtype=torch.int32, device="cuda")
+
+    def plain_bfs():
+        for gp, srcs in zip(graphs_p, sources):
+            G.gpma_bfs_multi(gp, srcs, lv[: len(srcs) * gp.row_num].view(len(srcs), gp.row_num), stream=stream)
+
+    plain_bfs()
+    tpb = timed(plain_bfs)
+    b.close()
+    total_edges = int(sum(len(kk) for _, kk in specs))
+    for x in graphs_b + graphs_p:
+        x.close()
+    sb, sp_ = sum(bt) / 1e3, sum(pt) / 1e3
+    return {
+        "workload": f"{k} R-MAT graphs, edges log-uniform [10k, 2M] (~edges/16 nodes), sliding-window batches "
+                    f"log-uniform [100, 200k] keys per graph per step (1:1 insert:delete), 64-source BFS per graph",
+        "graphs": k, "edges_total": total_edges, "half_loaded": int(off[-1]), "steps": len(bt),
+        "updates_per_step": nupd / max(1, len(bt)),
+        "update": {"batched_updates_per_s": nupd / sb, "batched_ms_per_step": 1e3 * sb / len(bt),
+                   "plain_updates_per_s": nupd / sp_, "plain_ms_per_step": 1e3 * sp_ / len(pt),
+                   "speedup": sp_ / sb, "identical_layouts": same},
+        "bfs": {"sources_per_graph": 64, "edges_traversed": edges_b,
+                "batched_ms": tbb, "batched_gteps": edges_b / (tbb * 1e-3) / 1e9,
+                "plain_ms": tpb, "plain_gteps": edges_b / (tpb * 1e-3) / 1e9, "speedup": tpb / tbb},
+        "setup_s": {"generate": gen_s},
+    }
 
 
 def cpu_baseline(n, keys, half, slide, steps):
@@ -376,6 +487,8 @@ def main():
     ap.add_argument("--bfs-repeats", type=int, default=3)
     ap.add_argument("--cpu-sample-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batched-graphs", type=int, default=256, help="graphs of the batched configuration (0: skip)")
+    ap.add_argument("--batched-steps", type=int, default=5)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

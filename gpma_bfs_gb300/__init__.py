@@ -95,6 +95,7 @@ def lib() -> ctypes.CDLL:
         "gpma_batch_destroy": (st, [P]),
         "gpma_batch_update": (st, [P, P, P, P, P, u32, P]),
         "gpma_batch_bfs_multi": (st, [P, P, P, P, u32, P, P, P]),
+        "gpma_batch_update_packed": (st, [P, P, P, P, P, u32, P]),
         "gpma_batch_set_profiling": (st, [P, ctypes.c_int]),
         "gpma_batch_get_profile": (st, [P, ctypes.POINTER(_Profile)]),
         "gpma_batch_reset_profile": (st, [P]),
@@ -423,6 +424,24 @@ class Batch:
             keep += [ka, kb]
             kp[i], vp[i], cnt[i], hs[i] = a, b, len(kk), g.handle.value
         _check(lib().gpma_batch_update(self._h, hs, kp, vp, cnt, k, _stream_ptr(stream)), "gpma_batch_update")
+
+    def update_packed(self, graphs, keys, values, offsets, stream=None) -> None:
+        """All batches in one buffer: graph i gets keys[offsets[i]:offsets[i+1]]."""
+        k = len(graphs)
+        off = np.ascontiguousarray(np.asarray(offsets, np.uint64))
+        if len(off) != k + 1 or len(keys) != len(values) or (k and int(off[-1]) > len(keys)):
+            raise ValueError("offsets must have len(graphs) + 1 entries within the key array")
+        if isinstance(keys, np.ndarray):
+            keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        if isinstance(values, np.ndarray):
+            values = np.ascontiguousarray(values).view(np.uint8) if values.dtype.itemsize == 1 \
+                else np.ascontiguousarray(values, dtype=np.uint8)
+        kp, kk = _ptr(keys)
+        vp, vk = _ptr(values)
+        hs = (ctypes.c_void_p * k)(*[g.handle.value for g in graphs])
+        _check(lib().gpma_batch_update_packed(self._h, hs, kp, vp, off.ctypes.data, k, _stream_ptr(stream)),
+               "gpma_batch_update_packed")
+        del kk, vk
 
     def bfs_multi(self, graphs, sources, levels: bool = False, stream=None):
         """(levels per graph or None, reached per graph) for up to 64 sources per graph."""

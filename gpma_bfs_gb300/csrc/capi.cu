@@ -152,6 +152,26 @@ __global__ void gather_live_kernel(const uint64_t *keys, const uint8_t *vals, ui
     }
 }
 
+// Destination segment j (dst_off[j] .. dst_off[j+1]) copied from the source
+// starting at src_start[j]: stages batches in segment-length order.
+__global__ void gather_segments_kernel(uint64_t *dk, uint8_t *dv, const uint64_t *sk, const uint8_t *sv,
+                                       const uint64_t *dst_off, const uint64_t *src_start, uint32_t m) {
+    const uint64_t n = dst_off[m];
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = m;
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (dst_off[mid] <= t)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        const uint64_t src = src_start[lo] + (t - dst_off[lo]);
+        dk[t] = sk[src];
+        dv[t] = sv[src];
+    }
+}
+
 int small_grid(uint64_t work, int sms) {
     uint64_t g = (work + BLOCK - 1) / BLOCK;
     return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, (uint64_t)sms * 8));
@@ -358,6 +378,7 @@ gpma_status gpma_batch_destroy(gpma_batch *b) {
     cudaDeviceSynchronize();
     free_buffers(b->buf);
     free_batch_bfs(b);
+    dev_free(b->gather_tab);
     for (auto &e : b->ev)
         if (e)
             cudaEventDestroy(e);
@@ -426,6 +447,89 @@ gpma_status gpma_batch_update(gpma_batch *b, gpma_graph *const *graphs, const ui
     }
     return update_graphs(gs.data(), off.data(), (uint32_t)gs.size(), b->buf, b->sms, s, true, b->profiling, b->ev,
                          &b->prof);
+}
+
+gpma_status gpma_batch_update_packed(gpma_batch *b, gpma_graph *const *graphs, const uint64_t *keys,
+                                     const uint8_t *values, const uint64_t *offsets, uint32_t k, void *stream) {
+    if (!b || (k && (!graphs || !offsets || !keys || !values))) {
+        set_error("gpma_batch_update_packed: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint64_t all = k ? offsets[k] - offsets[0] : 0;
+    for (uint32_t i = 0; i < k; ++i) {
+        if (!graphs[i] || offsets[i + 1] < offsets[i]) {
+            set_error("gpma_batch_update_packed: null graph or decreasing offsets at %u", i);
+            return GPMA_ERR_INVALID;
+        }
+        for (uint32_t j = 0; j < i; ++j)
+            if (graphs[j] == graphs[i]) {
+                set_error("gpma_batch_update_packed: graph %u appears twice", i);
+                return GPMA_ERR_INVALID;
+            }
+    }
+    if (all >= (1ull << 31)) {
+        set_error("gpma_batch_update_packed: %llu keys in one call exceed 2^31", (unsigned long long)all);
+        return GPMA_ERR_CAPACITY;
+    }
+    const bool on_device = is_device_pointer(keys) && is_device_pointer(values);
+    std::vector<uint32_t> order;
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < k; ++i) {
+        const uint64_t c = offsets[i + 1] - offsets[i];
+        graphs[i]->stats.updates++;
+        graphs[i]->stats.submitted += c;
+        if (c == 0)
+            continue;
+        if (c >= SIGNIFICANT_INSERTS) {
+            // a possible bulk rebuild: the single-graph path, on the graph's own buffers
+            GPMA_TRY(ensure_buffers(graphs[i]->buf, c, 1));
+            GPMA_TRY(copy_any(graphs[i]->buf.bkeys[0], keys + offsets[i], c * sizeof(uint64_t), s));
+            GPMA_TRY(copy_any(graphs[i]->buf.bvals[0], values + offsets[i], c, s));
+            GPMA_TRY(update_device(graphs[i], c, s));
+            continue;
+        }
+        order.push_back(i);
+        total += c;
+    }
+    if (order.empty())
+        return GPMA_OK;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint32_t x, uint32_t y) { return graphs[x]->geo.seg < graphs[y]->geo.seg; });
+    GPMA_TRY(ensure_buffers(b->buf, std::max<uint64_t>(total, all), (uint32_t)order.size()));
+    const uint64_t *src_k = keys;
+    const uint8_t *src_v = values;
+    uint64_t src_base = 0;
+    if (!on_device) {
+        // one upload of the packed range into the second sort buffer
+        GPMA_TRY(copy_any(b->buf.bkeys[1], keys + offsets[0], all * sizeof(uint64_t), s));
+        GPMA_TRY(copy_any(b->buf.bvals[1], values + offsets[0], all, s));
+        src_k = b->buf.bkeys[1];
+        src_v = b->buf.bvals[1];
+        src_base = offsets[0];
+    }
+    const uint32_t m = (uint32_t)order.size();
+    if (m > b->gather_cap || !b->gather_tab) {
+        dev_free(b->gather_tab);
+        b->gather_cap = 0;
+        GPMA_TRY(dev_alloc(&b->gather_tab, 2ull * m + 1));
+        b->gather_cap = m;
+    }
+    std::vector<gpma_graph *> gs(m);
+    std::vector<uint64_t> off(m + 1, 0), tab(2ull * m + 1, 0);
+    for (uint32_t j = 0; j < m; ++j) {
+        const uint32_t i = order[j];
+        gs[j] = graphs[i];
+        off[j + 1] = off[j] + (offsets[i + 1] - offsets[i]);
+        tab[m + 1 + j] = offsets[i] - src_base;  // source start of destination segment j
+    }
+    std::copy(off.begin(), off.end(), tab.begin());
+    GPMA_CUDA(cudaMemcpyAsync(b->gather_tab, tab.data(), sizeof(uint64_t) * tab.size(), cudaMemcpyHostToDevice, s));
+    gather_segments_kernel<<<small_grid(total, b->sms), BLOCK, 0, s>>>(b->buf.bkeys[0], b->buf.bvals[0], src_k, src_v,
+                                                                      b->gather_tab, b->gather_tab + m + 1, m);
+    GPMA_CUDA(cudaGetLastError());
+    b->prof.kernel_launches += 1;
+    return update_graphs(gs.data(), off.data(), m, b->buf, b->sms, s, true, b->profiling, b->ev, &b->prof);
 }
 
 gpma_status gpma_batch_bfs_multi(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs,

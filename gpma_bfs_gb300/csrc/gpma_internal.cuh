@@ -201,6 +201,8 @@ struct gpma_batch {
     uint2 *ms_chunks = nullptr;
     uint32_t ms_gcap = 0;
     uint64_t last_traversed = 0;       // edges scanned by the last multi-source BFS, all lanes
+    uint64_t *gather_tab = nullptr;    // packed-update staging table (2 * graphs + 1)
+    uint32_t gather_cap = 0;
 };
 
 namespace gpma {

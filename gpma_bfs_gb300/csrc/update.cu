@@ -836,6 +836,9 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
                     return;
             }
             acc_slots += (acc - before) * (unsigned long long)W;
+            // the next run lays out shared memory differently: every warp of
+            // the CTA must be done with this run's staging first
+            __syncthreads();
         }
         if (!grid_barrier(&st->bar, &st->err))
             return;

@@ -39,6 +39,43 @@ def make_graph(name: str | dict):
     raise ValueError(p["kind"])
 
 
+def batched_graphs(count: int = 256, seed: int = 4, min_edges: int = 10_000, max_edges: int = 2_000_000):
+    """Independent R-MAT graphs with edge counts log-uniform in [min, max] and
+    about edges/16 nodes (the batched configuration). Returns a list of
+    (node count, shuffled keys)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i, e in enumerate(np.exp(rng.uniform(np.log(min_edges), np.log(max_edges), count))):
+        scale = int(np.clip(np.round(np.log2(e / 16)), 4, 24))
+        ef = max(1, int(round(e / (1 << scale))))
+        src, dst = gen_rmat(scale, ef, seed=seed * 100_000 + i)
+        out.append((1 << scale, edges_to_keys(src, dst)))
+    return out
+
+
+class SlidingStream:
+    """Per-graph sliding window over a cyclic edge list: the first half is the
+    initial load; each step inserts the next b/2 edges and deletes the oldest
+    b/2 (gpma_bfs_demo.cu:85-104 with a per-step batch size)."""
+
+    def __init__(self, keys: np.ndarray):
+        self.keys = keys
+        self.m = len(keys)
+        self.ins = self.m // 2
+        self.dels = 0
+
+    def load(self):
+        return self.keys[: self.m // 2], np.ones(self.m // 2, np.uint8)
+
+    def step(self, batch: int):
+        h = max(1, min(batch // 2, self.m // 2))
+        ins = self.keys[(self.ins + np.arange(h)) % self.m]
+        dels = self.keys[(self.dels + np.arange(h)) % self.m]
+        self.ins += h
+        self.dels += h
+        return np.concatenate([ins, dels]), np.concatenate([np.ones(h, np.uint8), np.zeros(h, np.uint8)])
+
+
 @dataclass
 class SlidingWindow:
     half: int

@@ -133,6 +133,14 @@ GPMA_API gpma_status gpma_batch_update(gpma_batch *b, gpma_graph *const *graphs,
                                        const uint8_t *const *values, const uint64_t *counts, uint32_t k,
                                        void *stream);
 
+/* The same with all batches in one buffer: graph i's batch is
+ * keys[offsets[i] .. offsets[i+1]) (and values likewise); keys/values host or
+ * device, offsets a host array of k + 1 entries. One copy and one device
+ * gather stage every batch, whatever the graph order. */
+GPMA_API gpma_status gpma_batch_update_packed(gpma_batch *b, gpma_graph *const *graphs, const uint64_t *keys,
+                                              const uint8_t *values, const uint64_t *offsets, uint32_t k,
+                                              void *stream);
+
 /* Multi-source BFS on k graphs in one persistent launch: graph i searches
  * from nsrc[i] (1..64) sources srcs[i][0..nsrc[i]), one bit lane per source.
  * levels (optional; NULL or per-graph pointers, host or device, each
