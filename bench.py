@@ -279,6 +279,9 @@ def run_gpu(args):
     batched = None
     if args.batched_graphs > 0:
         batched = run_batched(args, stream)
+    served = None
+    if args.served_seconds > 0:
+        served = run_served(args, stream)
 
     if rank == 0:
         line = {
@@ -310,6 +313,8 @@ def run_gpu(args):
             line["cpu_baseline"] = cpu
         if batched:
             line["batched"] = batched
+        if served:
+            line["served"] = served
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -420,6 +425,114 @@ def run_batched(args, stream):
     }
 
 
+def run_served(args, stream):
+    """Served configuration: 32 R-MAT graphs drawn as in the batched one plus
+    two R-MAT graphs of scale 22 (edge factor 16), first halves resident;
+    Poisson arrivals over `served_seconds` simulated seconds, 70% update
+    batches (log-uniform 1k-1M keys, sliding window, 1:1 insert:delete) and 30%
+    BFS queries (1-64 sources from nodes with out-edges), each on a uniformly
+    drawn graph; HBM admission budget 120 GB. The server runs continuous
+    batching in virtual time (the clock advances by each round's measured wall
+    time). The plain drop-in serves the same trace one request at a time
+    (gpma_update / gpma_bfs_multi per request, FIFO) on its own copy of the
+    graphs. Latency = completion - arrival."""
+    import torch
+
+    import gpma_bfs_gb300 as G
+    import gpma_bfs_gb300.serving as S
+    from gpma_bfs_gb300.workloads import SlidingStream, batched_graphs
+
+    t0 = time.time()
+    specs = batched_graphs(32, seed=5)
+    for i in range(2):
+        src, dst = G.gen_rmat(args.served_big_scale, 16, seed=5_000 + i)
+        specs.append((1 << args.served_big_scale, G.edges_to_keys(src, dst)))
+        del src, dst
+    gen_s = time.time() - t0
+    phases = [(args.served_rate, args.served_seconds)]
+    if args.served_burst_seconds > 0:
+        phases.append((args.served_burst_rate, args.served_burst_seconds))
+    trace = S.make_trace(specs, phases, seed=5)
+
+    # ---- served form ----------------------------------------------------------
+    srv = G.Server(hbm_budget_bytes=120 << 30, max_round_keys=1 << 24, stream=stream)
+    gids = [srv.add_graph(nn, len(kk)) for nn, kk in specs]
+    streams = [SlidingStream(kk) for _, kk in specs]
+    t0 = time.time()
+    for gid, s in zip(gids, streams):
+        G.update_gpma(srv.graph(gid), *s.load(), stream=stream)
+    torch.cuda.synchronize()
+    load_s = time.time() - t0
+    w0 = time.perf_counter()
+    out = S.replay_served(srv, gids, streams, trace)
+    served_wall = time.perf_counter() - w0
+    layouts_s = [srv.graph(gid).export_layout()[0] for gid in gids]
+    committed = srv.committed_bytes()
+    srv.close()
+    del streams
+
+    # ---- plain drop-in, one request at a time ------------------------------------
+    plain, pstreams = S.plain_graphs(specs, stream)
+    lv = torch.empty(64 * max(nn for nn, _ in specs), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    done_p, busy_p, reach_p = S.replay_plain(plain, pstreams, trace, stream, lv, torch.cuda.synchronize)
+    same_reach = all(np.array_equal(a, b) for a, b, k in zip(out["reach"], reach_p, trace.kind) if k == 1)
+    same_layout = all(np.array_equal(x.export_layout()[0], y) for x, y in zip(plain, layouts_s))
+    for g in plain:
+        g.close()
+
+    # per phase: sustained rates over the phase's makespan, latency per type
+    rounds = out["rounds"]
+    rphase = [int(trace.phase[r["requests"][0]]) for r in rounds]
+    res = []
+    for p, (rate, seconds) in enumerate(phases):
+        sel = trace.phase == p
+        upd = sel & (trace.kind == 0)
+        keys = int(out["keys"][upd].sum())
+        rs = [r for r, q in zip(rounds, rphase) if q == p]
+        edges = int(sum(r["edges"] for r in rs))
+        t_start = trace.phase_start[p]
+        span_s = float(out["done"][sel].max() - t_start) if sel.any() else 0.0
+        span_p = float(done_p[sel].max() - t_start) if sel.any() else 0.0
+        busy = float(sum(r["seconds"] for r in rs))
+        busy_pl = float(busy_p[sel].sum())
+
+        def rates(span):
+            return {"requests_per_s": int(sel.sum()) / span if span else None,
+                    "edge_updates_per_s": keys / span if span else None,
+                    "bfs_gteps": edges / span / 1e9 if span else None}
+
+        res.append({
+            "rate_per_s": rate, "seconds": seconds, "requests": int(sel.sum()), "updates": int(upd.sum()),
+            "bfs_queries": int((sel & (trace.kind == 1)).sum()), "update_keys": keys, "edges_traversed": edges,
+            "served": {"rounds": len(rs), "requests_per_round": int(sel.sum()) / max(1, len(rs)),
+                       "max_updates_per_round": max((r["updates"] for r in rs), default=0),
+                       "max_graphs_searched_per_round": max((r["bfs_graphs"] for r in rs), default=0),
+                       "busy_s": busy, "makespan_s": span_s, "utilisation": busy / seconds,
+                       "update_device_ms": float(sum(r["update_ms"] for r in rs)),
+                       "bfs_device_ms": float(sum(r["bfs_ms"] for r in rs)),
+                       **rates(span_s),
+                       "update_latency": S.latency_summary(trace, out["done"], p, 0),
+                       "bfs_latency": S.latency_summary(trace, out["done"], p, 1)},
+            "plain": {"busy_s": busy_pl, "makespan_s": span_p, "utilisation": busy_pl / seconds, **rates(span_p),
+                      "update_latency": S.latency_summary(trace, done_p, p, 0),
+                      "bfs_latency": S.latency_summary(trace, done_p, p, 1)},
+            "speedup_sustained": span_p / span_s if span_s else None,
+        })
+    return {
+        "workload": f"32 R-MAT graphs (edges log-uniform [10k, 2M]) + 2 R-MAT scale {args.served_big_scale} "
+                    f"(edge factor 16); Poisson arrivals, 70% updates (log-uniform 1k-1M keys, 1:1 "
+                    f"insert:delete), 30% BFS (1-64 sources), uniform graph choice; HBM budget 120 GB; phases "
+                    + ", ".join(f"{r:g}/s for {s:g} simulated s" for r, s in phases),
+        "graphs": len(specs), "edges_total": int(sum(len(kk) for _, kk in specs)), "requests": len(trace),
+        "failed": int((~out["ok"]).sum()), "committed_bytes": int(committed),
+        "phases": res,
+        "identical_results": bool(same_reach and same_layout),
+        "driver_wall_s": served_wall,
+        "setup_s": {"generate": gen_s, "load": load_s},
+    }
+
+
 def cpu_baseline(n, keys, half, slide, steps):
     """The oracle restatement on all host cores: load untimed, `steps` slides timed."""
     from oracle.oracle import OracleGPMA, build
@@ -489,6 +602,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batched-graphs", type=int, default=256, help="graphs of the batched configuration (0: skip)")
     ap.add_argument("--batched-steps", type=int, default=5)
+    ap.add_argument("--served-seconds", type=float, default=600.0,
+                    help="simulated seconds of served traffic (0: skip the served configuration)")
+    ap.add_argument("--served-rate", type=float, default=20.0, help="served request arrivals per simulated second")
+    ap.add_argument("--served-big-scale", type=int, default=22, help="R-MAT scale of the two large served graphs")
+    ap.add_argument("--served-burst-rate", type=float, default=5000.0,
+                    help="arrivals per simulated second of the saturating phase that follows")
+    ap.add_argument("--served-burst-seconds", type=float, default=4.0)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -36,7 +36,10 @@ _PKG = Path(__file__).resolve().parent
 library_path = _PKG / "libgpma_gb300.so"
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "out of memory", 4: "capacity exceeded",
-          5: "device wait timed out", 6: "I/O error", 7: "device-side check failed"}
+          5: "device wait timed out", 6: "I/O error", 7: "device-side check failed", 8: "server queue full",
+          9: "HBM admission budget exceeded"}
+ERR_BUSY = 8
+ERR_BUDGET = 9
 
 
 class GPMAError(RuntimeError):
@@ -63,6 +66,27 @@ class _Profile(ctypes.Structure):
                 ("levels_ms", ctypes.c_double), ("update_kernel_ms", ctypes.c_double), ("rebuild_ms", ctypes.c_double),
                 ("bfs_ms", ctypes.c_double), ("update_kernels", ctypes.c_uint64), ("bfs_kernels", ctypes.c_uint64),
                 ("kernel_launches", ctypes.c_uint64), ("bfs_edges", ctypes.c_uint64)]
+
+
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_round_keys", ctypes.c_uint64),
+                ("max_round_bfs_graphs", ctypes.c_uint32), ("max_queued", ctypes.c_uint32),
+                ("max_queued_keys", ctypes.c_uint64), ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class _RequestInfo(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("graph", ctypes.c_uint32), ("kind", ctypes.c_uint32),
+                ("state", ctypes.c_uint32), ("status", ctypes.c_int32), ("arrival", ctypes.c_double),
+                ("start", ctypes.c_double), ("done", ctypes.c_double), ("round", ctypes.c_uint64),
+                ("keys", ctypes.c_uint64), ("nsrc", ctypes.c_uint32), ("lane", ctypes.c_uint32),
+                ("reached", ctypes.c_uint64 * 64)]
+
+
+class _RoundInfo(ctypes.Structure):
+    _fields_ = [("round", ctypes.c_uint64), ("start", ctypes.c_double), ("seconds", ctypes.c_double),
+                ("updates", ctypes.c_uint32), ("bfs_requests", ctypes.c_uint32), ("bfs_graphs", ctypes.c_uint32),
+                ("failed", ctypes.c_uint32), ("keys", ctypes.c_uint64), ("sources", ctypes.c_uint64),
+                ("edges", ctypes.c_uint64), ("update_ms", ctypes.c_double), ("bfs_ms", ctypes.c_double)]
 
 
 _lib = None
@@ -99,6 +123,17 @@ def lib() -> ctypes.CDLL:
         "gpma_batch_set_profiling": (st, [P, ctypes.c_int]),
         "gpma_batch_get_profile": (st, [P, ctypes.POINTER(_Profile)]),
         "gpma_batch_reset_profile": (st, [P]),
+        "gpma_server_create": (st, [ctypes.POINTER(_ServerConfig), P, ctypes.POINTER(P)]),
+        "gpma_server_destroy": (st, [P]),
+        "gpma_server_add_graph": (st, [P, u32, u64, ctypes.POINTER(u32)]),
+        "gpma_server_graph": (st, [P, u32, ctypes.POINTER(P)]),
+        "gpma_server_submit_update": (st, [P, u32, P, P, u64, ctypes.c_double, ctypes.POINTER(u64)]),
+        "gpma_server_submit_bfs": (st, [P, u32, P, u32, ctypes.c_double, P, ctypes.POINTER(u64)]),
+        "gpma_server_run_round": (st, [P, ctypes.c_double, ctypes.POINTER(_RoundInfo)]),
+        "gpma_server_poll": (st, [P, u64, ctypes.c_int, ctypes.POINTER(_RequestInfo)]),
+        "gpma_server_last_round": (st, [P, P, u32, ctypes.POINTER(u32)]),
+        "gpma_server_queued": (st, [P, ctypes.POINTER(u64), ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_double)]),
+        "gpma_server_committed_bytes": (st, [P, ctypes.POINTER(u64)]),
         "gpma_set_profiling": (st, [P, ctypes.c_int]),
         "gpma_get_profile": (st, [P, ctypes.POINTER(_Profile)]),
         "gpma_reset_profile": (st, [P]),
@@ -165,10 +200,21 @@ class GPMA:
         _check(lib().gpma_create(int(row_num), _stream_ptr(stream), ctypes.byref(h)), "gpma_create")
         self._h = h
         self.row_num = int(row_num)
+        self._owned = True
+
+    @classmethod
+    def _view(cls, handle: ctypes.c_void_p, row_num: int) -> "GPMA":
+        """A non-owning wrapper of a graph that something else (a Server) owns."""
+        g = cls.__new__(cls)
+        g._h = handle
+        g.row_num = int(row_num)
+        g._owned = False
+        return g
 
     def close(self) -> None:
         if getattr(self, "_h", None):
-            lib().gpma_destroy(self._h)
+            if getattr(self, "_owned", True):
+                lib().gpma_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -471,3 +517,110 @@ class Batch:
 
     def reset_profile(self) -> None:
         _check(lib().gpma_batch_reset_profile(self._h), "gpma_batch_reset_profile")
+
+
+PLAN_ONLY = 1
+
+
+class Server:
+    """Served form (no reference counterpart): resident graphs, update batches
+    and BFS queries with continuous batching, in virtual time.
+
+    ``submit_update`` / ``submit_bfs`` queue requests with their arrival time
+    (raising GPMAError with status ERR_BUSY when the queue is full);
+    ``run_round(now)`` runs one round over what has arrived and returns its
+    description; ``poll(id)`` gives a request's state, times and BFS reach.
+    """
+
+    def __init__(self, hbm_budget_bytes: int = 120 << 30, max_round_keys: int = 1 << 24,
+                 max_round_bfs_graphs: int = 4096, max_queued: int = 1 << 20, max_queued_keys: int = 1 << 28,
+                 plan_only: bool = False, stream=None):
+        cfg = _ServerConfig(int(hbm_budget_bytes), int(max_round_keys), int(max_round_bfs_graphs), int(max_queued),
+                            int(max_queued_keys), PLAN_ONLY if plan_only else 0, 0)
+        h = ctypes.c_void_p()
+        _check(lib().gpma_server_create(ctypes.byref(cfg), _stream_ptr(stream), ctypes.byref(h)), "gpma_server_create")
+        self._h = h
+        self._rows = []
+        self._keep = {}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().gpma_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_graph(self, row_num: int, reserve_edges: int = 0) -> int:
+        gid = ctypes.c_uint32()
+        _check(lib().gpma_server_add_graph(self._h, int(row_num), int(reserve_edges), ctypes.byref(gid)),
+               "gpma_server_add_graph")
+        self._rows.append(int(row_num))
+        return gid.value
+
+    def graph(self, gid: int):
+        """The graph as a non-owning GPMA (None in plan-only mode)."""
+        h = ctypes.c_void_p()
+        _check(lib().gpma_server_graph(self._h, int(gid), ctypes.byref(h)), "gpma_server_graph")
+        return GPMA._view(h, self._rows[gid]) if h.value else None
+
+    def submit_update(self, gid: int, keys: np.ndarray, values: np.ndarray, arrival: float) -> int:
+        keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        values = np.ascontiguousarray(values).view(np.uint8) if np.asarray(values).dtype.itemsize == 1 \
+            else np.ascontiguousarray(values, dtype=np.uint8)
+        if len(keys) != len(values):
+            raise ValueError("Inconsistant kv size.")
+        rid = ctypes.c_uint64()
+        _check(lib().gpma_server_submit_update(self._h, int(gid), keys.ctypes.data, values.ctypes.data, len(keys),
+                                               float(arrival), ctypes.byref(rid)), "gpma_server_submit_update")
+        return rid.value
+
+    def submit_bfs(self, gid: int, sources, arrival: float, levels: bool = False) -> int:
+        """Queues a search; with levels=True the [k][row_num] level array is
+        kept and returned by ``levels(id)`` once the request is done."""
+        src = np.ascontiguousarray(np.asarray(sources, np.uint32))
+        out = np.zeros((len(src), self._rows[gid]), np.uint32) if levels else None
+        rid = ctypes.c_uint64()
+        _check(lib().gpma_server_submit_bfs(self._h, int(gid), src.ctypes.data, len(src), float(arrival),
+                                            out.ctypes.data if levels else None, ctypes.byref(rid)),
+               "gpma_server_submit_bfs")
+        if levels:
+            self._keep[rid.value] = out
+        return rid.value
+
+    def run_round(self, now: float) -> dict:
+        ri = _RoundInfo()
+        _check(lib().gpma_server_run_round(self._h, float(now), ctypes.byref(ri)), "gpma_server_run_round")
+        return {name: getattr(ri, name) for name, _ in _RoundInfo._fields_}
+
+    def poll(self, rid: int, release: bool = False) -> dict:
+        info = _RequestInfo()
+        _check(lib().gpma_server_poll(self._h, int(rid), int(bool(release)), ctypes.byref(info)), "gpma_server_poll")
+        d = {name: getattr(info, name) for name, _ in _RequestInfo._fields_ if name != "reached"}
+        d["reached"] = np.array(info.reached[: info.nsrc], np.uint64)
+        return d
+
+    def levels(self, rid: int):
+        return self._keep.pop(rid, None)
+
+    def last_round(self) -> list:
+        n = ctypes.c_uint32()
+        _check(lib().gpma_server_last_round(self._h, None, 0, ctypes.byref(n)), "gpma_server_last_round")
+        ids = np.zeros(max(1, n.value), np.uint64)
+        _check(lib().gpma_server_last_round(self._h, ids.ctypes.data, n.value, ctypes.byref(n)),
+               "gpma_server_last_round")
+        return [int(x) for x in ids[: n.value]]
+
+    def queued(self) -> tuple[int, int, float]:
+        r, k, t = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_double()
+        _check(lib().gpma_server_queued(self._h, ctypes.byref(r), ctypes.byref(k), ctypes.byref(t)),
+               "gpma_server_queued")
+        return r.value, k.value, t.value
+
+    def committed_bytes(self) -> int:
+        b = ctypes.c_uint64()
+        _check(lib().gpma_server_committed_bytes(self._h, ctypes.byref(b)), "gpma_server_committed_bytes")
+        return b.value

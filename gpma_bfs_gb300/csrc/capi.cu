@@ -198,6 +198,8 @@ const char *gpma_status_string(gpma_status s) {
     case GPMA_ERR_TIMEOUT: return "device wait timed out";
     case GPMA_ERR_IO: return "I/O error";
     case GPMA_ERR_DEVICE: return "device-side check failed";
+    case GPMA_ERR_BUSY: return "server queue full";
+    case GPMA_ERR_BUDGET: return "HBM admission budget exceeded";
     }
     return "unknown status";
 }

@@ -63,17 +63,21 @@ class SlidingStream:
         self.m = len(keys)
         self.ins = self.m // 2
         self.dels = 0
+        self._cyc = None  # keys twice over: any cyclic window of <= m keys is one slice
 
     def load(self):
         return self.keys[: self.m // 2], np.ones(self.m // 2, np.uint8)
 
     def step(self, batch: int):
         h = max(1, min(batch // 2, self.m // 2))
-        ins = self.keys[(self.ins + np.arange(h)) % self.m]
-        dels = self.keys[(self.dels + np.arange(h)) % self.m]
+        if self._cyc is None:
+            self._cyc = np.concatenate([self.keys, self.keys])
+        i, d = self.ins % self.m, self.dels % self.m
         self.ins += h
         self.dels += h
-        return np.concatenate([ins, dels]), np.concatenate([np.ones(h, np.uint8), np.zeros(h, np.uint8)])
+        vals = np.zeros(2 * h, np.uint8)
+        vals[:h] = 1
+        return np.concatenate([self._cyc[i:i + h], self._cyc[d:d + h]]), vals
 
 
 @dataclass

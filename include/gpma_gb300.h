@@ -39,7 +39,9 @@ typedef enum gpma_status {
     GPMA_ERR_CAPACITY = 4, /* the structure would exceed 2^31 slots (32-bit slot ids) */
     GPMA_ERR_TIMEOUT = 5,  /* a bounded device-side wait gave up; the context stays usable */
     GPMA_ERR_IO = 6,       /* file could not be read or written */
-    GPMA_ERR_DEVICE = 7    /* a device-side consistency check failed */
+    GPMA_ERR_DEVICE = 7,   /* a device-side consistency check failed */
+    GPMA_ERR_BUSY = 8,     /* server queue full: retry after a round has run */
+    GPMA_ERR_BUDGET = 9    /* the server's HBM admission budget would be exceeded */
 } gpma_status;
 
 typedef struct gpma_graph gpma_graph;
@@ -150,6 +152,112 @@ GPMA_API gpma_status gpma_batch_update_packed(gpma_batch *b, gpma_graph *const *
 GPMA_API gpma_status gpma_batch_bfs_multi(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs,
                                           const uint32_t *nsrc, uint32_t k, uint32_t *const *levels,
                                           uint64_t *reached, void *stream);
+
+/* ---- served form ----------------------------------------------------------
+ * No reference counterpart. A gpma_server keeps many graphs resident on the
+ * current device and serves update batches and BFS queries against them with
+ * continuous batching: requests wait in one FIFO queue per graph; each round
+ * takes, for every graph whose queue head has arrived, at most one update
+ * batch and then the BFS queries queued directly behind it (packed as source
+ * lanes, up to 64 per graph), and runs all of the round's updates in one
+ * batched update launch followed by one multi-source BFS launch. Requests that
+ * arrive while a round runs join a later round. A graph's requests therefore
+ * take effect in arrival order and every result equals what the same requests
+ * give applied to that graph alone. Time is virtual: the caller passes the
+ * current time to each round, and a round's requests complete at that time
+ * plus the round's measured wall-clock duration.
+ *
+ * Admission. A graph is admitted only if its estimated device bytes fit the
+ * HBM budget; an update joins a round only if the graph's worst-case growth
+ * (the array doubling until it holds its current capacity plus the batch's
+ * insertions at the root density bound) still fits, otherwise it waits, and
+ * fails with GPMA_ERR_BUDGET when it could not fit even alone. Submissions
+ * beyond max_queued requests or max_queued_keys waiting update keys return
+ * GPMA_ERR_BUSY. */
+typedef struct gpma_server gpma_server;
+
+#define GPMA_SERVER_PLAN_ONLY 1u /* schedule only: no device work (checks the policy on a host without a GPU) */
+
+typedef struct gpma_server_config {
+    uint64_t hbm_budget_bytes;     /* device bytes the admitted graphs may hold */
+    uint64_t max_round_keys;       /* update keys per round (one larger batch may run alone) */
+    uint32_t max_round_bfs_graphs; /* graphs searched per round */
+    uint32_t max_queued;           /* waiting requests */
+    uint64_t max_queued_keys;      /* waiting update keys (host copies) */
+    uint32_t flags;                /* GPMA_SERVER_PLAN_ONLY */
+    uint32_t reserved;
+} gpma_server_config;
+
+typedef enum gpma_request_state {
+    GPMA_REQ_QUEUED = 0,
+    GPMA_REQ_DONE = 1,
+    GPMA_REQ_FAILED = 2
+} gpma_request_state;
+
+typedef struct gpma_request_info {
+    uint64_t id;
+    uint32_t graph;
+    uint32_t kind;     /* 0 update, 1 BFS */
+    uint32_t state;    /* gpma_request_state */
+    int32_t status;    /* gpma_status of a failed request */
+    double arrival;    /* virtual seconds, as submitted */
+    double start;      /* start of the round that ran it */
+    double done;       /* completion: start + the round's duration */
+    uint64_t round;    /* 1-based round number */
+    uint64_t keys;     /* update: keys in the batch */
+    uint32_t nsrc;     /* BFS: sources */
+    uint32_t lane;     /* BFS: first source lane of the request in its graph's search */
+    uint64_t reached[64]; /* BFS: nodes reached from each source (the source included) */
+} gpma_request_info;
+
+typedef struct gpma_round_info {
+    uint64_t round;
+    double start, seconds;   /* virtual start; wall-clock duration of the round */
+    uint32_t updates;        /* update requests run */
+    uint32_t bfs_requests;   /* BFS requests run */
+    uint32_t bfs_graphs;     /* graphs searched */
+    uint32_t failed;         /* requests failed in this round */
+    uint64_t keys;           /* update keys applied */
+    uint64_t sources;        /* BFS sources searched */
+    uint64_t edges;          /* edges traversed by the round's searches, all lanes */
+    double update_ms, bfs_ms; /* device time of the update and BFS launches (CUDA events) */
+} gpma_round_info;
+
+/* stream: the stream every round runs on (NULL = legacy default stream). */
+GPMA_API gpma_status gpma_server_create(const gpma_server_config *cfg, void *stream, gpma_server **out);
+GPMA_API gpma_status gpma_server_destroy(gpma_server *s);
+/* Admits a graph of row_num nodes sized for reserve_edges live edges
+ * (GPMA_ERR_BUDGET when its estimate does not fit); *graph_id numbers graphs
+ * from 0 in admission order. */
+GPMA_API gpma_status gpma_server_add_graph(gpma_server *s, uint32_t row_num, uint64_t reserve_edges,
+                                           uint32_t *graph_id);
+/* The graph's handle, for loading it directly and for the views (NULL in
+ * plan-only mode). Do not update it while requests for it are queued. */
+GPMA_API gpma_status gpma_server_graph(gpma_server *s, uint32_t graph_id, gpma_graph **out);
+/* Queues an update batch (host arrays, copied). */
+GPMA_API gpma_status gpma_server_submit_update(gpma_server *s, uint32_t graph_id, const uint64_t *keys,
+                                               const uint8_t *values, uint64_t n, double arrival,
+                                               uint64_t *request_id);
+/* Queues a BFS query from k (1..64) sources (host array, copied). levels
+ * (optional, host, [k][row_num]) receives the levels when the request is done
+ * and must stay valid until then. */
+GPMA_API gpma_status gpma_server_submit_bfs(gpma_server *s, uint32_t graph_id, const uint32_t *sources, uint32_t k,
+                                            double arrival, uint32_t *levels, uint64_t *request_id);
+/* Runs one round at virtual time `now` over the requests that arrived by
+ * then; info (optional) describes it. A round with nothing to run returns
+ * GPMA_OK with info->updates == info->bfs_requests == 0. */
+GPMA_API gpma_status gpma_server_run_round(gpma_server *s, double now, gpma_round_info *info);
+/* A request's state and result; release != 0 forgets a finished request. */
+GPMA_API gpma_status gpma_server_poll(gpma_server *s, uint64_t request_id, int release, gpma_request_info *out);
+/* Ids of the requests the last round ran, in execution order (updates, then
+ * searches graph by graph, lanes ascending). */
+GPMA_API gpma_status gpma_server_last_round(const gpma_server *s, uint64_t *ids, uint32_t capacity, uint32_t *count);
+/* Waiting requests and waiting update keys; earliest arrival among queue heads
+ * (+infinity when nothing waits). */
+GPMA_API gpma_status gpma_server_queued(const gpma_server *s, uint64_t *requests, uint64_t *keys,
+                                        double *next_arrival);
+/* Device bytes the admitted graphs are charged against the budget. */
+GPMA_API gpma_status gpma_server_committed_bytes(const gpma_server *s, uint64_t *bytes);
 
 /* ---- views ---------------------------------------------------------------
  * GPMA's public members (gpma.cuh:31-52) as read-only views. */
