@@ -68,6 +68,12 @@ class _Profile(ctypes.Structure):
                 ("kernel_launches", ctypes.c_uint64), ("bfs_edges", ctypes.c_uint64)]
 
 
+class _Tuning(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint32) for n in ("bfs_dense_div", "bfs_blocks_per_sm", "ms_dense_div",
+                                               "ms_blocks_per_sm", "update_blocks_per_sm")] + \
+               [("reserved", ctypes.c_uint32 * 3)]
+
+
 class _ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_round_keys", ctypes.c_uint64),
                 ("max_round_bfs_graphs", ctypes.c_uint32), ("max_queued", ctypes.c_uint32),
@@ -134,6 +140,9 @@ def lib() -> ctypes.CDLL:
         "gpma_server_last_round": (st, [P, P, u32, ctypes.POINTER(u32)]),
         "gpma_server_queued": (st, [P, ctypes.POINTER(u64), ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_double)]),
         "gpma_server_committed_bytes": (st, [P, ctypes.POINTER(u64)]),
+        "gpma_get_tuning": (st, [ctypes.POINTER(_Tuning)]),
+        "gpma_bfs_level_profile": (st, [P, P, P, P, u32, ctypes.POINTER(u32)]),
+        "gpma_set_tuning": (st, [ctypes.POINTER(_Tuning)]),
         "gpma_set_profiling": (st, [P, ctypes.c_int]),
         "gpma_get_profile": (st, [P, ctypes.POINTER(_Profile)]),
         "gpma_reset_profile": (st, [P]),
@@ -315,6 +324,18 @@ class GPMA:
     def reset_profile(self) -> None:
         _check(lib().gpma_reset_profile(self.handle), "gpma_reset_profile")
 
+    def bfs_levels_profile(self) -> list[dict]:
+        """Per level of the last profiled gpma_bfs: ms, frontier size, dense sweep or row walk."""
+        cap = 64
+        ms = np.zeros(cap)
+        fr = np.zeros(cap, np.uint32)
+        de = np.zeros(cap, np.uint8)
+        n = ctypes.c_uint32()
+        _check(lib().gpma_bfs_level_profile(self.handle, ms.ctypes.data, fr.ctypes.data, de.ctypes.data, cap,
+                                            ctypes.byref(n)), "gpma_bfs_level_profile")
+        k = min(n.value, cap)
+        return [{"ms": float(ms[i]), "frontier": int(fr[i]), "dense": bool(de[i])} for i in range(k)]
+
     def device_arrays(self) -> tuple[int, int, int]:
         k, v, r = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
         _check(lib().gpma_device_arrays(self.handle, ctypes.byref(k), ctypes.byref(v), ctypes.byref(r)),
@@ -377,6 +398,27 @@ def gpma_bfs_multi(gpma: GPMA, sources, results=None, stream=None):
            "gpma_bfs_multi")
     del keep
     return results, reached
+
+
+TUNING_FIELDS = ("bfs_dense_div", "bfs_blocks_per_sm", "ms_dense_div", "ms_blocks_per_sm", "update_blocks_per_sm")
+
+
+def get_tuning() -> dict:
+    """Launch shapes and switch points in effect (they never change results)."""
+    t = _Tuning()
+    _check(lib().gpma_get_tuning(ctypes.byref(t)), "gpma_get_tuning")
+    return {n: getattr(t, n) for n in TUNING_FIELDS}
+
+
+def set_tuning(**values) -> dict:
+    """Changes some tuning fields; returns the previous settings."""
+    old = get_tuning()
+    unknown = set(values) - set(TUNING_FIELDS)
+    if unknown:
+        raise ValueError(f"unknown tuning fields {sorted(unknown)}")
+    t = _Tuning(*[int(values.get(n, old[n])) for n in TUNING_FIELDS])
+    _check(lib().gpma_set_tuning(ctypes.byref(t)), "gpma_set_tuning")
+    return old
 
 
 # ---- synthetic graphs and the reference's text format -------------------------

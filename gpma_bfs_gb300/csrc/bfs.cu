@@ -35,6 +35,10 @@ enum : uint32_t {
     CTL_REACHED = 8,
     CTL_BAR = 10,     // GridBarrier (2 words)
     CTL_WORDS = 16,
+    // profiling record after the control words: u64 start stamp of each level
+    // (and of the final check), then u32 per level: frontier size | dense << 31
+    CTL_PROFILE_LEVELS = 64,
+    CTL_PROFILE_WORDS = 3 * CTL_PROFILE_LEVELS,
 };
 
 // Rows longer than BIG_ROW slots are cut into CHUNK_SLOTS-slot chunks that
@@ -58,6 +62,8 @@ struct BfsArgs {
     uint2 *chunks;     // [slot begin, slot end) of big-row chunks
     uint32_t chunk_cap;
     uint32_t *ctl;
+    uint32_t dense_div;  // a level whose frontier holds >= n / dense_div nodes sweeps every slot (0: never)
+    unsigned long long *stamps;  // per-level profile (CTL_PROFILE_LEVELS stamps + info words) or null
 };
 
 // Two edge slots per lane (s < SIZE_NONE means present): all loads are
@@ -95,6 +101,43 @@ __device__ __forceinline__ uint32_t visit_pair(const BfsArgs &A, uint32_t sa, ui
     return fresh;
 }
 
+// Dense levels: 8 consecutive slots of the linear sweep. The key's high word
+// is its source row, so the frontier test needs no row_offset lookup; guards,
+// empty slots, tombstones and bulk-rebuild gaps fail the same tests as in the
+// row walk (low word 0xFFFFFFFF or value 0; KEY_NONE's source is out of
+// range). The frontier words of all 8, then their visited words, are loaded
+// before any claim, so each thread keeps 8 requests in flight per stage.
+__device__ __forceinline__ uint32_t dense_visit8(const BfsArgs &A, const uint64_t (&k)[8], uint2 v,
+                                                 const uint32_t *front_cur, uint32_t next_level,
+                                                 uint32_t *front_next) {
+    uint32_t dst[8], word[8];
+    bool c[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const uint32_t src = (uint32_t)(k[j] >> 32);
+        const uint32_t val = ((j < 4 ? v.x : v.y) >> (8 * (j & 3))) & 0xFFu;
+        dst[j] = (uint32_t)k[j];
+        c[j] = dst[j] != 0xFFFFFFFFu && val != 0 && src < A.n && dst[j] < A.n;
+        word[j] = c[j] ? front_cur[src >> 5] >> (src & 31) : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        c[j] = c[j] && (word[j] & 1u);
+        word[j] = c[j] ? A.visited[dst[j] >> 5] : 0xFFFFFFFFu;
+    }
+    uint32_t fresh = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const uint32_t bit = 1u << (dst[j] & 31);
+        if (c[j] && !(word[j] & bit) && !(atomicOr(&A.visited[dst[j] >> 5], bit) & bit)) {
+            A.levels[dst[j]] = next_level;
+            atomicOr(&front_next[dst[j] >> 5], bit);
+            ++fresh;
+        }
+    }
+    return fresh;
+}
+
 // Slot of concatenated-range position p (< total) of a warp's rows: lane r
 // holds its row start b and exclusive prefix excl; finds the last r with
 // excl[r] <= p. All lanes must call it together.
@@ -122,7 +165,10 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
     uint32_t added = 0;
     uint32_t i = 0;
     for (;; ++i) {
-        if (ld_volatile(A.ctl + CTL_CNT + i % 3) == 0)
+        if (A.stamps && blockIdx.x == 0 && threadIdx.x == 0 && i < CTL_PROFILE_LEVELS)
+            A.stamps[i] = globaltimer_ns();
+        const uint32_t frontier = cta_broadcast_read(A.ctl + CTL_CNT + i % 3);
+        if (frontier == 0)
             break;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             A.ctl[CTL_CNT + (i + 2) % 3] = 0;
@@ -133,6 +179,42 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
         uint32_t *chunk_cnt = A.ctl + CTL_CHUNKS + i % 3;
         const uint32_t next_level = i + 2;
         uint32_t fresh = 0;
+        // Dense level (the frontier holds >= n / dense_div nodes): every slot
+        // in one coalesced sweep, 8 slots per thread per step; then, after a
+        // barrier, the frontier is cleared for its reuse two levels later.
+        const bool dense = A.dense_div && (uint64_t)frontier * A.dense_div >= A.n;
+        if (A.stamps && blockIdx.x == 0 && threadIdx.x == 0 && i < CTL_PROFILE_LEVELS)
+            reinterpret_cast<uint32_t *>(A.stamps + CTL_PROFILE_LEVELS)[i] = frontier | (dense ? 1u << 31 : 0u);
+        if (dense) {
+            const uint32_t gtid = blockIdx.x * BLOCK + threadIdx.x;
+            const uint32_t nthreads = gridDim.x * BLOCK;
+            const ulonglong2 *kv = reinterpret_cast<const ulonglong2 *>(A.keys);
+            const uint2 *vv = reinterpret_cast<const uint2 *>(A.vals);
+            for (uint32_t o = gtid; o < (A.size >> 3); o += nthreads) {
+                const ulonglong2 k0 = kv[4 * o], k1 = kv[4 * o + 1], k2 = kv[4 * o + 2], k3 = kv[4 * o + 3];
+                const uint64_t k[8] = {k0.x, k0.y, k1.x, k1.y, k2.x, k2.y, k3.x, k3.y};
+                fresh += dense_visit8(A, k, vv[o], front_cur, next_level, front_next);
+            }
+            // an array of 4 slots (the smallest size): one thread takes it, padded with empty slots
+            if (A.size < 8 && gtid == 0) {
+                const uint64_t k[8] = {A.keys[0], A.keys[1], A.keys[2], A.keys[3], KEY_NONE, KEY_NONE, KEY_NONE, KEY_NONE};
+                const uint2 v = make_uint2(A.vals[0] | (A.vals[1] << 8) | (A.vals[2] << 16) | ((uint32_t)A.vals[3] << 24), 0u);
+                fresh += dense_visit8(A, k, v, front_cur, next_level, front_next);
+            }
+            if (!grid_barrier(bar, err))
+                return;
+            for (uint32_t w = gtid; w < words; w += nthreads)
+                front_cur[w] = 0;
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1)
+                fresh += __shfl_xor_sync(0xFFFFFFFFu, fresh, d);
+            if (lane == 0 && fresh)
+                atomicAdd(A.ctl + CTL_CNT + (i + 1) % 3, fresh);
+            added += fresh;
+            if (!grid_barrier(bar, err))
+                return;
+            continue;
+        }
         // Phase 1: each warp takes one frontier word at a time, lane l owning
         // node 32*word + l. Short rows are walked as one concatenated slot
         // range, 64 slots per step; long rows are queued as chunks.
@@ -181,7 +263,7 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
         if (!grid_barrier(bar, err))
             return;
         // Phase 2: long-row chunks, one warp per chunk (64 slots = one step).
-        const uint32_t nch_all = min(ld_volatile(chunk_cnt), A.chunk_cap);
+        const uint32_t nch_all = min(cta_broadcast_read(chunk_cnt), A.chunk_cap);
         for (uint32_t c = gwarp; c < nch_all; c += nwarps) {
             const uint2 ch = A.chunks[c];
             for (uint32_t s0 = ch.x; s0 < ch.y; s0 += 64) {
@@ -226,9 +308,9 @@ gpma_status ensure_bfs(gpma_graph *g) {
     GPMA_TRY(dev_alloc(&g->bfs_front[0], n / 32 + 2));
     GPMA_TRY(dev_alloc(&g->bfs_front[1], n / 32 + 2));
     GPMA_TRY(dev_alloc(&g->bfs_chunks, BFS_CHUNK_CAP));
-    GPMA_TRY(dev_alloc(&g->bfs_ctl, CTL_WORDS + 2 * 64));
+    GPMA_TRY(dev_alloc(&g->bfs_ctl, CTL_WORDS + CTL_PROFILE_WORDS));
     if (!g->h_bfs_ctl) {
-        cudaError_t e = cudaMallocHost((void **)&g->h_bfs_ctl, sizeof(uint32_t) * (CTL_WORDS + 2 * 64));
+        cudaError_t e = cudaMallocHost((void **)&g->h_bfs_ctl, sizeof(uint32_t) * (CTL_WORDS + CTL_PROFILE_WORDS));
         if (e != cudaSuccess)
             return cuda_fail(e, "cudaMallocHost(bfs ctl)");
     }
@@ -240,7 +322,7 @@ gpma_status ensure_bfs(gpma_graph *g) {
             set_error("BFS kernel cannot be resident (occupancy 0)");
             return GPMA_ERR_CUDA;
         }
-        g->bfs_grid = g->sms * std::min(per_sm, 8);
+        g->bfs_grid = std::min(per_sm, MAX_BLOCKS_PER_SM);  // resident CTAs per SM
     }
     return GPMA_OK;
 }
@@ -281,10 +363,15 @@ gpma_status bfs_run(gpma_graph *g, uint32_t src, cudaStream_t s, uint64_t *reach
     A.chunks = g->bfs_chunks;
     A.chunk_cap = BFS_CHUNK_CAP;
     A.ctl = g->bfs_ctl;
+    A.dense_div = g_tuning.bfs_dense_div;
+    A.stamps = g->profiling ? reinterpret_cast<unsigned long long *>(g->bfs_ctl + CTL_WORDS) : nullptr;
     void *params[] = {&A};
-    GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)bfs_kernel, dim3(g->bfs_grid), dim3(BLOCK), params, 0, s));
+    const int grid = g->sms * blocks_per_sm(g->bfs_grid, g_tuning.bfs_blocks_per_sm);
+    GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)bfs_kernel, dim3(grid), dim3(BLOCK), params, 0, s));
     prof_mark(g, 1, s);
-    GPMA_CUDA(cudaMemcpyAsync(g->h_bfs_ctl, g->bfs_ctl, sizeof(uint32_t) * CTL_WORDS, cudaMemcpyDeviceToHost, s));
+    GPMA_CUDA(cudaMemcpyAsync(g->h_bfs_ctl, g->bfs_ctl,
+                              sizeof(uint32_t) * (CTL_WORDS + (g->profiling ? CTL_PROFILE_WORDS : 0)),
+                              cudaMemcpyDeviceToHost, s));
     GPMA_CUDA(cudaStreamSynchronize(s));
     g->prof.kernel_launches += 2;
     g->prof.bfs_kernels++;
@@ -344,11 +431,11 @@ gpma_status noalloc_scratch(uint32_t **out, int *grid, int sms) {
             set_error("gpma_bfs_noalloc: BFS kernel cannot be resident (occupancy 0)");
             return GPMA_ERR_CUDA;
         }
-        g_noalloc_grid[dev] = sms * std::min(per_sm, 8);
+        g_noalloc_grid[dev] = std::min(per_sm, MAX_BLOCKS_PER_SM);
         g_noalloc_ptr[dev] = static_cast<uint32_t *>(p);
     }
     *out = g_noalloc_ptr[dev];
-    *grid = g_noalloc_grid[dev];
+    *grid = sms * blocks_per_sm(g_noalloc_grid[dev], g_tuning.bfs_blocks_per_sm);
     return GPMA_OK;
 }
 
@@ -388,6 +475,8 @@ gpma_status bfs_noalloc_run(gpma_graph *g, uint32_t src, uint32_t *levels, uint6
     A.chunks = chunks;
     A.chunk_cap = NOALLOC_CHUNK_CAP;
     A.ctl = ctl;
+    A.dense_div = g_tuning.bfs_dense_div;
+    A.stamps = nullptr;
     void *params[] = {&A};
     GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)bfs_kernel, dim3(grid), dim3(BLOCK), params, 0, s));
     uint32_t h_ctl[CTL_WORDS];
@@ -403,3 +492,28 @@ gpma_status bfs_noalloc_run(gpma_graph *g, uint32_t src, uint32_t *levels, uint6
 }
 
 }  // namespace gpma
+
+extern "C" gpma_status gpma_bfs_level_profile(const gpma_graph *g, double *ms, uint32_t *frontier, uint8_t *dense,
+                                              uint32_t capacity, uint32_t *levels) {
+    using namespace gpma;
+    if (!g || !levels) {
+        gpma::set_error("gpma_bfs_level_profile: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    *levels = 0;
+    if (!g->profiling || !g->h_bfs_ctl)
+        return GPMA_OK;
+    const uint32_t L = std::min<uint32_t>(g->h_bfs_ctl[CTL_LEVELS], CTL_PROFILE_LEVELS - 1);
+    const uint64_t *st = reinterpret_cast<const uint64_t *>(g->h_bfs_ctl + CTL_WORDS);
+    const uint32_t *info = reinterpret_cast<const uint32_t *>(st + CTL_PROFILE_LEVELS);
+    *levels = L;
+    for (uint32_t i = 0; i < std::min(L, capacity); ++i) {
+        if (ms)
+            ms[i] = (double)(st[i + 1] - st[i]) * 1e-6;
+        if (frontier)
+            frontier[i] = info[i] & 0x7FFFFFFFu;
+        if (dense)
+            dense[i] = (uint8_t)(info[i] >> 31);
+    }
+    return GPMA_OK;
+}

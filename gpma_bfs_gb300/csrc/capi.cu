@@ -603,6 +603,38 @@ gpma_status gpma_batch_reset_profile(gpma_batch *b) {
     return GPMA_OK;
 }
 
+gpma_status gpma_get_tuning(gpma_tuning *out) {
+    if (!out) {
+        set_error("gpma_get_tuning: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    *out = gpma_tuning{};
+    out->bfs_dense_div = g_tuning.bfs_dense_div;
+    out->bfs_blocks_per_sm = g_tuning.bfs_blocks_per_sm;
+    out->ms_dense_div = g_tuning.ms_dense_div;
+    out->ms_blocks_per_sm = g_tuning.ms_blocks_per_sm;
+    out->update_blocks_per_sm = g_tuning.update_blocks_per_sm;
+    return GPMA_OK;
+}
+
+gpma_status gpma_set_tuning(const gpma_tuning *t) {
+    if (!t) {
+        set_error("gpma_set_tuning: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    if (t->bfs_blocks_per_sm > MAX_BLOCKS_PER_SM || t->ms_blocks_per_sm > MAX_BLOCKS_PER_SM ||
+        t->update_blocks_per_sm > MAX_BLOCKS_PER_SM) {
+        set_error("gpma_set_tuning: CTAs per SM above %d", MAX_BLOCKS_PER_SM);
+        return GPMA_ERR_INVALID;
+    }
+    g_tuning.bfs_dense_div = t->bfs_dense_div;
+    g_tuning.bfs_blocks_per_sm = t->bfs_blocks_per_sm;
+    g_tuning.ms_dense_div = t->ms_dense_div;
+    g_tuning.ms_blocks_per_sm = t->ms_blocks_per_sm;
+    g_tuning.update_blocks_per_sm = t->update_blocks_per_sm;
+    return GPMA_OK;
+}
+
 gpma_status gpma_get_geometry(const gpma_graph *g, gpma_geometry *out) {
     if (!g || !out) {
         set_error("gpma_get_geometry: null argument");

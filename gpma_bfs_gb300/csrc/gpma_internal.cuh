@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -171,7 +172,7 @@ struct gpma_graph {
     uint32_t *bfs_levels = nullptr;
     uint32_t *bfs_ctl = nullptr;       // counters + status
     uint32_t *h_bfs_ctl = nullptr;     // pinned
-    int bfs_grid = 0;
+    int bfs_grid = 0;                  // resident BFS-kernel CTAs per SM (0: not yet known)
     gpma_batch *own_batch = nullptr;   // multi-source BFS context of this graph
     gpma_stats stats{};
     // profiling: events on the caller's stream around each phase
@@ -192,6 +193,7 @@ struct gpma_batch {
     uint64_t ms_cap = 0;               // nodes
     uint64_t *ms_mask[3] = {nullptr, nullptr, nullptr};
     uint32_t *ms_voff = nullptr;       // node offsets, graphs + 1
+    uint64_t *ms_soff = nullptr;       // slot offsets of the concatenated arrays, graphs + 1
     uint32_t *ms_src = nullptr;        // sources, graphs * 64
     uint32_t *ms_nsrc = nullptr;       // sources per graph
     uint32_t *ms_ctl = nullptr;
@@ -283,6 +285,24 @@ void free_bfs(gpma_graph *g);
 void free_batch_bfs(gpma_batch *b);
 int update_grid_size(int sms);
 
+// Launch shapes and switch points: they change speed, never results
+// (process-wide, set through gpma_set_tuning; defaults from measurement).
+struct Tuning {
+    uint32_t bfs_dense_div = 4;
+    uint32_t bfs_blocks_per_sm = 8;
+    uint32_t ms_dense_div = 8;
+    uint32_t ms_blocks_per_sm = 8;
+    uint32_t update_blocks_per_sm = 0;  // 0: as many as fit
+};
+extern Tuning g_tuning;
+// CTAs per SM for a kernel that fits `fit` per SM, given a tuned request (0 = fit).
+inline int blocks_per_sm(int fit, uint32_t want) {
+    if (fit < 1)
+        return 0;
+    return want == 0 ? fit : std::min<int>(fit, (int)want);
+}
+constexpr int MAX_BLOCKS_PER_SM = 32;
+
 }  // namespace gpma
 
 // ---- device helpers --------------------------------------------------------
@@ -332,6 +352,18 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *bar, uint32_t *err) {
     }
     __syncthreads();
     return s_ok != 0;
+}
+
+// One volatile read per CTA, broadcast through shared memory: a word that
+// every warp of a persistent grid needs after a barrier costs one L2 request
+// per CTA instead of one per warp. Every thread of the CTA must call it.
+__device__ __forceinline__ uint32_t cta_broadcast_read(const uint32_t *p) {
+    __shared__ uint32_t s_v;
+    __syncthreads();  // readers of the previous value are done
+    if (threadIdx.x == 0)
+        s_v = ld_volatile(p);
+    __syncthreads();
+    return s_v;
 }
 
 __device__ __forceinline__ uint32_t lanemask_lt() {

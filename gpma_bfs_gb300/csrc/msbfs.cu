@@ -33,6 +33,7 @@ enum : uint32_t {
     MS_ERR = 6,
     MS_LEVELS = 7,
     MS_BAR = 10,    // GridBarrier (2 words)
+    MS_FRONT = 12,  // 3 rotating counters: nodes in the next union frontier
     MS_CTL_WORDS = 16,
 };
 
@@ -53,6 +54,7 @@ struct MsArgs {
     uint32_t G;
     const uint32_t *voff;  // G + 1
     const uint32_t *src;   // G * 64
+    const uint64_t *soff;  // slot offsets of the concatenated arrays, G + 1 (multiples of 4)
     uint64_t *visited;
     uint64_t *frontier;
     uint64_t *next;
@@ -61,6 +63,7 @@ struct MsArgs {
     uint32_t *ctl;
     unsigned long long *reached;  // G * 64
     unsigned long long *traversed;
+    uint32_t dense_div;    // a level whose union frontier holds >= N / dense_div nodes sweeps every slot (0: never)
 };
 
 __device__ __forceinline__ uint32_t graph_of_node(const MsArgs &A, uint32_t u) {
@@ -78,6 +81,47 @@ __device__ __forceinline__ uint32_t ms_visit(const MsArgs &A, const MsGraph &Gr,
     if (nb && (A.next[gw] & nb) != nb)
         atomicOr((unsigned long long *)&A.next[gw], (unsigned long long)nb);
     return 1;
+}
+
+// Dense levels: 4 consecutive slots of the sweep over every graph's array
+// (node offset vo, n nodes). The key's high word is its source row. The
+// frontier masks of all 4, then the visited and next masks of their targets,
+// are loaded before any update. Returns the lanes that traverse the 4 slots.
+__device__ __forceinline__ uint32_t ms_dense_visit4(const MsArgs &A, uint32_t vo, uint32_t n,
+                                                    const uint64_t (&k)[4], uint32_t v4) {
+    uint32_t dst[4];
+    uint64_t fm[4], nb[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t src = (uint32_t)(k[j] >> 32);
+        dst[j] = (uint32_t)k[j];
+        const bool ok = dst[j] != 0xFFFFFFFFu && ((v4 >> (8 * j)) & 0xFFu) != 0 && src < n && dst[j] < n;
+        fm[j] = ok ? A.frontier[vo + src] : 0ull;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        nb[j] = fm[j] ? fm[j] & ~A.visited[vo + dst[j]] : 0ull;
+    uint32_t lanes = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        lanes += __popcll(fm[j]);
+        if (nb[j] && (A.next[vo + dst[j]] & nb[j]) != nb[j])
+            atomicOr((unsigned long long *)&A.next[vo + dst[j]], (unsigned long long)nb[j]);
+    }
+    return lanes;
+}
+
+// Graph of concatenated slot t: the last g with soff[g] <= t.
+__device__ __forceinline__ uint32_t graph_of_slot(const MsArgs &A, uint64_t t) {
+    uint32_t lo = 0, hi = A.G;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (A.soff[mid] <= t)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
 }
 
 __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
@@ -109,10 +153,27 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             A.ctl[MS_CHANGE + (level + 1) % 3] = 0;
             A.ctl[MS_CHUNKS + (level + 1) % 3] = 0;
+            A.ctl[MS_FRONT + (level + 2) % 3] = 0;
         }
         uint32_t *chunk_cnt = A.ctl + MS_CHUNKS + level % 3;
-        // expand, phase 1
-        for (uint32_t base = gwarp * 32; base < N; base += nwarps * 32) {
+        const uint32_t fcount = cta_broadcast_read(A.ctl + MS_FRONT + level % 3);
+        const bool dense = A.dense_div && (uint64_t)fcount * A.dense_div >= N;
+        // expand, dense: every slot of every graph, 4 per thread per step; the
+        // frontier masks stay in place until the commit clears them
+        const uint64_t quads = dense ? A.soff[A.G] >> 2 : 0;
+        for (uint64_t q = gtid; q < quads; q += nthreads) {
+            const uint64_t t = q << 2;
+            const uint32_t g = A.G == 1 ? 0u : graph_of_slot(A, t);
+            const MsGraph &Gr = A.gr[g];
+            const uint32_t s = (uint32_t)(t - A.soff[g]);
+            const ulonglong2 k01 = *reinterpret_cast<const ulonglong2 *>(Gr.keys + s);
+            const ulonglong2 k23 = *reinterpret_cast<const ulonglong2 *>(Gr.keys + s + 2);
+            const uint32_t v4 = *reinterpret_cast<const uint32_t *>(Gr.vals + s);
+            const uint64_t k[4] = {k01.x, k01.y, k23.x, k23.y};
+            traversed += ms_dense_visit4(A, A.voff[g], Gr.n, k, v4);
+        }
+        // expand, phase 1 (sparse levels)
+        for (uint32_t base = gwarp * 32; !dense && base < N; base += nwarps * 32) {
             const uint32_t u = base + lane;
             const uint64_t f = u < N ? A.frontier[u] : 0ull;
             if (__ballot_sync(0xFFFFFFFFu, f != 0ull) == 0)
@@ -170,10 +231,10 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
                     traversed += ms_visit(A, A.gr[rg], rg, rb + (p - rex), rf) * (unsigned long long)__popcll(rf);
             }
         }
-        if (!grid_barrier(bar, err))
+        if (!dense && !grid_barrier(bar, err))
             return;
         // expand, phase 2: long-row chunks
-        const uint32_t nch_all = min(ld_volatile(chunk_cnt), A.chunk_cap);
+        const uint32_t nch_all = dense ? 0u : min(cta_broadcast_read(chunk_cnt), A.chunk_cap);
         for (uint32_t c = gwarp; c < nch_all; c += nwarps) {
             const uint4 ch = A.chunks[c];
             if (ch.x >= ch.y)
@@ -186,7 +247,7 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
         if (!grid_barrier(bar, err))
             return;
         // commit
-        uint32_t changed = 0;
+        uint32_t changed = 0, fnext = 0;
         for (uint32_t w = gtid; w < N; w += nthreads) {
             const uint64_t nxt = A.next[w];
             const uint64_t vis = A.visited[w];
@@ -199,6 +260,7 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
                 A.frontier[w] = nx;
                 A.visited[w] = vis | nx;
                 changed = 1;
+                ++fnext;
                 const uint32_t g = graph_of_node(A, w);
                 const MsGraph &Gr = A.gr[g];
                 if (Gr.levels) {
@@ -214,9 +276,14 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
         }
         if (__syncthreads_or(changed) && threadIdx.x == 0)
             atomicAdd(A.ctl + MS_CHANGE + level % 3, 1u);
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1)
+            fnext += __shfl_xor_sync(0xFFFFFFFFu, fnext, d);
+        if (lane == 0 && fnext)
+            atomicAdd(A.ctl + MS_FRONT + (level + 1) % 3, fnext);
         if (!grid_barrier(bar, err))
             return;
-        if (ld_volatile(A.ctl + MS_CHANGE + level % 3) == 0)
+        if (cta_broadcast_read(A.ctl + MS_CHANGE + level % 3) == 0)
             break;
     }
     // reached (graph, lane) counts: each CTA walks a contiguous node range
@@ -253,20 +320,20 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
         A.ctl[MS_LEVELS] = level;
 }
 
-int g_ms_grid[64] = {};
+int g_ms_fit[64] = {};  // resident CTAs per SM, per device
 
 int ms_grid_size(int sms) {
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64)
         dev = 0;
-    if (g_ms_grid[dev] == 0) {
+    if (g_ms_fit[dev] == 0) {
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, msbfs_kernel, BLOCK, 0) != cudaSuccess)
             return 0;
-        g_ms_grid[dev] = sms * std::min(per_sm, 8);
+        g_ms_fit[dev] = std::min(per_sm, MAX_BLOCKS_PER_SM);
     }
-    return g_ms_grid[dev];
+    return sms * blocks_per_sm(g_ms_fit[dev], g_tuning.ms_blocks_per_sm);
 }
 
 }  // namespace
@@ -275,6 +342,7 @@ void free_batch_bfs(gpma_batch *b) {
     for (int i = 0; i < 3; ++i)
         dev_free(b->ms_mask[i]);
     dev_free(b->ms_voff);
+    dev_free(b->ms_soff);
     dev_free(b->ms_src);
     dev_free(b->ms_nsrc);
     dev_free(b->ms_ctl);
@@ -300,8 +368,11 @@ gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32
         return GPMA_ERR_CUDA;
     }
     std::vector<uint32_t> voff(k + 1, 0);
-    for (uint32_t i = 0; i < k; ++i)
+    std::vector<uint64_t> soff(k + 1, 0);
+    for (uint32_t i = 0; i < k; ++i) {
         voff[i + 1] = voff[i] + graphs[i]->row_num;
+        soff[i + 1] = soff[i] + graphs[i]->geo.size;  // sizes are powers of two >= 4
+    }
     const uint64_t N = voff[k];
     if (N > b->ms_cap || !b->ms_mask[0]) {
         for (int i = 0; i < 3; ++i)
@@ -313,11 +384,13 @@ gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32
     }
     if (k > b->ms_gcap || !b->ms_voff) {
         dev_free(b->ms_voff);
+        dev_free(b->ms_soff);
         dev_free(b->ms_src);
         dev_free(b->ms_gdesc);
         dev_free(b->ms_reached);
         b->ms_gcap = 0;
         GPMA_TRY(dev_alloc(&b->ms_voff, k + 1));
+        GPMA_TRY(dev_alloc(&b->ms_soff, k + 1));
         GPMA_TRY(dev_alloc(&b->ms_src, 64ull * k));
         uint8_t *gd = nullptr;
         GPMA_TRY(dev_alloc(&gd, sizeof(MsGraph) * k));
@@ -367,6 +440,7 @@ gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32
     }
     auto step = [&]() -> gpma_status {
         GPMA_CUDA(cudaMemcpyAsync(b->ms_voff, voff.data(), sizeof(uint32_t) * (k + 1), cudaMemcpyHostToDevice, s));
+        GPMA_CUDA(cudaMemcpyAsync(b->ms_soff, soff.data(), sizeof(uint64_t) * (k + 1), cudaMemcpyHostToDevice, s));
         GPMA_CUDA(cudaMemcpyAsync(b->ms_src, hsrc.data(), sizeof(uint32_t) * 64 * k, cudaMemcpyHostToDevice, s));
         GPMA_CUDA(cudaMemcpyAsync(b->ms_gdesc, gr.data(), sizeof(MsGraph) * k, cudaMemcpyHostToDevice, s));
         for (int i = 0; i < 3; ++i)
@@ -378,6 +452,8 @@ gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32
         A.G = k;
         A.voff = b->ms_voff;
         A.src = b->ms_src;
+        A.soff = b->ms_soff;
+        A.dense_div = g_tuning.ms_dense_div;
         A.visited = b->ms_mask[0];
         A.frontier = b->ms_mask[1];
         A.next = b->ms_mask[2];

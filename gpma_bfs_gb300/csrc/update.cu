@@ -1171,25 +1171,27 @@ GraphDesc describe(const gpma_graph *g) {
     return d;
 }
 
-int g_update_grid[64] = {};
+int g_update_fit[64] = {};  // resident update-kernel CTAs per SM, per device
 
 }  // namespace
+
+Tuning g_tuning;
 
 int update_grid_size(int sms) {
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64)
         dev = 0;
-    if (g_update_grid[dev] == 0) {
+    if (g_update_fit[dev] == 0) {
         if (cudaFuncSetAttribute(update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)UPDATE_SMEM) !=
             cudaSuccess)
             return 0;
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, update_kernel, BLOCK, UPDATE_SMEM) != cudaSuccess)
             return 0;
-        g_update_grid[dev] = sms * std::min(per_sm, 4);
+        g_update_fit[dev] = std::min(per_sm, MAX_BLOCKS_PER_SM);
     }
-    return g_update_grid[dev];
+    return sms * blocks_per_sm(g_update_fit[dev], g_tuning.update_blocks_per_sm);
 }
 
 gpma_status ensure_scratch(gpma_graph *g, uint32_t slots) {
@@ -1328,7 +1330,7 @@ gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32
     }
     GPMA_TRY(ensure_buffers(buf, n, k));
     if (!buf.cta_cnt)
-        GPMA_TRY(dev_alloc(&buf.cta_cnt, 4ull * grid));
+        GPMA_TRY(dev_alloc(&buf.cta_cnt, 4ull * sms * MAX_BLOCKS_PER_SM));  // any tuned grid
     // per-graph tables: descriptors, batch offsets, sort tile offsets
     buf.h_gd.resize(k);
     buf.h_off.assign(2ull * (k + 1), 0);

@@ -311,6 +311,28 @@ GPMA_API gpma_status gpma_reset_profile(gpma_graph *g);
 GPMA_API gpma_status gpma_batch_set_profiling(gpma_batch *b, int enabled);
 GPMA_API gpma_status gpma_batch_get_profile(const gpma_batch *b, gpma_profile *out);
 GPMA_API gpma_status gpma_batch_reset_profile(gpma_batch *b);
+/* Per level of the last gpma_bfs run with profiling on: its duration (ms, from
+ * %globaltimer stamps at level starts), its frontier size and whether it swept
+ * the whole array (dense). Up to `capacity` entries; *levels = levels run
+ * (0 when the last BFS was not profiled). */
+GPMA_API gpma_status gpma_bfs_level_profile(const gpma_graph *g, double *ms, uint32_t *frontier, uint8_t *dense,
+                                            uint32_t capacity, uint32_t *levels);
+
+/* ---- tuning -----------------------------------------------------------------
+ * No reference counterpart. Launch shapes and switch points of the kernels;
+ * they change speed, never results (the PMA geometry itself is fixed by the
+ * reference's sizing rules). Process-wide; takes effect at the next call. */
+typedef struct gpma_tuning {
+    uint32_t bfs_dense_div;        /* single-source BFS: a level whose frontier holds >= row_num / bfs_dense_div
+                                      nodes sweeps the whole slot array instead of walking rows (0: never) */
+    uint32_t bfs_blocks_per_sm;    /* BFS grid: CTAs per SM (capped by occupancy; 0: as many as fit) */
+    uint32_t ms_dense_div;         /* multi-source BFS: the same switch on the union frontier of all lanes */
+    uint32_t ms_blocks_per_sm;     /* multi-source BFS grid */
+    uint32_t update_blocks_per_sm; /* persistent update kernel grid (0: as many as fit) */
+    uint32_t reserved[3];
+} gpma_tuning;
+GPMA_API gpma_status gpma_get_tuning(gpma_tuning *out);
+GPMA_API gpma_status gpma_set_tuning(const gpma_tuning *t);
 
 /* ---- diagnostics ---------------------------------------------------------- */
 GPMA_API const char *gpma_status_string(gpma_status s);
