@@ -370,7 +370,12 @@ def run_batched(args, stream):
         return a.elapsed_time(c)
 
     bt, pt, nupd = [], [], 0
+    b.set_profiling(True)
+    slots0 = 0
     for j, (dk, dv, o) in enumerate(staged):
+        if j == args.warmup:
+            b.reset_profile()
+            slots0 = sum(x.stats()["accepted_slots"] for x in graphs_p)
         tb = timed(lambda: b.update_packed(graphs_b, dk, dv, o, stream))
 
         def plain():
@@ -385,6 +390,20 @@ def run_batched(args, stream):
             nupd += int(o[-1])
     # the two copies must agree (same batches, same algorithm)
     same = all(np.array_equal(x.export_layout()[0], y.export_layout()[0]) for x, y in zip(graphs_b, graphs_p))
+    # phases of the batched launch (in-kernel stamps) and its roofline: the
+    # plain copies ran the same windows, so their stats give the accepted slots
+    prof = b.profile()
+    steps_t = max(1, len(bt))
+    slots = sum(x.stats()["accepted_slots"] for x in graphs_p) - slots0
+    upd_bytes = 18.0 * nupd + 18.0 * slots
+    peak, peak_src = peak_hbm()
+    kern_s = prof["update_kernel_ms"] * 1e-3
+    b_roof = {"bound": "hbm", "kernel": "update_kernel (256 graphs per launch)",
+              "achieved": upd_bytes / kern_s / 1e9 if kern_s else None, "peak": peak, "unit": "GB/s",
+              "frac": upd_bytes / kern_s / 1e9 / peak if kern_s else None,
+              "algorithmic_bytes_per_launch": upd_bytes / steps_t, "peak_source": peak_src}
+    b_phases = {k: prof[k] / steps_t for k in ("update_kernel_ms", "sort_ms", "locate_ms", "group_ms", "levels_ms",
+                                               "rebuild_ms")}
     # 64-source BFS on every graph
     sources = []
     for (nn, kk) in specs:
@@ -417,7 +436,8 @@ def run_batched(args, stream):
         "updates_per_step": nupd / max(1, len(bt)),
         "update": {"batched_updates_per_s": nupd / sb, "batched_ms_per_step": 1e3 * sb / len(bt),
                    "plain_updates_per_s": nupd / sp_, "plain_ms_per_step": 1e3 * sp_ / len(pt),
-                   "speedup": sp_ / sb, "identical_layouts": same},
+                   "speedup": sp_ / sb, "identical_layouts": same,
+                   "phases_ms_per_step": b_phases, "roofline": b_roof},
         "bfs": {"sources_per_graph": 64, "edges_traversed": edges_b,
                 "batched_ms": tbb, "batched_gteps": edges_b / (tbb * 1e-3) / 1e9,
                 "plain_ms": tpb, "plain_gteps": edges_b / (tpb * 1e-3) / 1e9, "speedup": tpb / tbb},

@@ -21,8 +21,13 @@
 
 namespace gpma {
 
-constexpr int SORT_ITEMS = 4;
-constexpr uint32_t SORT_TILE = BLOCK * SORT_ITEMS;  // 1024 keys
+// Keys per thread of a tile (build option; a tile of 2048 keys by default).
+#ifndef GPMA_SORT_ITEMS
+#define GPMA_SORT_ITEMS 8
+#endif
+constexpr int SORT_ITEMS = GPMA_SORT_ITEMS;
+constexpr uint32_t SORT_TILE = BLOCK * SORT_ITEMS;
+static_assert(SORT_TILE * 9 + (BLOCK / 32 + 2) * 256 * 4 <= UPDATE_SMEM, "sort tile exceeds the update kernel's smem");
 constexpr uint32_t SORT_FLAG_AGG = 1u << 30;
 constexpr uint32_t SORT_FLAG_INC = 2u << 30;
 constexpr uint32_t SORT_VALUE_MASK = (1u << 30) - 1;
