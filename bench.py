@@ -195,6 +195,11 @@ def run_gpu(args):
         ms = statistics.median(times)
         return {"reached": int(reached), "edges_traversed": edges, "ms": ms, "gteps": edges / (ms * 1e-3) / 1e9}
 
+    tuning = {}
+    if not args.no_autotune:
+        import gpma_bfs_gb300.autotune as T
+
+        tuning["bfs"] = T.autotune({"bfs": T.bfs_probe(g, 0, torch.empty(n, dtype=torch.int32, device="cuda"))})["bfs"]
     bfs_before = timed_bfs(args.bfs_repeats)
 
     total = args.warmup + args.steps
@@ -298,6 +303,7 @@ def run_gpu(args):
                     "d2h_bytes_per_step": 64},
             "gpu_launches": prof["kernel_launches"],
             "clocks": clk.summary(),
+            "autotune": tuning or None,
             "bfs": {"before": bfs_before, "after": bfs_after, "unit": "GTEPS",
                     "gteps": bfs_after["gteps"]},
             "phases_ms_per_step": {"update_kernel": prof["update_kernel_ms"] / args.steps,
@@ -410,6 +416,11 @@ def run_batched(args, stream):
         cand = np.unique((kk >> np.uint64(32)).astype(np.uint32))
         sources.append(rng.choice(cand, min(64, len(cand)), replace=False).astype(np.uint32))
     b.set_profiling(True)
+    tuned = None
+    if not args.no_autotune:
+        import gpma_bfs_gb300.autotune as T
+
+        tuned = T.autotune({"ms": T.ms_probe(b, graphs_b, sources)})["ms"]
     b.bfs_multi(graphs_b, sources)  # warm-up
     b.reset_profile()
     tbb = timed(lambda: b.bfs_multi(graphs_b, sources, stream=stream))
@@ -438,7 +449,7 @@ def run_batched(args, stream):
                    "plain_updates_per_s": nupd / sp_, "plain_ms_per_step": 1e3 * sp_ / len(pt),
                    "speedup": sp_ / sb, "identical_layouts": same,
                    "phases_ms_per_step": b_phases, "roofline": b_roof},
-        "bfs": {"sources_per_graph": 64, "edges_traversed": edges_b,
+        "bfs": {"sources_per_graph": 64, "edges_traversed": edges_b, "autotune": tuned,
                 "batched_ms": tbb, "batched_gteps": edges_b / (tbb * 1e-3) / 1e9,
                 "plain_ms": tpb, "plain_gteps": edges_b / (tpb * 1e-3) / 1e9, "speedup": tpb / tbb},
         "setup_s": {"generate": gen_s},
@@ -620,15 +631,16 @@ def main():
     ap.add_argument("--bfs-repeats", type=int, default=3)
     ap.add_argument("--cpu-sample-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the built-in tuning (no sweep before timing)")
     ap.add_argument("--batched-graphs", type=int, default=256, help="graphs of the batched configuration (0: skip)")
     ap.add_argument("--batched-steps", type=int, default=5)
     ap.add_argument("--served-seconds", type=float, default=600.0,
                     help="simulated seconds of served traffic (0: skip the served configuration)")
     ap.add_argument("--served-rate", type=float, default=20.0, help="served request arrivals per simulated second")
     ap.add_argument("--served-big-scale", type=int, default=22, help="R-MAT scale of the two large served graphs")
-    ap.add_argument("--served-burst-rate", type=float, default=5000.0,
+    ap.add_argument("--served-burst-rate", type=float, default=20000.0,
                     help="arrivals per simulated second of the saturating phase that follows")
-    ap.add_argument("--served-burst-seconds", type=float, default=4.0)
+    ap.add_argument("--served-burst-seconds", type=float, default=1.0)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -17,7 +17,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from . import GPMA, Server, gpma_bfs_multi, update_gpma
+from . import ERR_BUSY, GPMA, GPMAError, Server, gpma_bfs_multi, update_gpma
 from .workloads import SlidingStream
 
 
@@ -67,14 +67,22 @@ def replay_served(srv: Server, gids, streams, trace: Trace):
     ids = []
     rounds = []
     now, j = 0.0, 0
+    held = None  # a request the server refused as busy: retried after the next round
     while j < n or srv.queued()[0]:
         while j < n and trace.arrival[j] <= now:
             g = int(trace.graph[j])
-            if trace.kind[j] == 0:
-                k, v = streams[g].step(int(trace.size[j]))
-                ids.append(srv.submit_update(gids[g], k, v, float(trace.arrival[j])))
-            else:
-                ids.append(srv.submit_bfs(gids[g], trace.sources[j], float(trace.arrival[j])))
+            try:
+                if trace.kind[j] == 0:
+                    k, v = held if held is not None else streams[g].step(int(trace.size[j]))
+                    ids.append(srv.submit_update(gids[g], k, v, float(trace.arrival[j])))
+                else:
+                    ids.append(srv.submit_bfs(gids[g], trace.sources[j], float(trace.arrival[j])))
+            except GPMAError as e:
+                if e.status != ERR_BUSY or srv.queued()[0] == 0:
+                    raise  # not busy, or larger than the whole queue: never admissible
+                held = (k, v) if trace.kind[j] == 0 else None
+                break  # admission control: wait for a round to free queue slots
+            held = None
             j += 1
         r = srv.run_round(now)
         if r["updates"] + r["bfs_requests"] + r["failed"]:

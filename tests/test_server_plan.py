@@ -175,3 +175,28 @@ def test_replay_keeps_per_graph_order(G):
                 assert kinds[0] == 0  # the update is the first of the graph's requests in the round
     assert max(r["updates"] for r in out["rounds"]) > 1  # the burst batched several graphs
     srv.close()
+
+
+def test_replay_waits_when_the_queue_is_full(G):
+    """Admission control: with room for 4 requests the driver holds the rest
+    back until rounds free slots; every request still runs, in order."""
+    import gpma_bfs_gb300.serving as S
+    from gpma_bfs_gb300.workloads import SlidingStream
+
+    rng = np.random.default_rng(5)
+    specs = [(1024, rng.permutation(np.arange(1, 600, dtype=np.uint64) << np.uint64(32) | np.uint64(7)))
+             for _ in range(3)]
+    trace = S.make_trace(specs, [(1000.0, 0.2)], seed=2, min_batch=4, max_batch=40)
+    trace.arrival = np.zeros(len(trace))  # everything arrives at once
+    srv = G.Server(plan_only=True, max_queued=4)
+    gids = [srv.add_graph(n, len(k)) for n, k in specs]
+    out = S.replay_served(srv, gids, [SlidingStream(k) for _, k in specs], trace)
+    assert out["ok"].all()
+    assert max(len(r["requests"]) for r in out["rounds"]) <= 4
+    assert sorted(i for r in out["rounds"] for i in r["requests"]) == list(range(len(trace)))
+    big = G.Server(plan_only=True, max_queued_keys=10)
+    gid = big.add_graph(64, 10)
+    with pytest.raises(G.GPMAError):
+        big.submit_update(gid, *_upd(11), arrival=0.0)  # never admissible
+    srv.close()
+    big.close()
