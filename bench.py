@@ -564,6 +564,125 @@ def run_served(args, stream):
     }
 
 
+def run_sweep(args):
+    """Large single graph + batch sweep: R-MAT scale `sweep_scale` (edge factor
+    `sweep_edge_factor`, a/b/c = .57/.19/.19, seed 3, deduplicated, shuffled)
+    loaded except for a reserve of fresh edges; then, per insert:delete ratio
+    (1:0, 1:1, 0:1) and batch size (1k ... 10M), `sweep_reps` batches of fresh
+    inserts and uniformly drawn existing edges to delete, each timed alone
+    (device-resident batch, L2 flushed, CUDA events); then BFS from 16 random
+    non-isolated sources (one search each, and all 16 as lanes of one
+    multi-source search)."""
+    import torch
+
+    import gpma_bfs_gb300 as G
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    t0 = time.time()
+    src, dst = G.gen_rmat(args.sweep_scale, args.sweep_edge_factor, seed=3)
+    n = 1 << args.sweep_scale
+    keys = G.edges_to_keys(src, dst)
+    del src, dst
+    m = len(keys)
+    gen_s = time.time() - t0
+    reps = args.sweep_reps
+    # batch sizes the graph can feed (fresh inserts and distinct deletes)
+    sizes = [s for s in (1_000, 10_000, 100_000, 1_000_000, 10_000_000) if 2 * reps * s <= m // 4]
+    ratios = [(1, 0), (1, 1), (0, 1)]
+    reserve = sum(reps * s * i // (i + d) for s in sizes for i, d in ratios) + 1
+    loaded = keys[: m - reserve]
+    fresh = keys[m - reserve:]
+    rng = np.random.default_rng(3)
+    del_order = rng.permutation(len(loaded))  # deletes: uniformly drawn, each live edge at most once
+    g = G.GPMA(n, stream)
+    t0 = time.time()
+    chunk = 1 << 26
+    for i in range(0, len(loaded), chunk):
+        part = torch.from_numpy(loaded[i:i + chunk].view(np.int64)).cuda()
+        G.update_gpma(g, part, torch.ones(len(part), dtype=torch.uint8, device="cuda"), stream)
+        del part
+    torch.cuda.synchronize()
+    load_s = time.time() - t0
+    geo = g.geometry()
+    live = len(loaded) + n + 2
+    g.set_profiling(True)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    fi = di = 0
+    rows = []
+    peak, _ = peak_hbm()
+    for ins, dels in ratios:
+        for size in sizes:
+            times, kern, slots = [], [], []
+            for _ in range(reps):
+                ni = size * ins // (ins + dels)
+                nd = size - ni
+                k = np.concatenate([fresh[fi:fi + ni], loaded[del_order[di:di + nd]]])
+                v = np.concatenate([np.ones(ni, np.uint8), np.zeros(nd, np.uint8)])
+                fi += ni
+                di += nd
+                live += ni - nd
+                dk = torch.from_numpy(k.view(np.int64)).cuda()
+                dv = torch.from_numpy(v).cuda()
+                flush.fill_(1)
+                s0 = g.stats()["accepted_slots"]
+                g.reset_profile()
+                a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                G.update_gpma(g, dk, dv, stream)
+                c.record(stream)
+                torch.cuda.synchronize()
+                times.append(a.elapsed_time(c))
+                p = g.profile()
+                kern.append(p["update_kernel_ms"] + p["rebuild_ms"])
+                slots.append(g.stats()["accepted_slots"] - s0)
+            ms = statistics.median(times)
+            kms = statistics.median(kern)
+            bytes_ = 18.0 * size + 18.0 * statistics.median(slots)
+            rows.append({"ratio": f"{ins}:{dels}", "batch": size, "ms": ms, "edge_updates_per_s": size / (ms * 1e-3),
+                         "kernel_ms": kms, "hbm_frac": bytes_ / (kms * 1e-3) / 1e9 / peak if kms else None})
+    # BFS from 16 random non-isolated sources (live out-degree per row, once)
+    lk, lvals, ro = g.export_layout()
+    valid = ((lk & np.uint64(0xFFFFFFFF)) != np.uint64(0xFFFFFFFF)) & (lvals != 0)
+    del lk, lvals
+    csum = np.concatenate([[0], np.cumsum(valid, dtype=np.int64)])
+    del valid
+    ro = ro.astype(np.int64)
+    per_row = csum[ro[1:]] - csum[ro[:-1]]
+    del csum
+    cand = np.nonzero(per_row > 0)[0]
+    sources = rng.choice(cand, 16, replace=False).astype(np.uint32)
+    out = torch.empty(n, dtype=torch.int32, device="cuda")
+    single = []
+    for s in sources:
+        g.reset_profile()
+        G.gpma_bfs(g, n, live, int(s), out, stream)
+        lv = out.cpu().numpy().view(np.uint32)
+        single.append((g.profile()["bfs_ms"], int(per_row[lv != 0].sum()), int((lv != 0).sum())))
+    g.reset_profile()
+    lvm = torch.empty(16 * n, dtype=torch.int32, device="cuda")
+    G.gpma_bfs_multi(g, sources, lvm.view(16, n), stream=stream)
+    pm = g.profile()
+    bfs_ms = statistics.median(x[0] for x in single)
+    edges = statistics.median(x[1] for x in single)
+    g.close()
+    return {
+        "metric": "edge updates/s and BFS GTEPS, large single graph", "impl": "gpma",
+        "config": {"workload": f"R-MAT scale {args.sweep_scale}, edge factor {args.sweep_edge_factor}, "
+                               f"{m:,} edges after dedup, {len(loaded):,} loaded, batch sweep 1k-10M at 1:0 / 1:1 / "
+                               f"0:1, BFS from 16 random non-isolated sources",
+                   "l2": "flushed before every timed update"},
+        "geometry": geo, "density_after_load": (len(loaded) + n + 2) / geo["size"],
+        "load": {"edges": len(loaded), "seconds": load_s, "edges_per_s": len(loaded) / load_s},
+        "updates": rows,
+        "bfs": {"single_source_median_ms": bfs_ms, "median_edges": edges,
+                "gteps": edges / (bfs_ms * 1e-3) / 1e9,
+                "reached": [x[2] for x in single],
+                "multi16_ms": pm["bfs_ms"], "multi16_gteps": pm["bfs_edges"] / (pm["bfs_ms"] * 1e-3) / 1e9},
+        "setup_s": {"generate": gen_s},
+    }
+
+
 def cpu_baseline(n, keys, half, slide, steps):
     """The oracle restatement on all host cores: load untimed, `steps` slides timed."""
     from oracle.oracle import OracleGPMA, build
@@ -641,10 +760,17 @@ def main():
     ap.add_argument("--served-burst-rate", type=float, default=20000.0,
                     help="arrivals per simulated second of the saturating phase that follows")
     ap.add_argument("--served-burst-seconds", type=float, default=1.0)
+    ap.add_argument("--sweep", action="store_true",
+                    help="only the large-graph batch sweep (R-MAT scale 24, edge factor 32): its own JSON line")
+    ap.add_argument("--sweep-scale", type=int, default=24)
+    ap.add_argument("--sweep-edge-factor", type=int, default=32)
+    ap.add_argument("--sweep-reps", type=int, default=3)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
-    if args.impl == "reference":
+    if args.sweep:
+        print(json.dumps(run_sweep(args)), flush=True)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

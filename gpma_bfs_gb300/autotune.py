@@ -25,8 +25,8 @@ import numpy as np
 from . import GPMA, Batch, get_tuning, gpma_bfs, set_tuning
 
 SPACE = {
-    "bfs": {"bfs_blocks_per_sm": (2, 4, 8), "bfs_dense_div": (0, 2, 4, 8, 16)},
-    "ms": {"ms_blocks_per_sm": (4, 8), "ms_dense_div": (0, 4, 8, 16, 64)},
+    "bfs": {"bfs_blocks_per_sm": (4, 8), "bfs_dense_div": (0, 2, 3, 4, 6, 8)},
+    "ms": {"ms_blocks_per_sm": (4, 8), "ms_dense_div": (0, 2, 3, 4, 8, 16)},
     "update": {"update_blocks_per_sm": (1, 0)},
 }
 

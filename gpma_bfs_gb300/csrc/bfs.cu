@@ -18,6 +18,13 @@
 // atomicOr on the visited bitmap (a plain load filters visited targets first)
 // and enters the next frontier bitmap.
 //
+// Direction switch: a large frontier (>= n/64 nodes) is measured by a first
+// pass that queues its long rows' chunks and sums its rows' slots. If those
+// rows span >= size / dense_div slots the level instead sweeps the whole slot
+// array once, coalesced (a PMA of out-edges has no in-edges to pull from; the
+// sweep reads each key's source row from its high word and tests it against
+// the frontier bitmap). Both give the same levels.
+//
 #include "gpma_internal.cuh"
 
 #include <algorithm>
@@ -34,6 +41,7 @@ enum : uint32_t {
     CTL_LEVELS = 7,
     CTL_REACHED = 8,
     CTL_BAR = 10,     // GridBarrier (2 words)
+    CTL_SLOTS = 12,   // 3 rotating counters: slots of the current frontier's rows (measured levels)
     CTL_WORDS = 16,
     // profiling record after the control words: u64 start stamp of each level
     // (and of the final check), then u32 per level: frontier size | dense << 31
@@ -47,7 +55,11 @@ enum : uint32_t {
 // ordered by degree, one word can otherwise hold 32 heavy rows.)
 constexpr uint32_t BIG_ROW = 32;
 constexpr uint32_t CHUNK_SLOTS = 64;
-constexpr uint32_t BFS_CHUNK_CAP = 1u << 20;
+// Chunk list entries for an array of `size` slots: rows over BIG_ROW slots
+// yield at most len/64 + 1 chunks each and there are at most size/33 of them,
+// so one level queues fewer than size/64 + size/33 < size/16 chunks; the list
+// never overflows.
+inline uint32_t bfs_chunk_need(uint32_t size) { return size / 16 + 1024; }
 
 struct BfsArgs {
     const uint64_t *keys;
@@ -62,7 +74,7 @@ struct BfsArgs {
     uint2 *chunks;     // [slot begin, slot end) of big-row chunks
     uint32_t chunk_cap;
     uint32_t *ctl;
-    uint32_t dense_div;  // a level whose frontier holds >= n / dense_div nodes sweeps every slot (0: never)
+    uint32_t dense_div;  // a level whose frontier rows span >= size / dense_div slots sweeps every slot (0: never)
     unsigned long long *stamps;  // per-level profile (CTL_PROFILE_LEVELS stamps + info words) or null
 };
 
@@ -155,6 +167,89 @@ __device__ __forceinline__ uint32_t lb_slot(uint32_t p, uint32_t total, uint32_t
     return p < total ? rb + (p - rex) : SIZE_NONE;
 }
 
+// One pass over the frontier words, a word per warp at a time (lane l owns
+// node 32*word + l); `slots` accumulates the slots of every frontier row.
+//   QUEUE: rows over BIG_ROW slots are cut into CHUNK_SLOTS chunks for the
+//          whole grid (a full list leaves them to this pass);
+//   WALK:  the remaining rows are walked as one concatenated slot range, 64
+//          slots per step (without QUEUE, rows over BIG_ROW slots are left to
+//          the chunks an earlier pass queued);
+//   CLEAR: each word is zeroed once read, for its reuse two levels later.
+// Returns the nodes this lane claimed.
+template <bool QUEUE, bool WALK, bool CLEAR>
+__device__ __forceinline__ uint32_t frontier_pass(const BfsArgs &A, uint32_t *front_cur, uint32_t *front_next,
+                                                  uint32_t *chunk_cnt, uint32_t next_level, uint32_t words,
+                                                  uint32_t gwarp, uint32_t nwarps, uint32_t lane, uint32_t &slots) {
+    uint32_t fresh = 0;
+    for (uint32_t wi = gwarp; wi < words; wi += nwarps) {
+        const uint32_t f = front_cur[wi];
+        if (f == 0)
+            continue;
+        if (CLEAR && lane == 0)
+            front_cur[wi] = 0;
+        uint32_t b = 0, e = 0, len = 0;
+        if (f & (1u << lane)) {
+            const uint32_t u = (wi << 5) + lane;
+            b = A.ro[u];
+            e = min(A.ro[u + 1], A.size);
+            len = e > b ? e - b : 0;
+        }
+        slots += len;
+        bool overflow = false;
+        if (QUEUE) {
+            const uint32_t nch = len > BIG_ROW ? (len + CHUNK_SLOTS - 1) / CHUNK_SLOTS : 0;
+            const uint32_t ch_incl = warp_incl_scan(nch);
+            const uint32_t ch_total = __shfl_sync(0xFFFFFFFFu, ch_incl, 31);
+            if (ch_total) {
+                uint32_t base = 0;
+                if (lane == 0)
+                    base = atomicAdd(chunk_cnt, ch_total);
+                base = __shfl_sync(0xFFFFFFFFu, base, 0);
+                if (base + ch_total <= A.chunk_cap) {
+                    const uint32_t pos = base + ch_incl - nch;
+                    for (uint32_t c = 0; c < nch; ++c)
+                        A.chunks[pos + c] = make_uint2(b + c * CHUNK_SLOTS, min(e, b + (c + 1) * CHUNK_SLOTS));
+                } else {
+                    // list full: neutralise the claimed entries, walk the rows here
+                    for (uint32_t c = base + lane; c < min(base + ch_total, A.chunk_cap); c += 32)
+                        A.chunks[c] = make_uint2(0, 0);
+                    overflow = true;
+                }
+            }
+        }
+        if (!overflow && len > BIG_ROW)
+            len = 0;  // its chunks are (or were) queued
+        if (!WALK && !overflow)
+            len = 0;  // short rows wait for the walking pass
+        const uint32_t incl = warp_incl_scan(len);
+        const uint32_t excl = incl - len;
+        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        for (uint32_t p0 = 0; p0 < total; p0 += 64) {
+            const uint32_t sa = lb_slot(p0 + lane, total, b, excl);
+            const uint32_t sb = lb_slot(p0 + 32 + lane, total, b, excl);
+            fresh += visit_pair(A, sa, sb, next_level, front_next);
+        }
+    }
+    return fresh;
+}
+
+// Nodes first reached at level i: one atomic per warp into the counter the
+// next level reads. Returns the warp's total (every lane; lane 0 adds it to
+// the reached count at the end).
+__device__ __forceinline__ uint32_t level_count(const BfsArgs &A, uint32_t i, uint32_t fresh, uint32_t lane) {
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1)
+        fresh += __shfl_xor_sync(0xFFFFFFFFu, fresh, d);
+    if (lane == 0 && fresh)
+        atomicAdd(A.ctl + CTL_CNT + (i + 1) % 3, fresh);
+    return fresh;
+}
+
+// A level whose frontier holds fewer than n / DENSE_GATE nodes is walked
+// without measuring its rows first (it cannot span a large share of slots
+// often enough to pay for the extra pass).
+constexpr uint32_t DENSE_GATE = 64;
+
 __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
     GridBarrier *bar = reinterpret_cast<GridBarrier *>(A.ctl + CTL_BAR);
     uint32_t *err = A.ctl + CTL_ERR;
@@ -172,20 +267,36 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
             break;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             A.ctl[CTL_CNT + (i + 2) % 3] = 0;
+            A.ctl[CTL_SLOTS + (i + 1) % 3] = 0;
             A.ctl[CTL_CHUNKS + (i + 1) % 3] = 0;
         }
         uint32_t *front_cur = (i & 1) ? A.front1 : A.front0;
         uint32_t *front_next = (i & 1) ? A.front0 : A.front1;
         uint32_t *chunk_cnt = A.ctl + CTL_CHUNKS + i % 3;
         const uint32_t next_level = i + 2;
-        uint32_t fresh = 0;
-        // Dense level (the frontier holds >= n / dense_div nodes): every slot
-        // in one coalesced sweep, 8 slots per thread per step; then, after a
-        // barrier, the frontier is cleared for its reuse two levels later.
-        const bool dense = A.dense_div && (uint64_t)frontier * A.dense_div >= A.n;
+        uint32_t fresh = 0, slots = 0;
+        // A large frontier is measured first: one pass queues its long rows'
+        // chunks and sums its rows' slots; then the level either sweeps every
+        // slot (rows spanning >= size / dense_div slots) or walks the rest.
+        const bool probe = A.dense_div && (uint64_t)frontier * DENSE_GATE >= A.n;
+        bool dense = false;
+        if (probe) {
+            fresh += frontier_pass<true, false, false>(A, front_cur, front_next, chunk_cnt, next_level, words, gwarp,
+                                                       nwarps, lane, slots);
+#pragma unroll
+            for (int d = 16; d >= 1; d >>= 1)
+                slots += __shfl_xor_sync(0xFFFFFFFFu, slots, d);
+            if (lane == 0 && slots)
+                atomicAdd(A.ctl + CTL_SLOTS + i % 3, slots);
+            if (!grid_barrier(bar, err))
+                return;
+            dense = (uint64_t)cta_broadcast_read(A.ctl + CTL_SLOTS + i % 3) * A.dense_div >= A.size;
+        }
         if (A.stamps && blockIdx.x == 0 && threadIdx.x == 0 && i < CTL_PROFILE_LEVELS)
             reinterpret_cast<uint32_t *>(A.stamps + CTL_PROFILE_LEVELS)[i] = frontier | (dense ? 1u << 31 : 0u);
         if (dense) {
+            // every slot in one coalesced sweep, 8 slots per thread per step;
+            // then, after a barrier, the frontier is cleared
             const uint32_t gtid = blockIdx.x * BLOCK + threadIdx.x;
             const uint32_t nthreads = gridDim.x * BLOCK;
             const ulonglong2 *kv = reinterpret_cast<const ulonglong2 *>(A.keys);
@@ -205,63 +316,21 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
                 return;
             for (uint32_t w = gtid; w < words; w += nthreads)
                 front_cur[w] = 0;
-#pragma unroll
-            for (int d = 16; d >= 1; d >>= 1)
-                fresh += __shfl_xor_sync(0xFFFFFFFFu, fresh, d);
-            if (lane == 0 && fresh)
-                atomicAdd(A.ctl + CTL_CNT + (i + 1) % 3, fresh);
-            added += fresh;
+            added += level_count(A, i, fresh, lane);
             if (!grid_barrier(bar, err))
                 return;
             continue;
         }
-        // Phase 1: each warp takes one frontier word at a time, lane l owning
-        // node 32*word + l. Short rows are walked as one concatenated slot
-        // range, 64 slots per step; long rows are queued as chunks.
-        for (uint32_t wi = gwarp; wi < words; wi += nwarps) {
-            const uint32_t f = front_cur[wi];
-            if (f == 0)
-                continue;
-            if (lane == 0)
-                front_cur[wi] = 0;  // cleared for its reuse two levels later
-            uint32_t b = 0, e = 0, len = 0;
-            if (f & (1u << lane)) {
-                const uint32_t u = (wi << 5) + lane;
-                b = A.ro[u];
-                e = min(A.ro[u + 1], A.size);
-                len = e > b ? e - b : 0;
-            }
-            uint32_t nch = len > BIG_ROW ? (len + CHUNK_SLOTS - 1) / CHUNK_SLOTS : 0;
-            const uint32_t ch_incl = warp_incl_scan(nch);
-            const uint32_t ch_total = __shfl_sync(0xFFFFFFFFu, ch_incl, 31);
-            if (ch_total) {
-                uint32_t base = 0;
-                if (lane == 0)
-                    base = atomicAdd(chunk_cnt, ch_total);
-                base = __shfl_sync(0xFFFFFFFFu, base, 0);
-                if (base + ch_total <= A.chunk_cap) {
-                    const uint32_t pos = base + ch_incl - nch;
-                    for (uint32_t c = 0; c < nch; ++c)
-                        A.chunks[pos + c] = make_uint2(b + c * CHUNK_SLOTS, min(e, b + (c + 1) * CHUNK_SLOTS));
-                    if (nch)
-                        len = 0;
-                } else {
-                    // list full: neutralise the claimed entries, walk the rows here
-                    for (uint32_t c = base + lane; c < min(base + ch_total, A.chunk_cap); c += 32)
-                        A.chunks[c] = make_uint2(0, 0);
-                }
-            }
-            const uint32_t incl = warp_incl_scan(len);
-            const uint32_t excl = incl - len;
-            const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-            for (uint32_t p0 = 0; p0 < total; p0 += 64) {
-                const uint32_t sa = lb_slot(p0 + lane, total, b, excl);
-                const uint32_t sb = lb_slot(p0 + 32 + lane, total, b, excl);
-                fresh += visit_pair(A, sa, sb, next_level, front_next);
-            }
+        if (probe) {
+            // the short rows now; the long rows' chunks, queued by the first pass, below
+            fresh += frontier_pass<false, true, true>(A, front_cur, front_next, chunk_cnt, next_level, words, gwarp,
+                                                      nwarps, lane, slots);
+        } else {
+            fresh += frontier_pass<true, true, true>(A, front_cur, front_next, chunk_cnt, next_level, words, gwarp,
+                                                     nwarps, lane, slots);
+            if (!grid_barrier(bar, err))
+                return;
         }
-        if (!grid_barrier(bar, err))
-            return;
         // Phase 2: long-row chunks, one warp per chunk (64 slots = one step).
         const uint32_t nch_all = min(cta_broadcast_read(chunk_cnt), A.chunk_cap);
         for (uint32_t c = gwarp; c < nch_all; c += nwarps) {
@@ -272,13 +341,7 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
                 fresh += visit_pair(A, sa, sb, next_level, front_next);
             }
         }
-        // nodes first reached this level: one atomic per warp
-#pragma unroll
-        for (int d = 16; d >= 1; d >>= 1)
-            fresh += __shfl_xor_sync(0xFFFFFFFFu, fresh, d);
-        if (lane == 0 && fresh)
-            atomicAdd(A.ctl + CTL_CNT + (i + 1) % 3, fresh);
-        added += fresh;
+        added += level_count(A, i, fresh, lane);
         if (!grid_barrier(bar, err))
             return;
     }
@@ -295,6 +358,9 @@ __global__ void bfs_init_kernel(uint32_t *levels, uint32_t *visited, uint32_t *f
     ctl[CTL_CNT + 0] = 1;
     ctl[CTL_CNT + 1] = 0;
     ctl[CTL_CNT + 2] = 0;
+    ctl[CTL_SLOTS + 0] = 0;
+    ctl[CTL_SLOTS + 1] = 0;
+    ctl[CTL_SLOTS + 2] = 0;
     ctl[CTL_REACHED] = 1;
 }
 
@@ -307,7 +373,6 @@ gpma_status ensure_bfs(gpma_graph *g) {
     GPMA_TRY(dev_alloc(&g->bfs_visited, n / 32 + 2));
     GPMA_TRY(dev_alloc(&g->bfs_front[0], n / 32 + 2));
     GPMA_TRY(dev_alloc(&g->bfs_front[1], n / 32 + 2));
-    GPMA_TRY(dev_alloc(&g->bfs_chunks, BFS_CHUNK_CAP));
     GPMA_TRY(dev_alloc(&g->bfs_ctl, CTL_WORDS + CTL_PROFILE_WORDS));
     if (!g->h_bfs_ctl) {
         cudaError_t e = cudaMallocHost((void **)&g->h_bfs_ctl, sizeof(uint32_t) * (CTL_WORDS + CTL_PROFILE_WORDS));
@@ -335,6 +400,7 @@ void free_bfs(gpma_graph *g) {
     dev_free(g->bfs_front[0]);
     dev_free(g->bfs_front[1]);
     dev_free(g->bfs_chunks);
+    g->bfs_chunk_cap = 0;
     dev_free(g->bfs_ctl);
     g->bfs_cap = 0;
 }
@@ -342,6 +408,12 @@ void free_bfs(gpma_graph *g) {
 // Levels land in g->bfs_levels; *reached is the count of reached nodes.
 gpma_status bfs_run(gpma_graph *g, uint32_t src, cudaStream_t s, uint64_t *reached) {
     GPMA_TRY(ensure_bfs(g));
+    if (bfs_chunk_need(g->geo.size) > g->bfs_chunk_cap) {
+        dev_free(g->bfs_chunks);
+        g->bfs_chunk_cap = 0;
+        GPMA_TRY(dev_alloc(&g->bfs_chunks, bfs_chunk_need(g->geo.size)));
+        g->bfs_chunk_cap = bfs_chunk_need(g->geo.size);
+    }
     const uint32_t n = g->row_num;
     GPMA_CUDA(cudaMemsetAsync(g->bfs_levels, 0, sizeof(uint32_t) * n, s));
     GPMA_CUDA(cudaMemsetAsync(g->bfs_visited, 0, sizeof(uint32_t) * (n / 32 + 2), s));
@@ -361,7 +433,7 @@ gpma_status bfs_run(gpma_graph *g, uint32_t src, cudaStream_t s, uint64_t *reach
     A.front0 = g->bfs_front[0];
     A.front1 = g->bfs_front[1];
     A.chunks = g->bfs_chunks;
-    A.chunk_cap = BFS_CHUNK_CAP;
+    A.chunk_cap = g->bfs_chunk_cap;
     A.ctl = g->bfs_ctl;
     A.dense_div = g_tuning.bfs_dense_div;
     A.stamps = g->profiling ? reinterpret_cast<unsigned long long *>(g->bfs_ctl + CTL_WORDS) : nullptr;

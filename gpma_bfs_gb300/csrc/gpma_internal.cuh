@@ -169,6 +169,7 @@ struct gpma_graph {
     uint32_t *bfs_visited = nullptr;   // row_num/32 + 2 words
     uint32_t *bfs_front[2] = {nullptr, nullptr};  // frontier bitmaps, row_num/32 + 2 words
     uint2 *bfs_chunks = nullptr;       // big-row chunk list
+    uint32_t bfs_chunk_cap = 0;        // its entries: size / 16 + 1024, more than one level can queue
     uint32_t *bfs_levels = nullptr;
     uint32_t *bfs_ctl = nullptr;       // counters + status
     uint32_t *h_bfs_ctl = nullptr;     // pinned
@@ -201,6 +202,7 @@ struct gpma_batch {
     void *ms_gdesc = nullptr;          // BFS graph table
     uint64_t *ms_reached = nullptr;    // graphs * 64
     uint2 *ms_chunks = nullptr;
+    uint64_t ms_chunk_cap = 0;         // entries (uint4): total slots / 32 + 1024
     uint32_t ms_gcap = 0;
     uint64_t last_traversed = 0;       // edges scanned by the last multi-source BFS, all lanes
     uint64_t *gather_tab = nullptr;    // packed-update staging table (2 * graphs + 1)

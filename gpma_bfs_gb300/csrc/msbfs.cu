@@ -33,13 +33,16 @@ enum : uint32_t {
     MS_ERR = 6,
     MS_LEVELS = 7,
     MS_BAR = 10,    // GridBarrier (2 words)
-    MS_FRONT = 12,  // 3 rotating counters: nodes in the next union frontier
-    MS_CTL_WORDS = 16,
+    MS_FSLOTS = 16, // 3 rotating u64 counters (words 16..21): slots of the rows in the next union frontier
+    MS_CTL_WORDS = 24,
 };
 
 constexpr uint32_t MS_BIG_ROW = 64;
 constexpr uint32_t MS_CHUNK_SLOTS = 128;
-constexpr uint32_t MS_CHUNK_CAP = 1u << 20;
+// Chunk list entries for `slots` slots over all graphs: rows over MS_BIG_ROW
+// slots yield at most len/128 + 1 chunks each, at most slots/65 such rows, so
+// a level queues fewer than slots/128 + slots/65 < slots/32 chunks.
+inline uint64_t ms_chunk_need(uint64_t slots) { return slots / 32 + 1024; }
 
 struct MsGraph {
     const uint64_t *keys;
@@ -63,7 +66,7 @@ struct MsArgs {
     uint32_t *ctl;
     unsigned long long *reached;  // G * 64
     unsigned long long *traversed;
-    uint32_t dense_div;    // a level whose union frontier holds >= N / dense_div nodes sweeps every slot (0: never)
+    uint32_t dense_div;    // a level whose union frontier's rows span >= slots / dense_div slots sweeps every slot (0: never)
 };
 
 __device__ __forceinline__ uint32_t graph_of_node(const MsArgs &A, uint32_t u) {
@@ -124,6 +127,15 @@ __device__ __forceinline__ uint32_t graph_of_slot(const MsArgs &A, uint64_t t) {
     return lo;
 }
 
+__device__ __forceinline__ unsigned long long *fslots(const MsArgs &A, uint32_t level) {
+    return reinterpret_cast<unsigned long long *>(A.ctl + MS_FSLOTS) + level % 3;
+}
+
+__device__ __forceinline__ uint32_t ms_row_slots(const MsGraph &Gr, uint32_t v) {
+    const uint32_t b = Gr.ro[v], e = min(Gr.ro[v + 1], Gr.size);
+    return e > b ? e - b : 0u;
+}
+
 __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
     GridBarrier *bar = reinterpret_cast<GridBarrier *>(A.ctl + MS_BAR);
     uint32_t *err = A.ctl + MS_ERR;
@@ -143,6 +155,7 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
         const uint32_t s = A.src[t];
         atomicOr((unsigned long long *)&A.visited[A.voff[g] + s], 1ull << j);
         atomicOr((unsigned long long *)&A.frontier[A.voff[g] + s], 1ull << j);
+        atomicAdd(fslots(A, 1), (unsigned long long)ms_row_slots(Gr, s));
         if (Gr.levels)
             Gr.levels[(size_t)j * Gr.n + s] = 1;
     }
@@ -153,11 +166,15 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             A.ctl[MS_CHANGE + (level + 1) % 3] = 0;
             A.ctl[MS_CHUNKS + (level + 1) % 3] = 0;
-            A.ctl[MS_FRONT + (level + 2) % 3] = 0;
+            *fslots(A, level + 2) = 0;
         }
         uint32_t *chunk_cnt = A.ctl + MS_CHUNKS + level % 3;
-        const uint32_t fcount = cta_broadcast_read(A.ctl + MS_FRONT + level % 3);
-        const bool dense = A.dense_div && (uint64_t)fcount * A.dense_div >= N;
+        __shared__ unsigned long long s_fs;
+        __syncthreads();
+        if (threadIdx.x == 0)
+            s_fs = *reinterpret_cast<volatile unsigned long long *>(fslots(A, level));
+        __syncthreads();
+        const bool dense = A.dense_div && s_fs * A.dense_div >= A.soff[A.G];
         // expand, dense: every slot of every graph, 4 per thread per step; the
         // frontier masks stay in place until the commit clears them
         const uint64_t quads = dense ? A.soff[A.G] >> 2 : 0;
@@ -247,7 +264,8 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
         if (!grid_barrier(bar, err))
             return;
         // commit
-        uint32_t changed = 0, fnext = 0;
+        uint32_t changed = 0;
+        unsigned long long fnext = 0;
         for (uint32_t w = gtid; w < N; w += nthreads) {
             const uint64_t nxt = A.next[w];
             const uint64_t vis = A.visited[w];
@@ -260,9 +278,9 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
                 A.frontier[w] = nx;
                 A.visited[w] = vis | nx;
                 changed = 1;
-                ++fnext;
                 const uint32_t g = graph_of_node(A, w);
                 const MsGraph &Gr = A.gr[g];
+                fnext += ms_row_slots(Gr, w - A.voff[g]);
                 if (Gr.levels) {
                     const uint32_t lw = w - A.voff[g];
                     uint64_t m = nx;
@@ -280,7 +298,7 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
         for (int d = 16; d >= 1; d >>= 1)
             fnext += __shfl_xor_sync(0xFFFFFFFFu, fnext, d);
         if (lane == 0 && fnext)
-            atomicAdd(A.ctl + MS_FRONT + (level + 1) % 3, fnext);
+            atomicAdd(fslots(A, level + 1), fnext);
         if (!grid_barrier(bar, err))
             return;
         if (cta_broadcast_read(A.ctl + MS_CHANGE + level % 3) == 0)
@@ -349,6 +367,7 @@ void free_batch_bfs(gpma_batch *b) {
     dev_free(b->ms_gdesc);
     dev_free(b->ms_reached);
     dev_free(b->ms_chunks);
+    b->ms_chunk_cap = 0;
     if (b->h_ms_ctl)
         cudaFreeHost(b->h_ms_ctl);
     b->h_ms_ctl = nullptr;
@@ -398,9 +417,17 @@ gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32
         GPMA_TRY(dev_alloc(&b->ms_reached, 64ull * k + 1));
         b->ms_gcap = k;
     }
+    uint64_t slots = 0;
+    for (uint32_t i = 0; i < k; ++i)
+        slots += graphs[i]->geo.size;
+    if (ms_chunk_need(slots) > b->ms_chunk_cap) {
+        dev_free(b->ms_chunks);
+        b->ms_chunk_cap = 0;
+        GPMA_TRY(dev_alloc(&b->ms_chunks, 2 * ms_chunk_need(slots)));  // uint4 = 2 x uint2
+        b->ms_chunk_cap = ms_chunk_need(slots);
+    }
     if (!b->ms_ctl) {
         GPMA_TRY(dev_alloc(&b->ms_ctl, MS_CTL_WORDS));
-        GPMA_TRY(dev_alloc(&b->ms_chunks, MS_CHUNK_CAP * 2));  // uint4 = 2 x uint2
         cudaError_t e = cudaMallocHost((void **)&b->h_ms_ctl, sizeof(uint32_t) * MS_CTL_WORDS);
         if (e != cudaSuccess)
             return cuda_fail(e, "cudaMallocHost(ms ctl)");
@@ -458,7 +485,7 @@ gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32
         A.frontier = b->ms_mask[1];
         A.next = b->ms_mask[2];
         A.chunks = reinterpret_cast<uint4 *>(b->ms_chunks);
-        A.chunk_cap = MS_CHUNK_CAP;
+        A.chunk_cap = (uint32_t)std::min<uint64_t>(b->ms_chunk_cap, 0xFFFFFFFFull);
         A.ctl = b->ms_ctl;
         A.reached = reinterpret_cast<unsigned long long *>(b->ms_reached);
         A.traversed = reinterpret_cast<unsigned long long *>(b->ms_reached) + 64ull * k;

@@ -323,10 +323,11 @@ GPMA_API gpma_status gpma_bfs_level_profile(const gpma_graph *g, double *ms, uin
  * they change speed, never results (the PMA geometry itself is fixed by the
  * reference's sizing rules). Process-wide; takes effect at the next call. */
 typedef struct gpma_tuning {
-    uint32_t bfs_dense_div;        /* single-source BFS: a level whose frontier holds >= row_num / bfs_dense_div
-                                      nodes sweeps the whole slot array instead of walking rows (0: never) */
+    uint32_t bfs_dense_div;        /* single-source BFS: a level whose frontier's rows span >= size / bfs_dense_div
+                                      slots sweeps the whole slot array instead of walking rows (0: never) */
     uint32_t bfs_blocks_per_sm;    /* BFS grid: CTAs per SM (capped by occupancy; 0: as many as fit) */
-    uint32_t ms_dense_div;         /* multi-source BFS: the same switch on the union frontier of all lanes */
+    uint32_t ms_dense_div;         /* multi-source BFS: the same switch on the union frontier of all lanes,
+                                      against the slots of all graphs of the call */
     uint32_t ms_blocks_per_sm;     /* multi-source BFS grid */
     uint32_t update_blocks_per_sm; /* persistent update kernel grid (0: as many as fit) */
     uint32_t reserved[3];
