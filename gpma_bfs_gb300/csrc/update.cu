@@ -116,37 +116,95 @@ __device__ __forceinline__ uint32_t graph_of(const UpdateArgs &A, uint32_t i) {
 // their order are the reference's bit-by-bit descent (gpma.cuh:209-216).
 constexpr uint32_t LOCATE_CACHE = 4096;
 
-__device__ __forceinline__ uint32_t locate_one(const GraphDesc &D, uint64_t key, uint8_t value, const uint64_t *fk,
-                                               uint32_t log2stride) {
-    const uint32_t seg = D.seg;
-    uint32_t prefix = 0;
-    uint32_t bit = (seg << D.height) >> 1;
-    if (fk) {
-        const uint32_t stride = 1u << log2stride;
-        while (stride <= bit) {
-            if (fk[(prefix | bit) >> log2stride] <= key)
-                prefix |= bit;
-            bit >>= 1;
+// The leaf's first slot equal to `key` (handle_del_mod scans all seg slots),
+// or SIZE_NONE. All seg/2 16-byte loads are issued before any comparison.
+__device__ __forceinline__ uint32_t leaf_find(const GraphDesc &D, uint32_t leaf, uint64_t key) {
+    const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(D.keys + leaf);
+    const uint32_t halves = D.seg >> 1;  // 1..16
+    ulonglong2 q[16];
+#pragma unroll
+    for (uint32_t j = 0; j < 16; ++j)
+        if (j < halves)
+            q[j] = p[j];
+    uint32_t hit = SIZE_NONE;
+#pragma unroll
+    for (int j = 15; j >= 0; --j) {
+        if ((uint32_t)j < halves) {
+            if (q[j].y == key)
+                hit = 2 * j + 1;
+            if (q[j].x == key)
+                hit = 2 * j;
         }
     }
-    while (seg <= bit) {
-        if (D.keys[prefix | bit] <= key)
-            prefix |= bit;
-        bit >>= 1;
+    return hit;
+}
+
+// Locates LOC_ILP updates per thread together: at each level of the descent
+// every key's probe is issued before any comparison, so a thread keeps
+// LOC_ILP dependent chains in flight instead of one.
+constexpr int LOC_ILP = 4;
+
+__device__ __forceinline__ void locate_keys(const UpdateArgs &A, const uint64_t *bk, const uint8_t *bv,
+                                            uint32_t i0, uint32_t stride, const uint64_t *fk, uint32_t log2stride) {
+    uint32_t idx[LOC_ILP], prefix[LOC_ILP], bit[LOC_ILP], g[LOC_ILP];
+    uint64_t key[LOC_ILP];
+#pragma unroll
+    for (int j = 0; j < LOC_ILP; ++j) {
+        idx[j] = i0 + j * stride;
+        prefix[j] = 0;
+        bit[j] = 0;
+        g[j] = 0;
+        key[j] = 0;
+        if (idx[j] < A.n) {
+            g[j] = graph_of(A, idx[j]);
+            const GraphDesc &D = A.gd[g[j]];
+            key[j] = bk[idx[j]];
+            bit[j] = (D.seg << D.height) >> 1;
+            if (fk) {  // one graph: the top levels from shared memory
+                const uint32_t sstride = 1u << log2stride;
+                while (sstride <= bit[j]) {
+                    if (fk[(prefix[j] | bit[j]) >> log2stride] <= key[j])
+                        prefix[j] |= bit[j];
+                    bit[j] >>= 1;
+                }
+            }
+        }
     }
-    uint32_t leaf = value == 0 ? SIZE_NONE : prefix;
-    // first equal key of the leaf (handle_del_mod scans all seg slots)
-    const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(D.keys + prefix);
-    for (uint32_t j = 0; j < (seg >> 1); ++j) {
-        ulonglong2 q = p[j];
-        uint32_t hit = q.x == key ? 2 * j : (q.y == key ? 2 * j + 1 : SIZE_NONE);
-        if (hit != SIZE_NONE) {
-            D.vals[prefix + hit] = value;
-            leaf = SIZE_NONE;
+    // the remaining levels of the reference's descent (gpma.cuh:209-216), interleaved
+    for (;;) {
+        uint64_t probe[LOC_ILP];
+        bool any = false;
+#pragma unroll
+        for (int j = 0; j < LOC_ILP; ++j) {
+            const bool live = idx[j] < A.n && A.gd[g[j]].seg <= bit[j];
+            probe[j] = live ? A.gd[g[j]].keys[prefix[j] | bit[j]] : 0;
+            any |= live;
+        }
+        if (!any)
             break;
+#pragma unroll
+        for (int j = 0; j < LOC_ILP; ++j) {
+            if (idx[j] < A.n && A.gd[g[j]].seg <= bit[j]) {
+                if (probe[j] <= key[j])
+                    prefix[j] |= bit[j];
+                bit[j] >>= 1;
+            }
         }
     }
-    return leaf;
+#pragma unroll
+    for (int j = 0; j < LOC_ILP; ++j) {
+        if (idx[j] >= A.n)
+            continue;
+        const GraphDesc &D = A.gd[g[j]];
+        const uint8_t value = bv[idx[j]];
+        uint32_t leaf = value == 0 ? SIZE_NONE : prefix[j];
+        const uint32_t hit = leaf_find(D, prefix[j], key[j]);
+        if (hit != SIZE_NONE) {
+            D.vals[prefix[j] + hit] = value;  // delete / modify / revive in place
+            leaf = SIZE_NONE;
+        }
+        A.leaf[idx[j]] = leaf;
+    }
 }
 
 // ---- grid-wide exclusive scan helpers ------------------------------------
@@ -694,8 +752,9 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
             __syncthreads();
             fk = f;
         }
-        for (uint32_t i = blockIdx.x * BLOCK + threadIdx.x; i < A.n; i += G * BLOCK)
-            A.leaf[i] = locate_one(A.gd[graph_of(A, i)], bk[i], bv[i], fk, log2stride);
+        const uint32_t stride = G * BLOCK;
+        for (uint32_t i0 = blockIdx.x * BLOCK + threadIdx.x; i0 < A.n; i0 += LOC_ILP * stride)
+            locate_keys(A, bk, bv, i0, stride, fk, log2stride);
         __syncthreads();
     }
     if (!grid_barrier(&st->bar, &st->err))
