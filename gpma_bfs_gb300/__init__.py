@@ -155,6 +155,10 @@ def lib() -> ctypes.CDLL:
         "gpma_edges_to_keys": (st, [P, P, u64, P]),
         "gpma_read_edges_text": (st, [ctypes.c_char_p, ctypes.POINTER(u32), ctypes.POINTER(u64), P, P, u64]),
         "gpma_write_edges_text": (st, [ctypes.c_char_p, u32, P, P, u64]),
+        "gpma_read_edges_bin": (st, [ctypes.c_char_p, ctypes.POINTER(u32), ctypes.POINTER(u64), P, P, u64]),
+        "gpma_write_edges_bin": (st, [ctypes.c_char_p, u32, P, P, u64]),
+        "gpma_save": (st, [P, ctypes.c_char_p, P]),
+        "gpma_load": (st, [ctypes.c_char_p, P, ctypes.POINTER(P)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -453,6 +457,44 @@ def write_edges_text(path: str, n: int, src: np.ndarray, dst: np.ndarray) -> Non
     dst = np.ascontiguousarray(dst, np.uint32)
     _check(lib().gpma_write_edges_text(str(path).encode(), n, src.ctypes.data, dst.ctypes.data, len(src)),
            "gpma_write_edges_text")
+
+
+def write_edges_bin(path: str, n: int, src: np.ndarray, dst: np.ndarray) -> None:
+    src = np.ascontiguousarray(src, np.uint32)
+    dst = np.ascontiguousarray(dst, np.uint32)
+    _check(lib().gpma_write_edges_bin(str(path).encode(), n, src.ctypes.data, dst.ctypes.data, len(src)),
+           "gpma_write_edges_bin")
+
+
+def read_edges_bin(path: str):
+    """(n, src, dst) from a binary edge list."""
+    n = ctypes.c_uint32()
+    m = ctypes.c_uint64()
+    _check(lib().gpma_read_edges_bin(str(path).encode(), ctypes.byref(n), ctypes.byref(m), None, None, 0),
+           "gpma_read_edges_bin")
+    src = np.empty(m.value, np.uint32)
+    dst = np.empty(m.value, np.uint32)
+    _check(lib().gpma_read_edges_bin(str(path).encode(), ctypes.byref(n), ctypes.byref(m), src.ctypes.data,
+                                     dst.ctypes.data, m.value), "gpma_read_edges_bin")
+    return n.value, src, dst
+
+
+def save(gpma: GPMA, path: str, stream=None) -> None:
+    """Snapshot of the whole structure (exact layout) to `path`."""
+    _check(lib().gpma_save(gpma.handle, str(path).encode(), _stream_ptr(stream)), "gpma_save")
+
+
+def load(path: str, stream=None) -> GPMA:
+    """A graph restored from a snapshot, with exactly the saved layout."""
+    h = ctypes.c_void_p()
+    _check(lib().gpma_load(str(path).encode(), _stream_ptr(stream), ctypes.byref(h)), "gpma_load")
+    g = GPMA.__new__(GPMA)
+    g._h = h
+    g._owned = True
+    geo = _Geometry()
+    _check(lib().gpma_get_geometry(h, ctypes.byref(geo)), "gpma_get_geometry")
+    g.row_num = geo.row_num
+    return g
 
 
 def read_edges_text(path: str):

@@ -603,6 +603,186 @@ gpma_status gpma_batch_reset_profile(gpma_batch *b) {
     return GPMA_OK;
 }
 
+// ---- snapshot ------------------------------------------------------------------
+// File: "GPMASNP1", then u32 version (1), row_num, size, segment_length,
+// tree_height, u32 0, u64 payload checksum; payload: keys (size x u64),
+// masked values (size x u8), row_offset ((row_num + 1) x u32). Integers are
+// little-endian, written byte by byte.
+}  // extern "C"
+
+namespace gpma {
+namespace {
+
+const char SNAP_MAGIC[8] = {'G', 'P', 'M', 'A', 'S', 'N', 'P', '1'};
+constexpr size_t SNAP_HEADER = 40;
+
+void put_le(unsigned char *b, uint64_t v, int bytes) {
+    for (int i = 0; i < bytes; ++i)
+        b[i] = (unsigned char)(v >> (8 * i));
+}
+
+uint64_t get_le(const unsigned char *b, int bytes) {
+    uint64_t v = 0;
+    for (int i = 0; i < bytes; ++i)
+        v |= (uint64_t)b[i] << (8 * i);
+    return v;
+}
+
+// 64-bit multiply-xorshift mix over the payload bytes (not cryptographic:
+// it detects truncation and corruption).
+struct SnapHash {
+    uint64_t h = 0x243F6A8885A308D3ull;
+    void add(const unsigned char *p, size_t n) {
+        for (size_t i = 0; i < n; ++i) {
+            h = (h ^ p[i]) * 0x100000001B3ull;
+            h ^= h >> 29;
+        }
+    }
+};
+
+// Host byte order independent serialisation of a u64 / u32 array chunk.
+template <typename T>
+void to_le(const T *a, size_t n, unsigned char *out) {
+    for (size_t i = 0; i < n; ++i)
+        put_le(out + i * sizeof(T), (uint64_t)a[i], (int)sizeof(T));
+}
+
+template <typename T>
+void from_le(const unsigned char *in, size_t n, T *a) {
+    for (size_t i = 0; i < n; ++i)
+        a[i] = (T)get_le(in + i * sizeof(T), (int)sizeof(T));
+}
+
+bool valid_geometry(uint32_t size, uint32_t seg, uint32_t height) {
+    if (size < 4 || (size & (size - 1)) != 0 || size > MAX_SLOTS)
+        return false;
+    // gpma.cuh:921-922
+    const uint32_t want_seg = 1u << (fls32(fls32(size)) - 1);
+    return seg == want_seg && height == fls32(size / seg) - 1;
+}
+
+}  // namespace
+}  // namespace gpma
+
+extern "C" {
+
+gpma_status gpma_save(gpma_graph *g, const char *path, void *stream) {
+    if (!g || !path) {
+        set_error("gpma_save: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    const uint32_t size = g->geo.size;
+    const uint64_t ro_n = (uint64_t)g->row_num + 1;
+    std::vector<uint64_t> keys(size);
+    std::vector<uint8_t> vals(size);
+    std::vector<uint32_t> ro(ro_n);
+    GPMA_TRY(gpma_export_layout(g, keys.data(), vals.data(), ro.data(), stream));
+    std::vector<unsigned char> payload(size * 9ull + ro_n * 4);
+    to_le(keys.data(), size, payload.data());
+    std::memcpy(payload.data() + size * 8ull, vals.data(), size);
+    to_le(ro.data(), ro_n, payload.data() + size * 9ull);
+    SnapHash hash;
+    hash.add(payload.data(), payload.size());
+    unsigned char hdr[SNAP_HEADER];
+    std::memcpy(hdr, SNAP_MAGIC, 8);
+    put_le(hdr + 8, 1, 4);
+    put_le(hdr + 12, g->row_num, 4);
+    put_le(hdr + 16, size, 4);
+    put_le(hdr + 20, g->geo.seg, 4);
+    put_le(hdr + 24, g->geo.height, 4);
+    put_le(hdr + 28, 0, 4);
+    put_le(hdr + 32, hash.h, 8);
+    FILE *f = std::fopen(path, "wb");
+    if (!f) {
+        set_error("gpma_save: cannot open %s", path);
+        return GPMA_ERR_IO;
+    }
+    bool bad = std::fwrite(hdr, 1, SNAP_HEADER, f) != SNAP_HEADER ||
+               std::fwrite(payload.data(), 1, payload.size(), f) != payload.size();
+    bad |= std::fclose(f) != 0;
+    if (bad) {
+        set_error("gpma_save: write to %s failed", path);
+        return GPMA_ERR_IO;
+    }
+    return GPMA_OK;
+}
+
+gpma_status gpma_load(const char *path, void *stream, gpma_graph **out) {
+    if (!path || !out) {
+        set_error("gpma_load: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    *out = nullptr;
+    FILE *f = std::fopen(path, "rb");
+    if (!f) {
+        set_error("gpma_load: cannot open %s", path);
+        return GPMA_ERR_IO;
+    }
+    unsigned char hdr[SNAP_HEADER];
+    if (std::fread(hdr, 1, SNAP_HEADER, f) != SNAP_HEADER || std::memcmp(hdr, SNAP_MAGIC, 8) != 0 ||
+        get_le(hdr + 8, 4) != 1) {
+        std::fclose(f);
+        set_error("gpma_load: %s is not a snapshot of this version", path);
+        return GPMA_ERR_IO;
+    }
+    const uint32_t row_num = (uint32_t)get_le(hdr + 12, 4), size = (uint32_t)get_le(hdr + 16, 4);
+    const uint32_t seg = (uint32_t)get_le(hdr + 20, 4), height = (uint32_t)get_le(hdr + 24, 4);
+    if (!valid_geometry(size, seg, height) || row_num >= 0xFFFFFFFFu) {
+        std::fclose(f);
+        set_error("gpma_load: %s holds an impossible geometry (size %u, segment %u, height %u)", path, size, seg,
+                  height);
+        return GPMA_ERR_IO;
+    }
+    const uint64_t ro_n = (uint64_t)row_num + 1;
+    std::vector<unsigned char> payload(size * 9ull + ro_n * 4);
+    const bool short_read = std::fread(payload.data(), 1, payload.size(), f) != payload.size();
+    const bool trailing = !short_read && std::fgetc(f) != EOF;
+    std::fclose(f);
+    SnapHash hash;
+    if (!short_read)
+        hash.add(payload.data(), payload.size());
+    if (short_read || trailing || hash.h != get_le(hdr + 32, 8)) {
+        set_error("gpma_load: %s is truncated or corrupt", path);
+        return GPMA_ERR_IO;
+    }
+    std::vector<uint64_t> keys(size);
+    std::vector<uint32_t> ro(ro_n);
+    from_le(payload.data(), size, keys.data());
+    from_le(payload.data() + size * 9ull, ro_n, ro.data());
+    gpma_graph *g = new (std::nothrow) gpma_graph();
+    if (!g) {
+        set_error("gpma_load: host allocation failed");
+        return GPMA_ERR_NOMEM;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    gpma_status st = [&]() -> gpma_status {
+        GPMA_CUDA(cudaGetDevice(&g->device));
+        GPMA_CUDA(cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, g->device));
+        g->row_num = row_num;
+        g->cap = size;
+        GPMA_TRY(dev_alloc(&g->keys, size));
+        GPMA_TRY(dev_alloc(&g->values, size));
+        GPMA_TRY(dev_alloc(&g->row_offset, ro_n));
+        GPMA_TRY(ensure_scratch(g, size));
+        g->geo.size = size;
+        g->geo.seg = seg;
+        g->geo.height = height;
+        recalculate_density(g->geo);
+        GPMA_CUDA(cudaMemcpyAsync(g->keys, keys.data(), size * 8ull, cudaMemcpyHostToDevice, s));
+        GPMA_CUDA(cudaMemcpyAsync(g->values, payload.data() + size * 8ull, size, cudaMemcpyHostToDevice, s));
+        GPMA_CUDA(cudaMemcpyAsync(g->row_offset, ro.data(), ro_n * 4, cudaMemcpyHostToDevice, s));
+        GPMA_CUDA(cudaStreamSynchronize(s));
+        return GPMA_OK;
+    }();
+    if (st != GPMA_OK) {
+        release(g);
+        delete g;
+        return st;
+    }
+    *out = g;
+    return GPMA_OK;
+}
+
 gpma_status gpma_get_tuning(gpma_tuning *out) {
     if (!out) {
         set_error("gpma_get_tuning: null argument");

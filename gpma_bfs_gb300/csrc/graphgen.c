@@ -343,3 +343,90 @@ gpma_status gpma_read_edges_text(const char *path, uint32_t *n_out, uint64_t *m_
     fclose(f);
     return GPMA_OK;
 }
+
+/* ---- binary edge list ----------------------------------------------------
+ * "GPMAEDG1", u32 n, u32 reserved (0), u64 m, m x u32 src, m x u32 dst; all
+ * little-endian (written and read byte by byte, so host byte order does not
+ * matter). */
+static const char EDG_MAGIC[8] = {'G', 'P', 'M', 'A', 'E', 'D', 'G', '1'};
+
+static void put_le(unsigned char *b, uint64_t v, int bytes) {
+    for (int i = 0; i < bytes; ++i)
+        b[i] = (unsigned char)(v >> (8 * i));
+}
+
+static uint64_t get_le(const unsigned char *b, int bytes) {
+    uint64_t v = 0;
+    for (int i = 0; i < bytes; ++i)
+        v |= (uint64_t)b[i] << (8 * i);
+    return v;
+}
+
+static int write_u32s(FILE *f, const uint32_t *a, uint64_t m) {
+    unsigned char buf[4096];
+    uint64_t i = 0;
+    while (i < m) {
+        size_t k = 0;
+        for (; k < sizeof(buf) / 4 && i < m; ++k, ++i)
+            put_le(buf + 4 * k, a[i], 4);
+        if (fwrite(buf, 4, k, f) != k)
+            return -1;
+    }
+    return 0;
+}
+
+static int read_u32s(FILE *f, uint32_t *a, uint64_t m) {
+    unsigned char buf[4096];
+    uint64_t i = 0;
+    while (i < m) {
+        size_t want = (m - i) < sizeof(buf) / 4 ? (size_t)(m - i) : sizeof(buf) / 4;
+        if (fread(buf, 4, want, f) != want)
+            return -1;
+        for (size_t k = 0; k < want; ++k)
+            a[i++] = (uint32_t)get_le(buf + 4 * k, 4);
+    }
+    return 0;
+}
+
+gpma_status gpma_write_edges_bin(const char *path, uint32_t n, const uint32_t *src, const uint32_t *dst, uint64_t m) {
+    if (!path || ((!src || !dst) && m))
+        return GPMA_ERR_INVALID;
+    FILE *f = fopen(path, "wb");
+    if (!f)
+        return GPMA_ERR_IO;
+    unsigned char hdr[24];
+    memcpy(hdr, EDG_MAGIC, 8);
+    put_le(hdr + 8, n, 4);
+    put_le(hdr + 12, 0, 4);
+    put_le(hdr + 16, m, 8);
+    int bad = fwrite(hdr, 1, sizeof(hdr), f) != sizeof(hdr) || write_u32s(f, src, m) || write_u32s(f, dst, m);
+    bad |= fclose(f) != 0;
+    return bad ? GPMA_ERR_IO : GPMA_OK;
+}
+
+gpma_status gpma_read_edges_bin(const char *path, uint32_t *n_out, uint64_t *m_out, uint32_t *src, uint32_t *dst,
+                                uint64_t capacity) {
+    if (!path || !n_out || !m_out)
+        return GPMA_ERR_INVALID;
+    FILE *f = fopen(path, "rb");
+    if (!f)
+        return GPMA_ERR_IO;
+    unsigned char hdr[24];
+    if (fread(hdr, 1, sizeof(hdr), f) != sizeof(hdr) || memcmp(hdr, EDG_MAGIC, 8) != 0) {
+        fclose(f);
+        return GPMA_ERR_IO;
+    }
+    *n_out = (uint32_t)get_le(hdr + 8, 4);
+    *m_out = get_le(hdr + 16, 8);
+    if (!src || !dst) { /* header query */
+        fclose(f);
+        return GPMA_OK;
+    }
+    if (capacity < *m_out) {
+        fclose(f);
+        return GPMA_ERR_INVALID;
+    }
+    int bad = read_u32s(f, src, *m_out) || read_u32s(f, dst, *m_out);
+    fclose(f);
+    return bad ? GPMA_ERR_IO : GPMA_OK;
+}

@@ -367,6 +367,25 @@ GPMA_API gpma_status gpma_read_edges_text(const char *path, uint32_t *n_out, uin
                                  uint64_t capacity);
 GPMA_API gpma_status gpma_write_edges_text(const char *path, uint32_t n, const uint32_t *src, const uint32_t *dst, uint64_t m);
 
+/* Binary edge list (no reference counterpart; the text format is slow for
+ * 10^8+ edges): "GPMAEDG1", u32 n, u32 0, u64 m, m u32 sources, m u32
+ * destinations, little-endian. Same header-query convention as the text
+ * reader. */
+GPMA_API gpma_status gpma_write_edges_bin(const char *path, uint32_t n, const uint32_t *src, const uint32_t *dst,
+                                          uint64_t m);
+GPMA_API gpma_status gpma_read_edges_bin(const char *path, uint32_t *n_out, uint64_t *m_out, uint32_t *src,
+                                         uint32_t *dst, uint64_t capacity);
+
+/* ---- snapshot ----------------------------------------------------------------
+ * No reference counterpart. gpma_save writes the whole structure (geometry,
+ * keys, values, row_offset) with a checksum; gpma_load creates a graph on the
+ * current device with exactly that layout, so updates after a resume give
+ * the same layouts as updates without one. A file that is truncated,
+ * corrupt, of another version or with an impossible geometry is rejected
+ * with GPMA_ERR_IO before any device memory is allocated. */
+GPMA_API gpma_status gpma_save(gpma_graph *g, const char *path, void *stream);
+GPMA_API gpma_status gpma_load(const char *path, void *stream, gpma_graph **out);
+
 #ifdef __cplusplus
 }
 #endif
