@@ -158,6 +158,8 @@ def lib() -> ctypes.CDLL:
         "gpma_read_edges_bin": (st, [ctypes.c_char_p, ctypes.POINTER(u32), ctypes.POINTER(u64), P, P, u64]),
         "gpma_write_edges_bin": (st, [ctypes.c_char_p, u32, P, P, u64]),
         "gpma_save": (st, [P, ctypes.c_char_p, P]),
+        "gpma_pagerank": (st, [P, ctypes.c_float, u32, ctypes.c_double, P, ctypes.POINTER(u32), P]),
+        "gpma_components": (st, [P, P, ctypes.POINTER(u64), ctypes.POINTER(u32), P]),
         "gpma_load": (st, [ctypes.c_char_p, P, ctypes.POINTER(P)]),
     }
     for name, (res, args) in sig.items():
@@ -402,6 +404,32 @@ def gpma_bfs_multi(gpma: GPMA, sources, results=None, stream=None):
            "gpma_bfs_multi")
     del keep
     return results, reached
+
+
+def pagerank(gpma: GPMA, damping: float = 0.85, iterations: int = 20, tol: float = 0.0, out=None, stream=None):
+    """(ranks float32[row_num], iterations run). `out` may be a host array or
+    a CUDA tensor of row_num float32."""
+    if out is None:
+        out = np.zeros(gpma.row_num, np.float32)
+    p, keep = _ptr(out)
+    it = ctypes.c_uint32()
+    _check(lib().gpma_pagerank(gpma.handle, float(damping), int(iterations), float(tol), p, ctypes.byref(it),
+                               _stream_ptr(stream)), "gpma_pagerank")
+    del keep
+    return out, it.value
+
+
+def components(gpma: GPMA, out=None, stream=None):
+    """(labels uint32[row_num]: smallest node id of each node's weakly
+    connected component, component count, rounds)."""
+    if out is None:
+        out = np.zeros(gpma.row_num, np.uint32)
+    p, keep = _ptr(out)
+    c, r = ctypes.c_uint64(), ctypes.c_uint32()
+    _check(lib().gpma_components(gpma.handle, p, ctypes.byref(c), ctypes.byref(r), _stream_ptr(stream)),
+           "gpma_components")
+    del keep
+    return out, c.value, r.value
 
 
 TUNING_FIELDS = ("bfs_dense_div", "bfs_blocks_per_sm", "ms_dense_div", "ms_blocks_per_sm", "update_blocks_per_sm")

@@ -68,6 +68,8 @@ void release(gpma_graph *g) {
     dev_free(g->chunk_cnt);
     free_buffers(g->buf);
     free_bfs(g);
+    dev_free(g->an_buf);
+    g->an_cap = 0;
     if (g->own_batch)
         gpma_batch_destroy(g->own_batch);
     g->own_batch = nullptr;

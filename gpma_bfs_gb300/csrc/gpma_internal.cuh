@@ -175,6 +175,8 @@ struct gpma_graph {
     uint32_t *h_bfs_ctl = nullptr;     // pinned
     int bfs_grid = 0;                  // resident BFS-kernel CTAs per SM (0: not yet known)
     gpma_batch *own_batch = nullptr;   // multi-source BFS context of this graph
+    uint32_t *an_buf = nullptr;        // analytics: 4 x row_num words + control words, kept between calls
+    uint32_t an_cap = 0;               // row_num it was sized for
     gpma_stats stats{};
     // profiling: events on the caller's stream around each phase
     bool profiling = false;

@@ -119,6 +119,26 @@ GPMA_API gpma_status gpma_bfs_multi(gpma_graph *g, const uint32_t *srcs, uint32_
 GPMA_API gpma_status gpma_bfs_noalloc(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached,
                                       void *stream);
 
+/* ---- analytics on the same array --------------------------------------------
+ * No reference counterpart (the reference's only analytic is the BFS). Both
+ * sweep every slot of the gapped array once per iteration; an edge is a
+ * slot the BFS would follow.
+ *
+ * PageRank with damping d over the out-edges (dangling nodes spread their
+ * rank evenly): ranks start at 1/row_num; `iterations` iterations at most,
+ * fewer once the L1 change of an iteration drops below tol. ranks (host or
+ * device, row_num floats) receives the result; summation order is not fixed
+ * (float atomics), so results vary in the last bits between runs. */
+GPMA_API gpma_status gpma_pagerank(gpma_graph *g, float damping, uint32_t iterations, double tol, float *ranks,
+                                   uint32_t *iterations_run, void *stream);
+
+/* Weakly connected components: labels (host or device, row_num entries)
+ * receives, for every node, the smallest node id of its component (exact and
+ * deterministic); components (optional) the number of components, isolated
+ * nodes included; rounds (optional) the hook-and-jump rounds run. */
+GPMA_API gpma_status gpma_components(gpma_graph *g, uint32_t *labels, uint64_t *components, uint32_t *rounds,
+                                     void *stream);
+
 /* ---- many graphs per launch -------------------------------------------------
  * No reference counterpart: the reference updates one GPMA per call. A
  * gpma_batch owns the update buffers shared by the graphs of one call. All
