@@ -1063,47 +1063,159 @@ __global__ void __launch_bounds__(BLOCK) chunk_scan_kernel(uint32_t *chunk_cnt, 
         *total = run;
 }
 
-// Stable compaction of live slots into dst (thread t owns a contiguous run).
+// Stable compaction of live slots into dst. Warp w of a chunk takes its 256
+// slots as 8 steps of 32 consecutive slots (coalesced loads); a ballot per
+// step gives each live slot its rank, so the writes are coalesced too.
 __global__ void __launch_bounds__(BLOCK) chunk_compact_kernel(const uint64_t *keys, const uint8_t *vals, uint32_t size,
                                                               const uint32_t *chunk_off, uint64_t *dk, uint8_t *dv) {
-    __shared__ uint32_t tmp[BLOCK / 32 + 1];
-    constexpr uint32_t K = CHUNK / BLOCK;
-    uint32_t chunks = (size + CHUNK - 1) / CHUNK;
+    __shared__ uint32_t s_warp[BLOCK / 32];
+    constexpr uint32_t STEPS = CHUNK / BLOCK;  // 8 steps of 32 slots per warp
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t chunks = (size + CHUNK - 1) / CHUNK;
     for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {
-        uint32_t base = c * CHUNK + threadIdx.x * K;
-        uint32_t cl = 0;
-        for (uint32_t j = 0; j < K; ++j) {
-            uint32_t t = base + j;
-            cl += (t < size && keys[t] != KEY_NONE && vals[t] != 0);
+        const uint32_t base = c * CHUNK + warp * (32 * STEPS);
+        uint64_t k[STEPS];
+        uint8_t v[STEPS];
+        uint32_t mask[STEPS];
+        uint32_t total = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < STEPS; ++j) {
+            const uint32_t t = base + 32 * j + lane;
+            k[j] = t < size ? keys[t] : KEY_NONE;
+            v[j] = t < size ? vals[t] : 0;
+            mask[j] = __ballot_sync(0xFFFFFFFFu, k[j] != KEY_NONE && v[j] != 0);
+            total += __popc(mask[j]);
         }
-        uint32_t tot;
-        uint32_t o = chunk_off[c] + block_excl_scan(cl, &tot, tmp);
-        for (uint32_t j = 0; j < K; ++j) {
-            uint32_t t = base + j;
-            if (t < size && keys[t] != KEY_NONE && vals[t] != 0) {
-                dk[o] = keys[t];
-                dv[o] = vals[t];
-                ++o;
+        if (lane == 0)
+            s_warp[warp] = total;
+        __syncthreads();
+        uint32_t o = chunk_off[c];
+        for (uint32_t w = 0; w < warp; ++w)
+            o += s_warp[w];
+        __syncthreads();
+        const uint32_t lt = lanemask_lt();
+#pragma unroll
+        for (uint32_t j = 0; j < STEPS; ++j) {
+            if ((mask[j] >> lane) & 1u) {
+                const uint32_t pos = o + __popc(mask[j] & lt);
+                dk[pos] = k[j];
+                dv[pos] = v[j];
             }
+            o += __popc(mask[j]);
         }
     }
 }
 
-// Redispatch of the whole array [0, size) from live[0..L) and pend[0..P).
+// Live elements among the first d of the stable merge of live[0..L) and
+// pend[0..P) (ties: live first).
+__device__ __forceinline__ uint32_t merge_split(const uint64_t *lk, uint32_t L, const uint64_t *pk, uint32_t P,
+                                                uint64_t d) {
+    uint32_t lo = d > P ? (uint32_t)(d - P) : 0u, hi = (uint32_t)(d < L ? d : L);
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (pk[d - mid - 1] < lk[mid])
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    return lo;
+}
+
+// First merged element of each CHUNK-slot chunk of the redispatched array
+// (and of its end), split into live and pending parts: split[c] = live
+// elements before chunk c. One search per chunk boundary, all in parallel.
+__global__ void merge_split_kernel(const uint64_t *lk, uint32_t L, const uint64_t *pk, uint32_t P, uint32_t size,
+                                   uint32_t log2seg, uint32_t log2F, uint32_t *split) {
+    const uint64_t M = (uint64_t)L + P;
+    const uint32_t chunks = (size + CHUNK - 1) / CHUNK;
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c <= chunks; c += gridDim.x * blockDim.x) {
+        const uint32_t t0 = (uint32_t)min((uint64_t)c * CHUNK, (uint64_t)size);
+        const uint64_t f = seg_first(t0 >> log2seg, M, log2F);
+        split[c] = merge_split(lk, L, pk, P, f < M ? f : M);
+    }
+}
+
+// Redispatch of the whole array [0, size) from live[0..L) and pend[0..P):
+// chunk c's merged elements come from live[split[c] .. split[c+1]) and the
+// matching pending range; both are staged in shared memory (coalesced) and
+// merged there, then every slot of the chunk is written once, coalesced.
 __global__ void __launch_bounds__(BLOCK) rebuild_kernel(uint64_t *keys, uint8_t *vals, uint32_t *row_offset,
                                                         uint32_t row_num, uint32_t size, uint32_t log2seg,
                                                         uint32_t log2F, const uint64_t *lk, const uint8_t *lv,
                                                         uint32_t L, const uint64_t *pk, const uint8_t *pv, uint32_t P,
-                                                        uint64_t gap_key) {
+                                                        const uint32_t *split, uint64_t gap_key) {
     extern __shared__ __align__(16) unsigned char smem[];
-    uint64_t *mk = reinterpret_cast<uint64_t *>(smem);
-    uint8_t *mv = reinterpret_cast<uint8_t *>(mk + CHUNK);
-    uint32_t chunks = (size + CHUNK - 1) / CHUNK;
+    uint64_t *sk = reinterpret_cast<uint64_t *>(smem);  // staged: live part, then pending part
+    uint64_t *mk = sk + CHUNK;                          // merged
+    uint8_t *sv = reinterpret_cast<uint8_t *>(mk + CHUNK);
+    uint8_t *mv = sv + CHUNK;
+    const uint64_t M = (uint64_t)L + P;
+    const uint32_t seg = 1u << log2seg;
+    const uint32_t chunks = (size + CHUNK - 1) / CHUNK;
     for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {
-        uint32_t t0 = c * CHUNK;
-        uint32_t len = min(CHUNK, size - t0);
-        redispatch_chunk(keys, vals, row_offset, row_num, 0, log2seg, log2F, t0, len, lk, lv, L, pk, pv, P, gap_key,
-                         mk, mv);
+        const uint32_t t0 = c * CHUNK;
+        const uint32_t len = min(CHUNK, size - t0);
+        const uint64_t f_lo = seg_first(t0 >> log2seg, M, log2F), f_hi = seg_first((t0 + len) >> log2seg, M, log2F);
+        const uint32_t i_lo = (uint32_t)(f_lo < M ? f_lo : M), i_hi = (uint32_t)(f_hi < M ? f_hi : M);
+        const uint32_t x0 = split[c], x1 = split[c + 1];
+        const uint32_t y0 = i_lo - x0, y1 = i_hi - x1;
+        const uint32_t nl = x1 - x0, np = y1 - y0;  // nl + np = i_hi - i_lo <= len
+        for (uint32_t k = threadIdx.x; k < nl; k += BLOCK) {
+            sk[k] = lk[x0 + k];
+            sv[k] = lv[x0 + k];
+        }
+        for (uint32_t k = threadIdx.x; k < np; k += BLOCK) {
+            sk[nl + k] = pk[y0 + k];
+            sv[nl + k] = pv[y0 + k];
+        }
+        __syncthreads();
+        const uint32_t cnt = nl + np;
+        const uint32_t ipt = (cnt + BLOCK - 1) / BLOCK;
+        const uint32_t d = threadIdx.x * ipt;
+        if (d < cnt) {
+            uint32_t lo = d > np ? d - np : 0, hi = min(d, nl);
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (sk[nl + (d - mid - 1)] < sk[mid])
+                    hi = mid;
+                else
+                    lo = mid + 1;
+            }
+            uint32_t x = lo, y = d - lo;
+            const uint32_t end = min(cnt, d + ipt);
+            for (uint32_t e = d; e < end; ++e) {
+                const bool take_live = x < nl && (y >= np || sk[x] <= sk[nl + y]);
+                if (take_live) {
+                    mk[e] = sk[x];
+                    mv[e] = sv[x];
+                    ++x;
+                } else {
+                    mk[e] = sk[nl + y];
+                    mv[e] = sv[nl + y];
+                    ++y;
+                }
+            }
+        }
+        __syncthreads();
+        for (uint32_t t = threadIdx.x; t < len; t += BLOCK) {
+            const uint32_t slot = t0 + t;
+            const uint32_t s = slot >> log2seg, ln = slot & (seg - 1);
+            const uint64_t g0 = seg_first(s, M, log2F), g1 = seg_first(s + 1, M, log2F);
+            uint64_t k = gap_key;
+            uint8_t v = 0;
+            if (ln < g1 - g0) {
+                k = mk[g0 + ln - i_lo];
+                v = mv[g0 + ln - i_lo];
+            }
+            keys[slot] = k;
+            vals[slot] = v;
+            if (is_guard(k)) {
+                const uint32_t row = (uint32_t)(k >> 32);
+                if (row < row_num)
+                    row_offset[row + 1] = slot;
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -1177,20 +1289,36 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k
     const uint32_t log2F = fls32(geo.size) - 1 - log2seg;
     const uint32_t out_chunks = (geo.size + CHUNK - 1) / CHUNK;
     const int rgrid = grid_for((uint64_t)out_chunks * BLOCK, g->sms, 4);
-    const size_t rsmem = CHUNK * 9;
+    const size_t rsmem = 2ull * CHUNK * 9;  // staged sources + merged chunk
+    // merge splits at every chunk boundary of the new array: the chunk counts
+    // of the compaction are spent, so their buffer holds them (grown if the
+    // array grew)
+    if (out_chunks + 2 > g->scratch_cap / CHUNK + 2) {
+        dev_free(g->chunk_cnt);
+        GPMA_TRY(dev_alloc(&g->chunk_cnt, (uint64_t)out_chunks + 2));
+    }
+    uint32_t *split = g->chunk_cnt;
+    auto splits = [&]() {
+        merge_split_kernel<<<grid_for((uint64_t)out_chunks + 1, g->sms, 8), BLOCK, 0, s>>>(
+            g->skeys, live, pend_k, pend_n, geo.size, log2seg, log2F, split);
+        g->prof.kernel_launches += 1;
+    };
     if (significant) {
         // significant_insert: everything redispatched, gaps are key 0 / value 0
+        splits();
         rebuild_kernel<<<rgrid, BLOCK, rsmem, s>>>(g->keys, g->values, g->row_offset, g->row_num, geo.size, log2seg,
-                                                    log2F, g->skeys, g->svals, live, pend_k, pend_v, pend_n, 0ull);
+                                                    log2F, g->skeys, g->svals, live, pend_k, pend_v, pend_n, split,
+                                                    0ull);
         g->stats.significant++;
         g->stats.accepted_windows++;
         g->stats.accepted_slots += geo.size;
     } else {
         const uint32_t h = geo.height;
         if (geo.lower[h] <= merge && merge <= geo.upper[h]) {
+            splits();
             rebuild_kernel<<<rgrid, BLOCK, rsmem, s>>>(g->keys, g->values, g->row_offset, g->row_num, geo.size,
                                                         log2seg, log2F, g->skeys, g->svals, live, pend_k, pend_v,
-                                                        pend_n, KEY_NONE);
+                                                        pend_n, split, KEY_NONE);
             g->stats.accepted_windows++;
             g->stats.accepted_slots += geo.size;
         } else {
