@@ -129,23 +129,30 @@ struct BatchBuffers {
     uint64_t sort_status_cap = 0;
     uint32_t *sort_hist = nullptr;     // [graph][8][256] digit counts
     uint32_t hist_cap = 0;             // graphs
-    // per-graph tables
+    // per-graph tables, one upload per launch from pinned memory:
+    // [GraphDesc x gcap][batch offsets x (gcap + 1)][sort tile offsets x (gcap + 1)]
     uint32_t gcap = 0;
-    GraphDesc *gd = nullptr;
-    GraphStatus *gs = nullptr;
-    GraphStatus *h_gs = nullptr;       // pinned
-    uint32_t *boff = nullptr;          // batch offsets, graphs + 1
-    uint32_t *toff = nullptr;          // sort tile offsets, graphs + 1
-    std::vector<GraphDesc> h_gd;
-    std::vector<uint32_t> h_off;       // boff then toff
+    unsigned char *d_tab = nullptr;
+    unsigned char *h_tab = nullptr;    // pinned
+    GraphDesc *gd = nullptr;           // views into d_tab
+    uint32_t *boff = nullptr;
+    uint32_t *toff = nullptr;
+    // status, double-buffered: a slot is [DeviceStatus][GraphStatus x gcap]
+    // (GraphStatus from STAT_GS_OFFSET); each launch zeroes the other slot and
+    // the sort state it used, so steady-state launches need no memsets
+    unsigned char *d_stat = nullptr;   // 2 slots
+    unsigned char *h_stat = nullptr;   // 1 slot, pinned
+    size_t stat_slot = 0;              // bytes per slot
+    int parity = 0;
+    bool dirty = true;                 // sort state / status slots need a host-side clear
     // grid-path chunk counts (sum of window widths / CHUNK)
     uint32_t *chunk_cnt = nullptr;
     uint64_t chunk_cap = 0;
     // persistent-kernel scratch
     uint32_t *cta_cnt = nullptr;       // 4 * grid
-    DeviceStatus *status = nullptr;
-    DeviceStatus *h_status = nullptr;  // pinned
 };
+constexpr size_t STAT_GS_OFFSET = 128;
+static_assert(sizeof(DeviceStatus) <= STAT_GS_OFFSET, "status slot layout");
 
 }  // namespace gpma
 

@@ -96,6 +96,12 @@ struct UpdateArgs {
     uint32_t *chunk_cnt;
     uint32_t *cta_cnt;
     DeviceStatus *st;
+    // clean-up for the next launch: the other status slot (as words) and the
+    // sort state this launch used
+    uint32_t *next_slot;
+    uint32_t next_slot_words;
+    uint32_t hist_words;
+    uint32_t status_words;
 };
 
 // Current window list of a level.
@@ -728,6 +734,7 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
     const uint64_t *bk = sel ? A.bk[1] : A.bk[0];
     const uint8_t *bv = sel ? A.bv[1] : A.bv[0];
     const uint32_t G = gridDim.x;
+
     uint32_t scan_id = 0;
 #define CNT(id) ((id) ? A.cta_cnt + G : A.cta_cnt)
 #define CNTI(id) ((id) ? A.cta_cnt + 3 * G : A.cta_cnt + 2 * G)
@@ -759,6 +766,19 @@ __global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(U
     }
     if (!grid_barrier(&st->bar, &st->err))
         return;
+    {
+        // every CTA is past the sort (trivial-digit mask, passes): zero its
+        // state and the next launch's status slot
+        const uint32_t gt = blockIdx.x * BLOCK + threadIdx.x, nt = G * BLOCK;
+        for (uint32_t i = gt; i < A.hist_words; i += nt)
+            A.sort_hist[i] = 0;
+        for (uint32_t i = gt; i < A.status_words; i += nt)
+            A.sort_status[i] = 0;
+        if (gt < 8)
+            A.sort_tiles[gt] = 0;
+        for (uint32_t i = gt; i < A.next_slot_words; i += nt)
+            A.next_slot[i] = 0;
+    }
     if (stamper)
         st->stamp[2] = globaltimer_ns();
 
@@ -1416,19 +1436,20 @@ void free_buffers(BatchBuffers &b) {
     dev_free(b.sort_tiles);
     dev_free(b.sort_status);
     dev_free(b.sort_hist);
-    dev_free(b.gd);
-    dev_free(b.gs);
-    dev_free(b.boff);
-    dev_free(b.toff);
+    dev_free(b.d_tab);
+    dev_free(b.d_stat);
     dev_free(b.chunk_cnt);
     dev_free(b.cta_cnt);
-    dev_free(b.status);
-    if (b.h_status)
-        cudaFreeHost(b.h_status);
-    if (b.h_gs)
-        cudaFreeHost(b.h_gs);
-    b.h_status = nullptr;
-    b.h_gs = nullptr;
+    if (b.h_tab)
+        cudaFreeHost(b.h_tab);
+    if (b.h_stat)
+        cudaFreeHost(b.h_stat);
+    b.h_tab = nullptr;
+    b.h_stat = nullptr;
+    b.gd = nullptr;
+    b.boff = b.toff = nullptr;
+    b.stat_slot = 0;
+    b.dirty = true;
     b.cap = 0;
     b.gcap = 0;
     b.hist_cap = 0;
@@ -1437,12 +1458,9 @@ void free_buffers(BatchBuffers &b) {
 }
 
 gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
-    if (!b.status) {
-        GPMA_TRY(dev_alloc(&b.status, 1));
+    if (!b.sort_tiles) {
         GPMA_TRY(dev_alloc(&b.sort_tiles, 8));
-        cudaError_t e = cudaMallocHost((void **)&b.h_status, sizeof(DeviceStatus));
-        if (e != cudaSuccess)
-            return cuda_fail(e, "cudaMallocHost(status)");
+        b.dirty = true;
     }
     if (n > b.cap || !b.bkeys[0]) {
         uint64_t cap = std::max<uint64_t>(n, 1024);
@@ -1483,23 +1501,33 @@ gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
         GPMA_TRY(dev_alloc(&b.rvals, cap));
         b.cap = cap;
     }
-    if (graphs > b.gcap || !b.gd) {
-        uint32_t gc = std::max<uint32_t>(graphs, 1);
-        dev_free(b.gd);
-        dev_free(b.gs);
-        dev_free(b.boff);
-        dev_free(b.toff);
-        if (b.h_gs)
-            cudaFreeHost(b.h_gs);
-        b.h_gs = nullptr;
+    if (graphs > b.gcap || !b.d_tab) {
+        const uint32_t gc = std::max<uint32_t>(graphs, 1);
+        dev_free(b.d_tab);
+        dev_free(b.d_stat);
+        if (b.h_tab)
+            cudaFreeHost(b.h_tab);
+        if (b.h_stat)
+            cudaFreeHost(b.h_stat);
+        b.h_tab = b.h_stat = nullptr;
+        b.gd = nullptr;
+        b.boff = b.toff = nullptr;
         b.gcap = 0;
-        GPMA_TRY(dev_alloc(&b.gd, gc));
-        GPMA_TRY(dev_alloc(&b.gs, gc));
-        GPMA_TRY(dev_alloc(&b.boff, gc + 1));
-        GPMA_TRY(dev_alloc(&b.toff, gc + 1));
-        cudaError_t e = cudaMallocHost((void **)&b.h_gs, sizeof(GraphStatus) * gc);
+        const size_t tab = sizeof(GraphDesc) * gc + 2 * sizeof(uint32_t) * (gc + 1);
+        const size_t slot = (STAT_GS_OFFSET + sizeof(GraphStatus) * gc + 255) & ~size_t(255);
+        GPMA_TRY(dev_alloc(&b.d_tab, tab));
+        GPMA_TRY(dev_alloc(&b.d_stat, 2 * slot));
+        cudaError_t e = cudaMallocHost((void **)&b.h_tab, tab);
+        if (e == cudaSuccess)
+            e = cudaMallocHost((void **)&b.h_stat, slot);
         if (e != cudaSuccess)
-            return cuda_fail(e, "cudaMallocHost(graph status)");
+            return cuda_fail(e, "cudaMallocHost(update tables)");
+        b.gd = reinterpret_cast<GraphDesc *>(b.d_tab);
+        b.boff = reinterpret_cast<uint32_t *>(b.d_tab + sizeof(GraphDesc) * gc);
+        b.toff = b.boff + gc + 1;
+        b.stat_slot = slot;
+        b.parity = 0;
+        b.dirty = true;
         b.gcap = gc;
     }
     return GPMA_OK;
@@ -1518,13 +1546,15 @@ gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32
     GPMA_TRY(ensure_buffers(buf, n, k));
     if (!buf.cta_cnt)
         GPMA_TRY(dev_alloc(&buf.cta_cnt, 4ull * sms * MAX_BLOCKS_PER_SM));  // any tuned grid
-    // per-graph tables: descriptors, batch offsets, sort tile offsets
-    buf.h_gd.resize(k);
-    buf.h_off.assign(2ull * (k + 1), 0);
+    // per-graph tables in the pinned staging copy: descriptors, batch offsets,
+    // sort tile offsets (the previous launch's upload finished: it synchronised)
+    GraphDesc *h_gd = reinterpret_cast<GraphDesc *>(buf.h_tab);
+    uint32_t *h_boff = reinterpret_cast<uint32_t *>(buf.h_tab + sizeof(GraphDesc) * buf.gcap);
+    uint32_t *h_toff = h_boff + buf.gcap + 1;
     uint32_t max_height = 0;
     uint64_t chunk_need = 1;
     for (uint32_t i = 0; i < k; ++i) {
-        buf.h_gd[i] = describe(graphs[i]);
+        h_gd[i] = describe(graphs[i]);
         max_height = std::max(max_height, graphs[i]->geo.height);
         chunk_need += graphs[i]->geo.size / CHUNK + 1;
         if (i > 0 && graphs[i]->geo.seg < graphs[i - 1]->geo.seg) {
@@ -1532,44 +1562,54 @@ gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32
             return GPMA_ERR_INVALID;
         }
     }
+    h_toff[0] = 0;
     for (uint32_t i = 0; i <= k; ++i) {
-        buf.h_off[i] = (uint32_t)off[i];
+        h_boff[i] = (uint32_t)off[i];
         if (i > 0) {
             const uint64_t ni = off[i] - off[i - 1];
-            buf.h_off[k + 1 + i] = buf.h_off[k + i] + (uint32_t)((ni + SORT_TILE - 1) / SORT_TILE);
+            h_toff[i] = h_toff[i - 1] + (uint32_t)((ni + SORT_TILE - 1) / SORT_TILE);
         }
     }
-    const uint32_t tiles = buf.h_off[2 * k + 1];
+    const uint32_t tiles = h_toff[k];
     const uint64_t status_words = 8ull * tiles * 256;
     if (status_words > buf.sort_status_cap) {
         dev_free(buf.sort_status);
         GPMA_TRY(dev_alloc(&buf.sort_status, status_words));
         buf.sort_status_cap = status_words;
+        buf.dirty = true;
     }
     const uint32_t hist_rows = k == 1 ? 1 : k + 1;
     if (hist_rows > buf.hist_cap) {
         dev_free(buf.sort_hist);
         GPMA_TRY(dev_alloc(&buf.sort_hist, (size_t)hist_rows * 2048));
         buf.hist_cap = hist_rows;
+        buf.dirty = true;
     }
     if (chunk_need > buf.chunk_cap) {
         dev_free(buf.chunk_cnt);
         GPMA_TRY(dev_alloc(&buf.chunk_cnt, chunk_need));
         buf.chunk_cap = chunk_need;
     }
-    GPMA_CUDA(cudaMemcpyAsync(buf.gd, buf.h_gd.data(), sizeof(GraphDesc) * k, cudaMemcpyHostToDevice, s));
-    GPMA_CUDA(cudaMemcpyAsync(buf.boff, buf.h_off.data(), sizeof(uint32_t) * (k + 1), cudaMemcpyHostToDevice, s));
-    GPMA_CUDA(cudaMemcpyAsync(buf.toff, buf.h_off.data() + k + 1, sizeof(uint32_t) * (k + 1), cudaMemcpyHostToDevice,
-                              s));
-    GPMA_CUDA(cudaMemsetAsync(buf.status, 0, sizeof(DeviceStatus), s));
-    GPMA_CUDA(cudaMemsetAsync(buf.gs, 0, sizeof(GraphStatus) * k, s));
-    GPMA_CUDA(cudaMemsetAsync(buf.sort_hist, 0, sizeof(uint32_t) * hist_rows * 2048, s));
-    GPMA_CUDA(cudaMemsetAsync(buf.sort_tiles, 0, 8 * sizeof(uint32_t), s));
-    GPMA_CUDA(cudaMemsetAsync(buf.sort_status, 0, status_words * sizeof(uint32_t), s));
+    // one upload of the tables (up to the last tile offset in use)
+    const size_t tab_bytes = reinterpret_cast<unsigned char *>(h_toff + k + 1) - buf.h_tab;
+    GPMA_CUDA(cudaMemcpyAsync(buf.d_tab, buf.h_tab, tab_bytes, cudaMemcpyHostToDevice, s));
+    if (buf.dirty) {
+        // first launch, new buffers or an aborted launch: clear everything the
+        // kernel otherwise leaves zeroed for its successor
+        GPMA_CUDA(cudaMemsetAsync(buf.d_stat, 0, 2 * buf.stat_slot, s));
+        GPMA_CUDA(cudaMemsetAsync(buf.sort_hist, 0, sizeof(uint32_t) * buf.hist_cap * 2048, s));
+        GPMA_CUDA(cudaMemsetAsync(buf.sort_tiles, 0, 8 * sizeof(uint32_t), s));
+        GPMA_CUDA(cudaMemsetAsync(buf.sort_status, 0, buf.sort_status_cap * sizeof(uint32_t), s));
+        buf.dirty = false;
+    }
+    unsigned char *slot = buf.d_stat + buf.parity * buf.stat_slot;
+    unsigned char *next = buf.d_stat + (buf.parity ^ 1) * buf.stat_slot;
+    DeviceStatus *d_status = reinterpret_cast<DeviceStatus *>(slot);
+    GraphStatus *d_gs = reinterpret_cast<GraphStatus *>(slot + STAT_GS_OFFSET);
     prof_mark(profiling, ev, 1, s);
     UpdateArgs A;
     A.gd = buf.gd;
-    A.gs = buf.gs;
+    A.gs = d_gs;
     A.G = k;
     A.max_height = max_height;
     A.boff = buf.boff;
@@ -1598,15 +1638,23 @@ gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32
     A.rvals = buf.rvals;
     A.chunk_cnt = buf.chunk_cnt;
     A.cta_cnt = buf.cta_cnt;
-    A.st = buf.status;
+    A.st = d_status;
+    A.next_slot = reinterpret_cast<uint32_t *>(next);
+    A.next_slot_words = (uint32_t)(buf.stat_slot / sizeof(uint32_t));
+    A.hist_words = hist_rows * 2048;
+    A.status_words = (uint32_t)status_words;
     void *params[] = {&A};
     GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)update_kernel, dim3(grid), dim3(BLOCK), params, UPDATE_SMEM,
                                           s));
     prof_mark(profiling, ev, 2, s);
-    GPMA_CUDA(cudaMemcpyAsync(buf.h_status, buf.status, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
-    GPMA_CUDA(cudaMemcpyAsync(buf.h_gs, buf.gs, sizeof(GraphStatus) * k, cudaMemcpyDeviceToHost, s));
+    // one read-back: the status and this launch's per-graph results
+    GPMA_CUDA(cudaMemcpyAsync(buf.h_stat, slot, STAT_GS_OFFSET + sizeof(GraphStatus) * k, cudaMemcpyDeviceToHost, s));
     GPMA_CUDA(cudaStreamSynchronize(s));
-    const DeviceStatus &h = *buf.h_status;
+    buf.parity ^= 1;
+    const DeviceStatus &h = *reinterpret_cast<const DeviceStatus *>(buf.h_stat);
+    const GraphStatus *h_gs = reinterpret_cast<const GraphStatus *>(buf.h_stat + STAT_GS_OFFSET);
+    if (h.err || h.invalid_keys)
+        buf.dirty = true;  // the kernel stopped before (or during) its clean-up
     if (prof) {
         prof->kernel_launches += 1;  // the sort runs inside the update kernel
         prof->update_kernels++;
@@ -1629,7 +1677,7 @@ gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32
     }
     for (uint32_t i = 0; i < k; ++i) {
         gpma_graph *g = graphs[i];
-        const GraphStatus &gs = buf.h_gs[i];
+        const GraphStatus &gs = h_gs[i];
         const uint32_t inserts = gs.inserts ? gs.inserts - gs.ins_base : 0;  // end - first
         g->stats.last_inserts = h.significant ? h.inserts : inserts;
         g->stats.levels_visited += h.levels;
@@ -1641,7 +1689,7 @@ gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32
     if (h.significant)
         return root_rebuild(graphs[0], true, buf.ikeys[0], buf.ivals[0], h.inserts, s);
     for (uint32_t i = 0; i < k; ++i) {
-        const GraphStatus &gs = buf.h_gs[i];
+        const GraphStatus &gs = h_gs[i];
         if (gs.remaining > 0)
             GPMA_TRY(root_rebuild(graphs[i], false, buf.rkeys + gs.ins_base, buf.rvals + gs.ins_base, gs.remaining,
                                   s));
