@@ -27,7 +27,7 @@ from . import GPMA, Batch, get_tuning, gpma_bfs, set_tuning
 SPACE = {
     "bfs": {"bfs_blocks_per_sm": (4, 8), "bfs_dense_div": (0, 2, 3, 4, 6, 8)},
     "ms": {"ms_blocks_per_sm": (4, 8), "ms_dense_div": (0, 2, 3, 4, 8, 16)},
-    "update": {"update_blocks_per_sm": (1, 0)},
+    "update": {"update_blocks_per_sm": (2, 3)},
 }
 
 

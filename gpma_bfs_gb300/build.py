@@ -57,21 +57,18 @@ def _run(cmd: list[str]) -> None:
 def build(verbose: bool = False, ptxas_info: bool = False) -> Path:
     """Compiles (if needed) and returns the path of libgpma_gb300.so.
 
-    GPMA_UPDATE_MIN_BLOCKS (environment) sets the update kernel's minimum
-    resident CTAs per SM for register allocation and GPMA_SORT_ITEMS the keys
-    per thread of a radix-sort tile; changing either rebuilds.
+    GPMA_SORT_ITEMS (environment) sets the keys per thread of a radix-sort
+    tile; changing it rebuilds.
     """
     if verbose:
         os.environ["GPMA_BUILD_VERBOSE"] = "1"
     nvcc = _nvcc()
     BUILD.mkdir(exist_ok=True)
-    min_blocks = os.environ.get("GPMA_UPDATE_MIN_BLOCKS", "2")
     sort_items = os.environ.get("GPMA_SORT_ITEMS", "8")
     stamp = BUILD / "options.txt"
-    options = f"GPMA_UPDATE_MIN_BLOCKS={min_blocks}\nGPMA_SORT_ITEMS={sort_items}\n"
+    options = f"GPMA_SORT_ITEMS={sort_items}\n"
     if not stamp.exists() or stamp.read_text() != options:
         stamp.write_text(options)
-    NVCC_FLAGS.append(f"-DGPMA_UPDATE_MIN_BLOCKS={min_blocks}")
     NVCC_FLAGS.append(f"-DGPMA_SORT_ITEMS={sort_items}")
     HEADERS.append(stamp)
     jobs = []

@@ -294,7 +294,7 @@ gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32
                           uint32_t k, uint32_t *const *levels, uint64_t *reached, cudaStream_t s);
 void free_bfs(gpma_graph *g);
 void free_batch_bfs(gpma_batch *b);
-int update_grid_size(int sms);
+int update_grid_size(int sms, uint64_t n);
 
 // Launch shapes and switch points: they change speed, never results
 // (process-wide, set through gpma_set_tuning; defaults from measurement).
@@ -303,7 +303,7 @@ struct Tuning {
     uint32_t bfs_blocks_per_sm = 8;
     uint32_t ms_dense_div = 8;
     uint32_t ms_blocks_per_sm = 8;
-    uint32_t update_blocks_per_sm = 0;  // 0: as many as fit
+    uint32_t update_blocks_per_sm = 0;  // 0: chosen per launch (3-CTA build from 1M keys)
 };
 extern Tuning g_tuning;
 // CTAs per SM for a kernel that fits `fit` per SM, given a tuned request (0 = fit).

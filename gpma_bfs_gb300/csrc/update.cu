@@ -682,13 +682,13 @@ __device__ __forceinline__ uint32_t first_window_of_seg(const UpdateArgs &A, con
     return lo;
 }
 
-// Minimum resident CTAs per SM the register allocation must allow (build
-// option; 2 keeps every path spill-free).
-#ifndef GPMA_UPDATE_MIN_BLOCKS
-#define GPMA_UPDATE_MIN_BLOCKS 2
-#endif
-
-__global__ void __launch_bounds__(BLOCK, GPMA_UPDATE_MIN_BLOCKS) update_kernel(UpdateArgs A) {
+// Two register budgets of the same kernel: MINB resident CTAs per SM. Two
+// (128 registers, almost no spills) suits single large graphs, whose phases
+// are short and barrier-bound; three (80 registers, some spills to local
+// memory) suits many graphs per launch, whose phases are longer and gain from
+// the extra warps. gpma_tuning.update_blocks_per_sm selects one.
+template <int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint32_t tmp[BLOCK / 32 + 1];
     DeviceStatus *st = A.st;
@@ -1378,27 +1378,41 @@ GraphDesc describe(const gpma_graph *g) {
     return d;
 }
 
-int g_update_fit[64] = {};  // resident update-kernel CTAs per SM, per device
+int g_update_fit[64][2] = {};  // resident CTAs per SM of the two variants, per device
+
+// The variant for a launch of n keys: the tuned CTAs per SM (3 or more
+// selects the 3-CTA build), or when left to the library (0) the 3-CTA build
+// for launches of at least AUTO_WIDE_KEYS keys.
+constexpr uint64_t AUTO_WIDE_KEYS = 1u << 20;
+int update_variant(uint64_t n) {
+    const uint32_t t = g_tuning.update_blocks_per_sm;
+    return t >= 3 || (t == 0 && n >= AUTO_WIDE_KEYS) ? 1 : 0;
+}
+
+const void *update_kernel_ptr(int variant) {
+    return variant ? (const void *)update_kernel<3> : (const void *)update_kernel<2>;
+}
 
 }  // namespace
 
 Tuning g_tuning;
 
-int update_grid_size(int sms) {
+int update_grid_size(int sms, uint64_t n) {
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64)
         dev = 0;
-    if (g_update_fit[dev] == 0) {
-        if (cudaFuncSetAttribute(update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)UPDATE_SMEM) !=
-            cudaSuccess)
+    const int v = update_variant(n);
+    if (g_update_fit[dev][v] == 0) {
+        const void *k = update_kernel_ptr(v);
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)UPDATE_SMEM) != cudaSuccess)
             return 0;
         int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, update_kernel, BLOCK, UPDATE_SMEM) != cudaSuccess)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, BLOCK, UPDATE_SMEM) != cudaSuccess)
             return 0;
-        g_update_fit[dev] = std::min(per_sm, MAX_BLOCKS_PER_SM);
+        g_update_fit[dev][v] = std::min(per_sm, MAX_BLOCKS_PER_SM);
     }
-    return sms * blocks_per_sm(g_update_fit[dev], g_tuning.update_blocks_per_sm);
+    return sms * blocks_per_sm(g_update_fit[dev][v], g_tuning.update_blocks_per_sm);
 }
 
 gpma_status ensure_scratch(gpma_graph *g, uint32_t slots) {
@@ -1538,7 +1552,7 @@ gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32
     const uint64_t n = off[k];
     if (n == 0)
         return GPMA_OK;
-    const int grid = update_grid_size(sms);
+    const int grid = update_grid_size(sms, n);
     if (grid == 0) {
         set_error("update kernel cannot be resident");
         return GPMA_ERR_CUDA;
@@ -1644,7 +1658,7 @@ gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32
     A.hist_words = hist_rows * 2048;
     A.status_words = (uint32_t)status_words;
     void *params[] = {&A};
-    GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)update_kernel, dim3(grid), dim3(BLOCK), params, UPDATE_SMEM,
+    GPMA_CUDA(cudaLaunchCooperativeKernel(update_kernel_ptr(update_variant(n)), dim3(grid), dim3(BLOCK), params, UPDATE_SMEM,
                                           s));
     prof_mark(profiling, ev, 2, s);
     // one read-back: the status and this launch's per-graph results

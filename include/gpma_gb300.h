@@ -349,7 +349,8 @@ typedef struct gpma_tuning {
     uint32_t ms_dense_div;         /* multi-source BFS: the same switch on the union frontier of all lanes,
                                       against the slots of all graphs of the call */
     uint32_t ms_blocks_per_sm;     /* multi-source BFS grid */
-    uint32_t update_blocks_per_sm; /* persistent update kernel grid (0: as many as fit) */
+    uint32_t update_blocks_per_sm; /* persistent update kernel: 1-2 use the 128-register build, 3 the 80-register
+                                      one (more warps, some spills); 0 lets each launch choose (3 from 1M keys) */
     uint32_t reserved[3];
 } gpma_tuning;
 GPMA_API gpma_status gpma_get_tuning(gpma_tuning *out);

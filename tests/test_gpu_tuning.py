@@ -73,14 +73,14 @@ def test_update_results_independent_of_grid(restore_tuning):
     G = restore_tuning
     n, keys = _graphs()[1]
     layouts = []
-    for blocks in (1, 0):
+    for blocks in (1, 3, 0):  # the 128-register build at 1 CTA/SM, the 80-register build, automatic
         G.set_tuning(update_blocks_per_sm=blocks)
         g = G.GPMA(n)
         for i in range(0, len(keys), 7000):
             G.update_gpma(g, keys[i:i + 7000], np.ones(len(keys[i:i + 7000]), np.uint8))
         layouts.append(g.export_layout())
         g.close()
-    assert all(np.array_equal(x, y) for x, y in zip(*layouts))
+    assert all(all(np.array_equal(x, y) for x, y in zip(layouts[0], other)) for other in layouts[1:])
 
 
 def test_set_tuning_rejects_bad_grid(restore_tuning):
