@@ -39,7 +39,7 @@ def test_result_changing_setting_is_an_error(T):
     import gpma_bfs_gb300 as G
 
     def probe():
-        return 1.0, "a" if G.get_tuning()["update_blocks_per_sm"] != 1 else "b"
+        return 1.0, "a" if G.get_tuning()["update_blocks_per_sm"] != 3 else "b"
 
     before = G.get_tuning()
     with pytest.raises(RuntimeError, match="changed the result"):
