@@ -169,8 +169,9 @@ __device__ __forceinline__ uint32_t lb_slot(uint32_t p, uint32_t total, uint32_t
 
 // One pass over the frontier words, a word per warp at a time (lane l owns
 // node 32*word + l); `slots` accumulates the slots of every frontier row.
-//   QUEUE: rows over BIG_ROW slots are cut into CHUNK_SLOTS chunks for the
-//          whole grid (a full list leaves them to this pass);
+//   QUEUE: rows over BIG_ROW slots are cut into CHUNK_SLOTS chunks appended
+//          to `list` (the grid's list or the CTA's own; a full list leaves
+//          them to this pass);
 //   WALK:  the remaining rows are walked as one concatenated slot range, 64
 //          slots per step (without QUEUE, rows over BIG_ROW slots are left to
 //          the chunks an earlier pass queued);
@@ -178,8 +179,9 @@ __device__ __forceinline__ uint32_t lb_slot(uint32_t p, uint32_t total, uint32_t
 // Returns the nodes this lane claimed.
 template <bool QUEUE, bool WALK, bool CLEAR>
 __device__ __forceinline__ uint32_t frontier_pass(const BfsArgs &A, uint32_t *front_cur, uint32_t *front_next,
-                                                  uint32_t *chunk_cnt, uint32_t next_level, uint32_t words,
-                                                  uint32_t gwarp, uint32_t nwarps, uint32_t lane, uint32_t &slots) {
+                                                  uint2 *list, uint32_t list_cap, uint32_t *chunk_cnt,
+                                                  uint32_t next_level, uint32_t words, uint32_t gwarp, uint32_t nwarps,
+                                                  uint32_t lane, uint32_t &slots) {
     uint32_t fresh = 0;
     for (uint32_t wi = gwarp; wi < words; wi += nwarps) {
         const uint32_t f = front_cur[wi];
@@ -205,14 +207,14 @@ __device__ __forceinline__ uint32_t frontier_pass(const BfsArgs &A, uint32_t *fr
                 if (lane == 0)
                     base = atomicAdd(chunk_cnt, ch_total);
                 base = __shfl_sync(0xFFFFFFFFu, base, 0);
-                if (base + ch_total <= A.chunk_cap) {
+                if (base + ch_total <= list_cap) {
                     const uint32_t pos = base + ch_incl - nch;
                     for (uint32_t c = 0; c < nch; ++c)
-                        A.chunks[pos + c] = make_uint2(b + c * CHUNK_SLOTS, min(e, b + (c + 1) * CHUNK_SLOTS));
+                        list[pos + c] = make_uint2(b + c * CHUNK_SLOTS, min(e, b + (c + 1) * CHUNK_SLOTS));
                 } else {
                     // list full: neutralise the claimed entries, walk the rows here
-                    for (uint32_t c = base + lane; c < min(base + ch_total, A.chunk_cap); c += 32)
-                        A.chunks[c] = make_uint2(0, 0);
+                    for (uint32_t c = base + lane; c < min(base + ch_total, list_cap); c += 32)
+                        list[c] = make_uint2(0, 0);
                     overflow = true;
                 }
             }
@@ -250,7 +252,12 @@ __device__ __forceinline__ uint32_t level_count(const BfsArgs &A, uint32_t i, ui
 // often enough to pay for the extra pass).
 constexpr uint32_t DENSE_GATE = 64;
 
+// Long-row chunks one CTA keeps in shared memory on a small level.
+constexpr uint32_t LOCAL_CHUNKS = 1024;
+
 __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
+    __shared__ uint2 s_chunks[LOCAL_CHUNKS];
+    __shared__ uint32_t s_nch;
     GridBarrier *bar = reinterpret_cast<GridBarrier *>(A.ctl + CTL_BAR);
     uint32_t *err = A.ctl + CTL_ERR;
     const uint32_t lane = threadIdx.x & 31;
@@ -258,6 +265,7 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
     const uint32_t nwarps = gridDim.x * (BLOCK / 32);
     const uint32_t words = (A.n + 31) >> 5;
     uint32_t added = 0;
+    uint32_t last_frontier = 0;
     uint32_t i = 0;
     for (;; ++i) {
         if (A.stamps && blockIdx.x == 0 && threadIdx.x == 0 && i < CTL_PROFILE_LEVELS)
@@ -265,6 +273,8 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
         const uint32_t frontier = cta_broadcast_read(A.ctl + CTL_CNT + i % 3);
         if (frontier == 0)
             break;
+        const uint32_t prev_frontier = last_frontier;
+        last_frontier = frontier;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             A.ctl[CTL_CNT + (i + 2) % 3] = 0;
             A.ctl[CTL_SLOTS + (i + 1) % 3] = 0;
@@ -281,8 +291,8 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
         const bool probe = A.dense_div && (uint64_t)frontier * DENSE_GATE >= A.n;
         bool dense = false;
         if (probe) {
-            fresh += frontier_pass<true, false, false>(A, front_cur, front_next, chunk_cnt, next_level, words, gwarp,
-                                                       nwarps, lane, slots);
+            fresh += frontier_pass<true, false, false>(A, front_cur, front_next, A.chunks, A.chunk_cap, chunk_cnt,
+                                                       next_level, words, gwarp, nwarps, lane, slots);
 #pragma unroll
             for (int d = 16; d >= 1; d >>= 1)
                 slots += __shfl_xor_sync(0xFFFFFFFFu, slots, d);
@@ -323,11 +333,35 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
         }
         if (probe) {
             // the short rows now; the long rows' chunks, queued by the first pass, below
-            fresh += frontier_pass<false, true, true>(A, front_cur, front_next, chunk_cnt, next_level, words, gwarp,
-                                                      nwarps, lane, slots);
+            fresh += frontier_pass<false, true, true>(A, front_cur, front_next, A.chunks, A.chunk_cap, chunk_cnt,
+                                                      next_level, words, gwarp, nwarps, lane, slots);
+        } else if ((uint64_t)frontier * DENSE_GATE < A.n && frontier < prev_frontier) {
+            // a small, shrinking frontier (the tail of the search, past the
+            // hubs): each CTA queues its long rows' chunks in shared memory
+            // and its own warps take them, so the level needs one grid barrier
+            // instead of two
+            if (threadIdx.x == 0)
+                s_nch = 0;
+            __syncthreads();
+            fresh += frontier_pass<true, true, true>(A, front_cur, front_next, s_chunks, LOCAL_CHUNKS, &s_nch,
+                                                     next_level, words, gwarp, nwarps, lane, slots);
+            __syncthreads();
+            const uint32_t nloc = min(s_nch, LOCAL_CHUNKS);
+            for (uint32_t c = threadIdx.x >> 5; c < nloc; c += BLOCK / 32) {
+                const uint2 ch = s_chunks[c];
+                for (uint32_t s0 = ch.x; s0 < ch.y; s0 += 64) {
+                    const uint32_t sa = s0 + lane < ch.y ? s0 + lane : SIZE_NONE;
+                    const uint32_t sb = s0 + 32 + lane < ch.y ? s0 + 32 + lane : SIZE_NONE;
+                    fresh += visit_pair(A, sa, sb, next_level, front_next);
+                }
+            }
+            added += level_count(A, i, fresh, lane);
+            if (!grid_barrier(bar, err))
+                return;
+            continue;
         } else {
-            fresh += frontier_pass<true, true, true>(A, front_cur, front_next, chunk_cnt, next_level, words, gwarp,
-                                                     nwarps, lane, slots);
+            fresh += frontier_pass<true, true, true>(A, front_cur, front_next, A.chunks, A.chunk_cap, chunk_cnt,
+                                                     next_level, words, gwarp, nwarps, lane, slots);
             if (!grid_barrier(bar, err))
                 return;
         }
