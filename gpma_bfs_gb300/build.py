@@ -58,18 +58,21 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> Path:
     """Compiles (if needed) and returns the path of libgpma_gb300.so.
 
     GPMA_SORT_ITEMS (environment) sets the keys per thread of a radix-sort
-    tile; changing it rebuilds.
+    tile and GPMA_BFS_LANE_SLOTS the slots a BFS lane walks per step;
+    changing either rebuilds.
     """
     if verbose:
         os.environ["GPMA_BUILD_VERBOSE"] = "1"
     nvcc = _nvcc()
     BUILD.mkdir(exist_ok=True)
     sort_items = os.environ.get("GPMA_SORT_ITEMS", "8")
+    lane_slots = os.environ.get("GPMA_BFS_LANE_SLOTS", "4")
     stamp = BUILD / "options.txt"
-    options = f"GPMA_SORT_ITEMS={sort_items}\n"
+    options = f"GPMA_SORT_ITEMS={sort_items}\nGPMA_BFS_LANE_SLOTS={lane_slots}\n"
     if not stamp.exists() or stamp.read_text() != options:
         stamp.write_text(options)
     NVCC_FLAGS.append(f"-DGPMA_SORT_ITEMS={sort_items}")
+    NVCC_FLAGS.append(f"-DGPMA_BFS_LANE_SLOTS={lane_slots}")
     HEADERS.append(stamp)
     jobs = []
     objs = []

@@ -53,8 +53,16 @@ enum : uint32_t {
 // every warp of the grid shares in a second phase of the level; shorter rows
 // of one frontier word are walked together by one warp. (With node ids
 // ordered by degree, one word can otherwise hold 32 heavy rows.)
-constexpr uint32_t BIG_ROW = 32;
-constexpr uint32_t CHUNK_SLOTS = 64;
+// A warp walks LANE_SLOTS slots per lane per step (build option), all loads
+// of a step issued before any claim; a chunk is one step of a warp.
+#ifndef GPMA_BFS_LANE_SLOTS
+#define GPMA_BFS_LANE_SLOTS 4
+#endif
+constexpr uint32_t LANE_SLOTS = GPMA_BFS_LANE_SLOTS;
+static_assert(LANE_SLOTS >= 1 && LANE_SLOTS <= 8, "BFS lane slots out of range");
+constexpr uint32_t STEP_SLOTS = 32 * LANE_SLOTS;
+constexpr uint32_t BIG_ROW = STEP_SLOTS / 2;
+constexpr uint32_t CHUNK_SLOTS = STEP_SLOTS;
 // Chunk list entries for an array of `size` slots: rows over BIG_ROW slots
 // yield at most len/64 + 1 chunks each and there are at most size/33 of them,
 // so one level queues fewer than size/64 + size/33 < size/16 chunks; the list
@@ -78,37 +86,36 @@ struct BfsArgs {
     unsigned long long *stamps;  // per-level profile (CTL_PROFILE_LEVELS stamps + info words) or null
 };
 
-// Two edge slots per lane (s < SIZE_NONE means present): all loads are
-// issued before any claim, so each lane keeps several requests in flight.
-// Returns the number of nodes this lane claimed.
-__device__ __forceinline__ uint32_t visit_pair(const BfsArgs &A, uint32_t sa, uint32_t sb, uint32_t next_level,
-                                               uint32_t *front_next) {
-    uint64_t ka = KEY_NONE, kb = KEY_NONE;
-    uint8_t va = 0, vb = 0;
-    if (sa != SIZE_NONE) {
-        ka = A.keys[sa];
-        va = A.vals[sa];
+// LANE_SLOTS edge slots of one lane (SIZE_NONE: absent): every key, value
+// and visited word is loaded before any claim, so each lane keeps several
+// requests in flight. Returns the number of nodes this lane claimed.
+__device__ __forceinline__ uint32_t visit_slots(const BfsArgs &A, const uint32_t (&sl)[LANE_SLOTS],
+                                                uint32_t next_level, uint32_t *front_next) {
+    uint32_t w[LANE_SLOTS], seen[LANE_SLOTS];
+#pragma unroll
+    for (uint32_t j = 0; j < LANE_SLOTS; ++j) {
+        uint64_t k = KEY_NONE;
+        uint8_t v = 0;
+        if (sl[j] != SIZE_NONE) {
+            k = A.keys[sl[j]];
+            v = A.vals[sl[j]];
+        }
+        w[j] = (uint32_t)k;
+        seen[j] = (w[j] != 0xFFFFFFFFu && v != 0 && w[j] < A.n) ? 0u : 0xFFFFFFFFu;
     }
-    if (sb != SIZE_NONE) {
-        kb = A.keys[sb];
-        vb = A.vals[sb];
-    }
-    const uint32_t wa = (uint32_t)ka, wb = (uint32_t)kb;
-    const bool oka = wa != 0xFFFFFFFFu && va != 0 && wa < A.n;
-    const bool okb = wb != 0xFFFFFFFFu && vb != 0 && wb < A.n;
-    const uint32_t bita = 1u << (wa & 31), bitb = 1u << (wb & 31);
-    const uint32_t seen_a = oka ? A.visited[wa >> 5] : 0xFFFFFFFFu;
-    const uint32_t seen_b = okb ? A.visited[wb >> 5] : 0xFFFFFFFFu;
+#pragma unroll
+    for (uint32_t j = 0; j < LANE_SLOTS; ++j)
+        if (!seen[j])
+            seen[j] = A.visited[w[j] >> 5];
     uint32_t fresh = 0;
-    if (!(seen_a & bita) && !(atomicOr(&A.visited[wa >> 5], bita) & bita)) {
-        A.levels[wa] = next_level;
-        atomicOr(&front_next[wa >> 5], bita);
-        ++fresh;
-    }
-    if (!(seen_b & bitb) && !(atomicOr(&A.visited[wb >> 5], bitb) & bitb)) {
-        A.levels[wb] = next_level;
-        atomicOr(&front_next[wb >> 5], bitb);
-        ++fresh;
+#pragma unroll
+    for (uint32_t j = 0; j < LANE_SLOTS; ++j) {
+        const uint32_t bit = 1u << (w[j] & 31);
+        if (!(seen[j] & bit) && !(atomicOr(&A.visited[w[j] >> 5], bit) & bit)) {
+            A.levels[w[j]] = next_level;
+            atomicOr(&front_next[w[j] >> 5], bit);
+            ++fresh;
+        }
     }
     return fresh;
 }
@@ -226,10 +233,12 @@ __device__ __forceinline__ uint32_t frontier_pass(const BfsArgs &A, uint32_t *fr
         const uint32_t incl = warp_incl_scan(len);
         const uint32_t excl = incl - len;
         const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-        for (uint32_t p0 = 0; p0 < total; p0 += 64) {
-            const uint32_t sa = lb_slot(p0 + lane, total, b, excl);
-            const uint32_t sb = lb_slot(p0 + 32 + lane, total, b, excl);
-            fresh += visit_pair(A, sa, sb, next_level, front_next);
+        for (uint32_t p0 = 0; p0 < total; p0 += STEP_SLOTS) {
+            uint32_t sl[LANE_SLOTS];
+#pragma unroll
+            for (uint32_t j = 0; j < LANE_SLOTS; ++j)
+                sl[j] = lb_slot(p0 + 32 * j + lane, total, b, excl);
+            fresh += visit_slots(A, sl, next_level, front_next);
         }
     }
     return fresh;
@@ -349,10 +358,12 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
             const uint32_t nloc = min(s_nch, LOCAL_CHUNKS);
             for (uint32_t c = threadIdx.x >> 5; c < nloc; c += BLOCK / 32) {
                 const uint2 ch = s_chunks[c];
-                for (uint32_t s0 = ch.x; s0 < ch.y; s0 += 64) {
-                    const uint32_t sa = s0 + lane < ch.y ? s0 + lane : SIZE_NONE;
-                    const uint32_t sb = s0 + 32 + lane < ch.y ? s0 + 32 + lane : SIZE_NONE;
-                    fresh += visit_pair(A, sa, sb, next_level, front_next);
+                for (uint32_t s0 = ch.x; s0 < ch.y; s0 += STEP_SLOTS) {
+                    uint32_t sl[LANE_SLOTS];
+#pragma unroll
+                    for (uint32_t j = 0; j < LANE_SLOTS; ++j)
+                        sl[j] = s0 + 32 * j + lane < ch.y ? s0 + 32 * j + lane : SIZE_NONE;
+                    fresh += visit_slots(A, sl, next_level, front_next);
                 }
             }
             added += level_count(A, i, fresh, lane);
@@ -369,10 +380,12 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
         const uint32_t nch_all = min(cta_broadcast_read(chunk_cnt), A.chunk_cap);
         for (uint32_t c = gwarp; c < nch_all; c += nwarps) {
             const uint2 ch = A.chunks[c];
-            for (uint32_t s0 = ch.x; s0 < ch.y; s0 += 64) {
-                const uint32_t sa = s0 + lane < ch.y ? s0 + lane : SIZE_NONE;
-                const uint32_t sb = s0 + 32 + lane < ch.y ? s0 + 32 + lane : SIZE_NONE;
-                fresh += visit_pair(A, sa, sb, next_level, front_next);
+            for (uint32_t s0 = ch.x; s0 < ch.y; s0 += STEP_SLOTS) {
+                uint32_t sl[LANE_SLOTS];
+#pragma unroll
+                for (uint32_t j = 0; j < LANE_SLOTS; ++j)
+                    sl[j] = s0 + 32 * j + lane < ch.y ? s0 + 32 * j + lane : SIZE_NONE;
+                fresh += visit_slots(A, sl, next_level, front_next);
             }
         }
         added += level_count(A, i, fresh, lane);

@@ -299,7 +299,7 @@ int update_grid_size(int sms, uint64_t n);
 // Launch shapes and switch points: they change speed, never results
 // (process-wide, set through gpma_set_tuning; defaults from measurement).
 struct Tuning {
-    uint32_t bfs_dense_div = 4;
+    uint32_t bfs_dense_div = 0;  // rows only: with 4 slots per lane the walk beat the sweep on every level measured
     uint32_t bfs_blocks_per_sm = 8;
     uint32_t ms_dense_div = 8;
     uint32_t ms_blocks_per_sm = 8;

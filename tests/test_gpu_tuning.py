@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 SETTINGS = [
     dict(bfs_dense_div=0, ms_dense_div=0),                    # rows only
     dict(bfs_dense_div=1 << 30, ms_dense_div=1 << 30),        # every level sweeps all slots
-    dict(bfs_dense_div=4, ms_dense_div=4),                    # the default switch
+    dict(bfs_dense_div=4, ms_dense_div=4),                    # a middle switch point
     dict(bfs_dense_div=16, ms_dense_div=2, bfs_blocks_per_sm=1, ms_blocks_per_sm=3, update_blocks_per_sm=1),
 ]
 
