@@ -24,7 +24,7 @@ import numpy as np
 __all__ = [
     "GPMA", "GPMAError", "update_gpma", "gpma_bfs", "gpma_bfs_multi", "lib", "library_path",
     "KEY_NONE", "KEY_MAX", "COL_IDX_NONE", "VALUE_NONE", "gen_rmat", "gen_chung_lu", "edges_to_keys",
-    "read_edges_text", "write_edges_text",
+    "read_edges_text", "write_edges_text", "Step",
 ]
 
 KEY_NONE = 0xFFFFFFFFFFFFFFFF  # gpma.cuh:15
@@ -72,6 +72,11 @@ class _Tuning(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint32) for n in ("bfs_dense_div", "bfs_blocks_per_sm", "ms_dense_div",
                                                "ms_blocks_per_sm", "update_blocks_per_sm")] + \
                [("reserved", ctypes.c_uint32 * 3)]
+
+
+class _StepStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("runs", "graph_launches", "builds", "param_updates", "host_runs")] + \
+        [("last_ms", ctypes.c_double), ("total_ms", ctypes.c_double)]
 
 
 class _ServerConfig(ctypes.Structure):
@@ -161,6 +166,10 @@ def lib() -> ctypes.CDLL:
         "gpma_pagerank": (st, [P, ctypes.c_float, u32, ctypes.c_double, P, ctypes.POINTER(u32), P]),
         "gpma_components": (st, [P, P, ctypes.POINTER(u64), ctypes.POINTER(u32), P]),
         "gpma_load": (st, [ctypes.c_char_p, P, ctypes.POINTER(P)]),
+        "gpma_step_create": (st, [P, ctypes.POINTER(P)]),
+        "gpma_step_destroy": (st, [P]),
+        "gpma_step_run": (st, [P, P, P, u64, u32, P, ctypes.POINTER(u64), P]),
+        "gpma_step_get_stats": (st, [P, ctypes.POINTER(_StepStats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -390,6 +399,61 @@ def gpma_bfs(gpma: GPMA, node_size: int, edge_size: int, start_node: int, result
     _check(lib().gpma_bfs(gpma.handle, int(start_node), rp, ctypes.byref(reached), _stream_ptr(stream)), "gpma_bfs")
     del keep
     return results, reached.value
+
+
+class Step:
+    """One slide step of a graph -- update_gpma of a batch, then gpma_bfs
+    from a source -- recorded as a CUDA graph on first use and replayed for
+    every later step (gpma_step_* in the C ABI). ``run`` returns exactly what
+    update_gpma followed by gpma_bfs returns. Close the step before its graph.
+    """
+
+    def __init__(self, gpma: GPMA):
+        self.gpma = gpma
+        h = ctypes.c_void_p()
+        _check(lib().gpma_step_create(gpma.handle, ctypes.byref(h)), "gpma_step_create")
+        self.handle = h
+
+    def run(self, update_keys, update_values, start_node: int, results=None, stream=None) -> int:
+        """Applies the batch, runs the BFS from start_node and returns the
+        reachable node count; levels go to ``results`` (host or device,
+        row_num entries) when given."""
+        if len(update_keys) != len(update_values):
+            raise ValueError("Inconsistant kv size.")
+        if isinstance(update_keys, np.ndarray):
+            update_keys = np.ascontiguousarray(update_keys, dtype=np.uint64)
+        if isinstance(update_values, np.ndarray):
+            update_values = np.ascontiguousarray(update_values).view(np.uint8) \
+                if update_values.dtype.itemsize == 1 else np.ascontiguousarray(update_values, dtype=np.uint8)
+        n = len(update_keys)
+        kp, kk = _ptr(update_keys) if n else (None, None)
+        vp, vk = _ptr(update_values) if n else (None, None)
+        rp, rk = (None, None)
+        if results is not None:
+            if len(results) < self.gpma.row_num:
+                raise ValueError("results holds fewer than row_num entries")
+            rp, rk = _ptr(results)
+        reached = ctypes.c_uint64()
+        _check(lib().gpma_step_run(self.handle, kp, vp, n, int(start_node), rp, ctypes.byref(reached),
+                                   _stream_ptr(stream)), "gpma_step_run")
+        del kk, vk, rk
+        return reached.value
+
+    def stats(self) -> dict:
+        s = _StepStats()
+        _check(lib().gpma_step_get_stats(self.handle, ctypes.byref(s)), "gpma_step_get_stats")
+        return {n: getattr(s, n) for n, _ in _StepStats._fields_}
+
+    def close(self) -> None:
+        if self.handle:
+            lib().gpma_step_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def gpma_bfs_multi(gpma: GPMA, sources, results=None, stream=None):

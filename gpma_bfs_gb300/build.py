@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", f"-I{INCLUDE}"]
 CC_FLAGS = ["-O2", "-std=c11", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall", f"-I{INCLUDE}"]
 
-CU_SOURCES = ["update.cu", "bfs.cu", "msbfs.cu", "capi.cu", "server.cu", "analytics.cu"]
+CU_SOURCES = ["update.cu", "bfs.cu", "msbfs.cu", "capi.cu", "server.cu", "analytics.cu", "step.cu"]
 C_SOURCES = ["graphgen.c"]
 HEADERS = [CSRC / "gpma_internal.cuh", CSRC / "sort.cuh", INCLUDE / "gpma_gb300.h"]
 

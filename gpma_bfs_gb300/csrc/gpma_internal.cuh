@@ -15,6 +15,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -278,6 +279,46 @@ inline double prof_elapsed(bool on, cudaEvent_t *ev, int a, int b) {
 inline void prof_mark(gpma_graph *g, int i, cudaStream_t s) { prof_mark(g->profiling, g->ev, i, s); }
 inline double prof_elapsed(gpma_graph *g, int a, int b) { return prof_elapsed(g->profiling, g->ev, a, b); }
 
+// One kernel launch whose argument is a single by-value struct, recorded so
+// that it can be launched directly or added to a CUDA graph as a kernel node.
+struct KernelLaunch {
+    static constexpr size_t ARG_BYTES = 512;
+    const void *func = nullptr;
+    dim3 grid{1, 1, 1};
+    dim3 block{BLOCK, 1, 1};
+    size_t smem = 0;
+    size_t arg_bytes = 0;
+    alignas(16) unsigned char args[ARG_BYTES] = {};
+    void *params[1] = {nullptr};  // points at args when handed to CUDA
+
+    void set(const void *f, int grid_x, size_t smem_bytes, const void *a, size_t bytes) {
+        func = f;
+        grid = dim3((unsigned)grid_x, 1, 1);
+        smem = smem_bytes;
+        arg_bytes = bytes;
+        memcpy(args, a, bytes);
+    }
+    cudaError_t launch_cooperative(cudaStream_t s) {
+        params[0] = args;
+        return cudaLaunchCooperativeKernel(func, grid, block, params, smem, s);
+    }
+    cudaKernelNodeParams node() {
+        params[0] = args;
+        cudaKernelNodeParams p{};
+        p.func = const_cast<void *>(func);
+        p.gridDim = grid;
+        p.blockDim = block;
+        p.sharedMemBytes = (unsigned)smem;
+        p.kernelParams = params;
+        p.extra = nullptr;
+        return p;
+    }
+    bool same(const KernelLaunch &o) const {
+        return func == o.func && grid.x == o.grid.x && smem == o.smem && arg_bytes == o.arg_bytes &&
+               memcmp(args, o.args, arg_bytes) == 0;
+    }
+};
+
 // ---- host entry points implemented per translation unit -------------------
 gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs);
 void free_buffers(BatchBuffers &b);
@@ -288,7 +329,47 @@ gpma_status ensure_scratch(gpma_graph *g, uint32_t slots);
 gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32_t k, BatchBuffers &buf, int sms,
                           cudaStream_t s, bool check_keys, bool profiling, cudaEvent_t *ev, gpma_profile *prof);
 gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys = true);
+// The three host parts of update_graphs, for callers that enqueue the launch
+// themselves (a CUDA graph step). update_plan sizes the buffers, fills the
+// pinned tables (*tab_bytes of buf.h_tab to upload to buf.d_tab) and records
+// the cooperative kernel launch; its status lands in slot buf.parity of
+// buf.d_stat (update_status_bytes(k) bytes to read back). update_clear zeroes
+// the sort state and status slots after a failed or first launch. update_finish
+// reads the copied status, updates the graphs' stats, finishes root rebuilds
+// on the host and flips the status slot. update_needs_host: the status asks
+// for host work or reports an error (the array changed after the kernel).
+gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t k, BatchBuffers &buf, int sms,
+                        bool check_keys, size_t *tab_bytes, KernelLaunch *L);
+gpma_status update_clear(BatchBuffers &buf, cudaStream_t s);
+size_t update_status_bytes(uint32_t k);
+gpma_status update_finish(gpma_graph *const *graphs, uint32_t k, BatchBuffers &buf, const unsigned char *stat,
+                          cudaStream_t s, gpma_profile *prof, double kernel_ms);
+bool update_needs_host(const unsigned char *stat, uint32_t k);
 gpma_status bfs_run(gpma_graph *g, uint32_t src, cudaStream_t s, uint64_t *reached);
+// The host parts of bfs_run, for callers that enqueue it themselves: the
+// buffers to zero, the one-thread init kernel (its five arguments) and the
+// cooperative BFS kernel; ctl_bytes of g->bfs_ctl are read back into
+// g->h_bfs_ctl and checked by bfs_finish.
+struct BfsPlan {
+    static constexpr int CLEARS = 5;
+    void *clear_ptr[CLEARS];
+    size_t clear_bytes[CLEARS];
+    const void *init_func;
+    uint32_t *init_levels, *init_visited, *init_front0, *init_ctl;
+    uint32_t init_src;
+    void *init_params[5];  // point at the init_* fields when handed to CUDA
+    KernelLaunch main;
+    size_t ctl_bytes;
+    void bind_init() {
+        init_params[0] = &init_levels;
+        init_params[1] = &init_visited;
+        init_params[2] = &init_front0;
+        init_params[3] = &init_ctl;
+        init_params[4] = &init_src;
+    }
+};
+gpma_status bfs_plan(gpma_graph *g, uint32_t src, BfsPlan *P);
+gpma_status bfs_finish(gpma_graph *g, uint64_t *reached);
 gpma_status bfs_noalloc_run(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached, cudaStream_t s);
 gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs, const uint32_t *nsrc,
                           uint32_t k, uint32_t *const *levels, uint64_t *reached, cudaStream_t s);

@@ -1,0 +1,324 @@
+// step.cu - one sliding-window step of a graph (update_gpma of a batch, then
+// BFS from one source) recorded once as a CUDA graph and replayed per step.
+//
+// The reference's demo loop (gpma_bfs_demo.cu, main loop) calls update_gpma
+// and then gpma_bfs for every slide step; each call is a chain of launches,
+// copies and host synchronisations. Here the device work of a whole step is
+// one graph launch:
+//   table upload -> update kernel (cooperative) -> 5 BFS clears -> BFS init ->
+//   BFS kernel (cooperative) -> status and BFS control read-back
+// with a single host synchronisation. The batch upload and the optional copy
+// of the levels go on the same stream outside the graph, so the caller's
+// buffers may be pageable, pinned or device memory.
+//
+// The graph is rebuilt only when something baked into its nodes changes
+// (buffers reallocated, the kernel variant or grid, the array geometry
+// enlarging the BFS buffers); the per-step arguments (batch size, status
+// slot, source) are updated in place with cudaGraphExecKernelNodeSetParams.
+// When the update kernel asks for host work (root resize, the bulk rebuild
+// of a large batch) or fails, the step finishes on the host exactly as
+// update_gpma does and the BFS is run again on the final array, so results
+// are always those of update_gpma followed by gpma_bfs.
+#include "gpma_internal.cuh"
+
+struct gpma_step {
+    gpma_graph *g = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t n_update = nullptr, n_init = nullptr, n_bfs = nullptr;
+    // what the nodes were built with
+    gpma::KernelLaunch upd, bfs;
+    uint32_t *init_args[4] = {};
+    uint32_t init_src = 0;
+    struct Baked {
+        const void *h_tab, *d_tab, *d_stat, *bfs_ctl, *h_bfs_ctl;
+        size_t tab_bytes, stat_slot, ctl_bytes;
+        const void *upd_func, *bfs_func;
+        unsigned upd_grid, bfs_grid;
+        size_t upd_smem;
+        void *clear_ptr[gpma::BfsPlan::CLEARS];
+        size_t clear_bytes[gpma::BfsPlan::CLEARS];
+    } baked{};
+    unsigned char *h_stat = nullptr;  // pinned copy of both status slots
+    size_t h_stat_bytes = 0;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    gpma_step_stats stats{};
+};
+
+namespace gpma {
+namespace {
+
+void drop_graph(gpma_step *st) {
+    if (st->exec)
+        cudaGraphExecDestroy(st->exec);
+    if (st->graph)
+        cudaGraphDestroy(st->graph);
+    st->exec = nullptr;
+    st->graph = nullptr;
+    st->n_update = st->n_init = st->n_bfs = nullptr;
+}
+
+gpma_step::Baked bake(const gpma_graph *g, size_t tab_bytes, const KernelLaunch &upd, const BfsPlan &bp) {
+    gpma_step::Baked b;
+    memset(&b, 0, sizeof(b));  // compared byte-wise
+    b.h_tab = g->buf.h_tab;
+    b.d_tab = g->buf.d_tab;
+    b.d_stat = g->buf.d_stat;
+    b.bfs_ctl = g->bfs_ctl;
+    b.h_bfs_ctl = g->h_bfs_ctl;
+    b.tab_bytes = tab_bytes;
+    b.stat_slot = g->buf.stat_slot;
+    b.ctl_bytes = bp.ctl_bytes;
+    b.upd_func = upd.func;
+    b.bfs_func = bp.main.func;
+    b.upd_grid = upd.grid.x;
+    b.bfs_grid = bp.main.grid.x;
+    b.upd_smem = upd.smem;
+    for (int i = 0; i < BfsPlan::CLEARS; ++i) {
+        b.clear_ptr[i] = bp.clear_ptr[i];
+        b.clear_bytes[i] = bp.clear_bytes[i];
+    }
+    return b;
+}
+
+bool same_baked(const gpma_step::Baked &a, const gpma_step::Baked &b) { return memcmp(&a, &b, sizeof(a)) == 0; }
+
+gpma_status set_cooperative(cudaGraphNode_t node) {
+    cudaLaunchAttributeValue v{};
+    v.cooperative = 1;
+    GPMA_CUDA(cudaGraphKernelNodeSetAttribute(node, cudaLaunchAttributeCooperative, &v));
+    return GPMA_OK;
+}
+
+// Builds and instantiates the step's graph from the current plans (one chain).
+gpma_status build_graph(gpma_step *st, size_t tab_bytes, KernelLaunch &upd, BfsPlan &bp) {
+    drop_graph(st);
+    gpma_graph *g = st->g;
+    const size_t stat_bytes = 2 * g->buf.stat_slot;
+    if (stat_bytes > st->h_stat_bytes) {
+        if (st->h_stat)
+            cudaFreeHost(st->h_stat);
+        st->h_stat = nullptr;
+        st->h_stat_bytes = 0;
+        GPMA_CUDA(cudaMallocHost((void **)&st->h_stat, stat_bytes));
+        st->h_stat_bytes = stat_bytes;
+    }
+    GPMA_CUDA(cudaGraphCreate(&st->graph, 0));
+    cudaGraphNode_t prev = nullptr, node = nullptr;
+    auto deps = [&]() { return prev ? &prev : (const cudaGraphNode_t *)nullptr; };
+    auto ndeps = [&]() { return prev ? (size_t)1 : (size_t)0; };
+    GPMA_CUDA(cudaGraphAddMemcpyNode1D(&node, st->graph, deps(), ndeps(), g->buf.d_tab, g->buf.h_tab, tab_bytes,
+                                       cudaMemcpyHostToDevice));
+    prev = node;
+    cudaKernelNodeParams kp = upd.node();
+    GPMA_CUDA(cudaGraphAddKernelNode(&st->n_update, st->graph, deps(), ndeps(), &kp));
+    GPMA_TRY(set_cooperative(st->n_update));
+    prev = st->n_update;
+    for (int i = 0; i < BfsPlan::CLEARS; ++i) {
+        cudaMemsetParams mp{};
+        mp.dst = bp.clear_ptr[i];
+        mp.value = 0;
+        mp.elementSize = 4;  // every cleared buffer is 32-bit words
+        mp.width = bp.clear_bytes[i] / 4;
+        mp.height = 1;
+        mp.pitch = 0;
+        GPMA_CUDA(cudaGraphAddMemsetNode(&node, st->graph, deps(), ndeps(), &mp));
+        prev = node;
+    }
+    bp.bind_init();
+    cudaKernelNodeParams ip{};
+    ip.func = const_cast<void *>(bp.init_func);
+    ip.gridDim = dim3(1, 1, 1);
+    ip.blockDim = dim3(1, 1, 1);
+    ip.sharedMemBytes = 0;
+    ip.kernelParams = bp.init_params;
+    GPMA_CUDA(cudaGraphAddKernelNode(&st->n_init, st->graph, deps(), ndeps(), &ip));
+    prev = st->n_init;
+    kp = bp.main.node();
+    GPMA_CUDA(cudaGraphAddKernelNode(&st->n_bfs, st->graph, deps(), ndeps(), &kp));
+    GPMA_TRY(set_cooperative(st->n_bfs));
+    prev = st->n_bfs;
+    GPMA_CUDA(cudaGraphAddMemcpyNode1D(&node, st->graph, deps(), ndeps(), st->h_stat, g->buf.d_stat, stat_bytes,
+                                       cudaMemcpyDeviceToHost));
+    prev = node;
+    GPMA_CUDA(cudaGraphAddMemcpyNode1D(&node, st->graph, deps(), ndeps(), g->h_bfs_ctl, g->bfs_ctl, bp.ctl_bytes,
+                                       cudaMemcpyDeviceToHost));
+    GPMA_CUDA(cudaGraphInstantiate(&st->exec, st->graph, 0));
+    st->upd = upd;
+    st->bfs = bp.main;
+    st->init_args[0] = bp.init_levels;
+    st->init_args[1] = bp.init_visited;
+    st->init_args[2] = bp.init_front0;
+    st->init_args[3] = bp.init_ctl;
+    st->init_src = bp.init_src;
+    st->baked = bake(g, tab_bytes, upd, bp);
+    st->stats.builds++;
+    return GPMA_OK;
+}
+
+// Brings the instantiated graph's per-step arguments up to date.
+gpma_status refresh_params(gpma_step *st, KernelLaunch &upd, BfsPlan &bp) {
+    if (!upd.same(st->upd)) {
+        cudaKernelNodeParams kp = upd.node();
+        GPMA_CUDA(cudaGraphExecKernelNodeSetParams(st->exec, st->n_update, &kp));
+        st->upd = upd;
+        st->stats.param_updates++;
+    }
+    const uint32_t *ia[4] = {bp.init_levels, bp.init_visited, bp.init_front0, bp.init_ctl};
+    bool init_same = bp.init_src == st->init_src;
+    for (int i = 0; i < 4; ++i)
+        init_same = init_same && ia[i] == st->init_args[i];
+    if (!init_same) {
+        bp.bind_init();
+        cudaKernelNodeParams ip{};
+        ip.func = const_cast<void *>(bp.init_func);
+        ip.gridDim = dim3(1, 1, 1);
+        ip.blockDim = dim3(1, 1, 1);
+        ip.kernelParams = bp.init_params;
+        GPMA_CUDA(cudaGraphExecKernelNodeSetParams(st->exec, st->n_init, &ip));
+        st->init_args[0] = bp.init_levels;
+        st->init_args[1] = bp.init_visited;
+        st->init_args[2] = bp.init_front0;
+        st->init_args[3] = bp.init_ctl;
+        st->init_src = bp.init_src;
+        st->stats.param_updates++;
+    }
+    if (!bp.main.same(st->bfs)) {
+        cudaKernelNodeParams kp = bp.main.node();
+        GPMA_CUDA(cudaGraphExecKernelNodeSetParams(st->exec, st->n_bfs, &kp));
+        st->bfs = bp.main;
+        st->stats.param_updates++;
+    }
+    return GPMA_OK;
+}
+
+}  // namespace
+
+gpma_status step_run(gpma_step *st, const uint64_t *keys, const uint8_t *values, uint64_t n, uint32_t src,
+                     uint32_t *levels, uint64_t *reached, cudaStream_t s) {
+    gpma_graph *g = st->g;
+    g->stats.updates++;
+    g->stats.submitted += n;
+    st->stats.runs++;
+    if (n == 0) {
+        // nothing to update: the step is the BFS alone
+        st->stats.host_runs++;
+        GPMA_TRY(bfs_run(g, src, s, reached));
+    } else {
+        GPMA_TRY(ensure_buffers(g->buf, n, 1));
+        GPMA_TRY(copy_any(g->buf.bkeys[0], keys, n * sizeof(uint64_t), s));
+        GPMA_TRY(copy_any(g->buf.bvals[0], values, n, s));
+        const uint64_t off[2] = {0, n};
+        gpma_graph *gl[1] = {g};
+        size_t tab_bytes = 0;
+        KernelLaunch upd;
+        GPMA_TRY(update_plan(gl, off, 1, g->buf, g->sms, true, &tab_bytes, &upd));
+        BfsPlan bp;
+        const bool profiling = g->profiling;
+        g->profiling = false;  // no per-level stamps inside a recorded step
+        const gpma_status ps = bfs_plan(g, src, &bp);
+        g->profiling = profiling;
+        GPMA_TRY(ps);
+        if (!st->exec || !same_baked(bake(g, tab_bytes, upd, bp), st->baked))
+            GPMA_TRY(build_graph(st, tab_bytes, upd, bp));
+        else
+            GPMA_TRY(refresh_params(st, upd, bp));
+        GPMA_TRY(update_clear(g->buf, s));
+        const unsigned char *stat = st->h_stat + g->buf.parity * g->buf.stat_slot;
+        GPMA_CUDA(cudaEventRecord(st->ev[0], s));
+        GPMA_CUDA(cudaGraphLaunch(st->exec, s));
+        GPMA_CUDA(cudaEventRecord(st->ev[1], s));
+        GPMA_CUDA(cudaStreamSynchronize(s));
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, st->ev[0], st->ev[1]) != cudaSuccess) {
+            cudaGetLastError();
+            ms = 0.f;
+        }
+        st->stats.last_ms = ms;
+        st->stats.total_ms += ms;
+        st->stats.graph_launches++;
+        g->prof.kernel_launches += 3;  // update, BFS init, BFS
+        const bool host_work = update_needs_host(stat, 1);
+        GPMA_TRY(update_finish(gl, 1, g->buf, stat, s, nullptr, 0.0));
+        if (host_work) {
+            // the array changed on the host after the recorded BFS ran: redo it
+            st->stats.host_runs++;
+            GPMA_TRY(bfs_run(g, src, s, reached));
+        } else {
+            GPMA_TRY(bfs_finish(g, reached));
+        }
+    }
+    if (levels) {
+        GPMA_TRY(copy_any(levels, g->bfs_levels, sizeof(uint32_t) * g->row_num, s));
+        GPMA_CUDA(cudaStreamSynchronize(s));
+    }
+    return GPMA_OK;
+}
+
+}  // namespace gpma
+
+extern "C" {
+
+gpma_status gpma_step_create(gpma_graph *g, gpma_step **out) {
+    if (!g || !out) {
+        gpma::set_error("gpma_step_create: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    *out = nullptr;
+    gpma_step *st = new (std::nothrow) gpma_step();
+    if (!st) {
+        gpma::set_error("gpma_step_create: out of host memory");
+        return GPMA_ERR_NOMEM;
+    }
+    st->g = g;
+    for (int i = 0; i < 2; ++i) {
+        cudaError_t e = cudaEventCreate(&st->ev[i]);
+        if (e != cudaSuccess) {
+            gpma_step_destroy(st);
+            return gpma::cuda_fail(e, "cudaEventCreate");
+        }
+    }
+    *out = st;
+    return GPMA_OK;
+}
+
+gpma_status gpma_step_destroy(gpma_step *st) {
+    if (!st)
+        return GPMA_OK;
+    gpma::drop_graph(st);
+    for (int i = 0; i < 2; ++i)
+        if (st->ev[i])
+            cudaEventDestroy(st->ev[i]);
+    if (st->h_stat)
+        cudaFreeHost(st->h_stat);
+    delete st;
+    return GPMA_OK;
+}
+
+gpma_status gpma_step_run(gpma_step *st, const uint64_t *keys, const uint8_t *values, uint64_t n, uint32_t src,
+                          uint32_t *levels, uint64_t *reached, void *stream) {
+    if (!st || (n && (!keys || !values))) {
+        gpma::set_error("gpma_step_run: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    if (n >= (1ull << 30)) {
+        gpma::set_error("gpma_step_run: batch of %llu keys exceeds 2^30", (unsigned long long)n);
+        return GPMA_ERR_CAPACITY;
+    }
+    if (src >= st->g->row_num) {
+        gpma::set_error("gpma_step_run: start node %u out of range (row_num %u)", src, st->g->row_num);
+        return GPMA_ERR_INVALID;
+    }
+    return gpma::step_run(st, keys, values, n, src, levels, reached, (cudaStream_t)stream);
+}
+
+gpma_status gpma_step_get_stats(const gpma_step *st, gpma_step_stats *out) {
+    if (!st || !out) {
+        gpma::set_error("gpma_step_get_stats: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    *out = st->stats;
+    return GPMA_OK;
+}
+
+}  // extern "C"

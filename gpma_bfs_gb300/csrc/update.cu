@@ -1547,11 +1547,10 @@ gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
     return GPMA_OK;
 }
 
-gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32_t k, BatchBuffers &buf, int sms,
-                          cudaStream_t s, bool check_keys, bool profiling, cudaEvent_t *ev, gpma_profile *prof) {
+gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t k, BatchBuffers &buf, int sms,
+                        bool check_keys, size_t *tab_bytes, KernelLaunch *L) {
+    static_assert(sizeof(UpdateArgs) <= KernelLaunch::ARG_BYTES, "update arguments exceed the launch record");
     const uint64_t n = off[k];
-    if (n == 0)
-        return GPMA_OK;
     const int grid = update_grid_size(sms, n);
     if (grid == 0) {
         set_error("update kernel cannot be resident");
@@ -1604,26 +1603,14 @@ gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32
         GPMA_TRY(dev_alloc(&buf.chunk_cnt, chunk_need));
         buf.chunk_cap = chunk_need;
     }
-    // one upload of the tables (up to the last tile offset in use)
-    const size_t tab_bytes = reinterpret_cast<unsigned char *>(h_toff + k + 1) - buf.h_tab;
-    GPMA_CUDA(cudaMemcpyAsync(buf.d_tab, buf.h_tab, tab_bytes, cudaMemcpyHostToDevice, s));
-    if (buf.dirty) {
-        // first launch, new buffers or an aborted launch: clear everything the
-        // kernel otherwise leaves zeroed for its successor
-        GPMA_CUDA(cudaMemsetAsync(buf.d_stat, 0, 2 * buf.stat_slot, s));
-        GPMA_CUDA(cudaMemsetAsync(buf.sort_hist, 0, sizeof(uint32_t) * buf.hist_cap * 2048, s));
-        GPMA_CUDA(cudaMemsetAsync(buf.sort_tiles, 0, 8 * sizeof(uint32_t), s));
-        GPMA_CUDA(cudaMemsetAsync(buf.sort_status, 0, buf.sort_status_cap * sizeof(uint32_t), s));
-        buf.dirty = false;
-    }
+    // the upload covers the tables up to the last tile offset in use
+    *tab_bytes = reinterpret_cast<unsigned char *>(h_toff + k + 1) - buf.h_tab;
     unsigned char *slot = buf.d_stat + buf.parity * buf.stat_slot;
     unsigned char *next = buf.d_stat + (buf.parity ^ 1) * buf.stat_slot;
-    DeviceStatus *d_status = reinterpret_cast<DeviceStatus *>(slot);
-    GraphStatus *d_gs = reinterpret_cast<GraphStatus *>(slot + STAT_GS_OFFSET);
-    prof_mark(profiling, ev, 1, s);
     UpdateArgs A;
+    memset(&A, 0, sizeof(A));  // padding too: launches are compared byte-wise
     A.gd = buf.gd;
-    A.gs = d_gs;
+    A.gs = reinterpret_cast<GraphStatus *>(slot + STAT_GS_OFFSET);
     A.G = k;
     A.max_height = max_height;
     A.boff = buf.boff;
@@ -1652,27 +1639,41 @@ gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32
     A.rvals = buf.rvals;
     A.chunk_cnt = buf.chunk_cnt;
     A.cta_cnt = buf.cta_cnt;
-    A.st = d_status;
+    A.st = reinterpret_cast<DeviceStatus *>(slot);
     A.next_slot = reinterpret_cast<uint32_t *>(next);
     A.next_slot_words = (uint32_t)(buf.stat_slot / sizeof(uint32_t));
     A.hist_words = hist_rows * 2048;
     A.status_words = (uint32_t)status_words;
-    void *params[] = {&A};
-    GPMA_CUDA(cudaLaunchCooperativeKernel(update_kernel_ptr(update_variant(n)), dim3(grid), dim3(BLOCK), params, UPDATE_SMEM,
-                                          s));
-    prof_mark(profiling, ev, 2, s);
-    // one read-back: the status and this launch's per-graph results
-    GPMA_CUDA(cudaMemcpyAsync(buf.h_stat, slot, STAT_GS_OFFSET + sizeof(GraphStatus) * k, cudaMemcpyDeviceToHost, s));
-    GPMA_CUDA(cudaStreamSynchronize(s));
+    L->set(update_kernel_ptr(update_variant(n)), grid, UPDATE_SMEM, &A, sizeof(A));
+    return GPMA_OK;
+}
+
+gpma_status update_clear(BatchBuffers &buf, cudaStream_t s) {
+    if (!buf.dirty)
+        return GPMA_OK;
+    // first launch, new buffers or an aborted launch: clear everything the
+    // kernel otherwise leaves zeroed for its successor
+    GPMA_CUDA(cudaMemsetAsync(buf.d_stat, 0, 2 * buf.stat_slot, s));
+    GPMA_CUDA(cudaMemsetAsync(buf.sort_hist, 0, sizeof(uint32_t) * buf.hist_cap * 2048, s));
+    GPMA_CUDA(cudaMemsetAsync(buf.sort_tiles, 0, 8 * sizeof(uint32_t), s));
+    GPMA_CUDA(cudaMemsetAsync(buf.sort_status, 0, buf.sort_status_cap * sizeof(uint32_t), s));
+    buf.dirty = false;
+    return GPMA_OK;
+}
+
+size_t update_status_bytes(uint32_t k) { return STAT_GS_OFFSET + sizeof(GraphStatus) * k; }
+
+gpma_status update_finish(gpma_graph *const *graphs, uint32_t k, BatchBuffers &buf, const unsigned char *stat,
+                          cudaStream_t s, gpma_profile *prof, double kernel_ms) {
     buf.parity ^= 1;
-    const DeviceStatus &h = *reinterpret_cast<const DeviceStatus *>(buf.h_stat);
-    const GraphStatus *h_gs = reinterpret_cast<const GraphStatus *>(buf.h_stat + STAT_GS_OFFSET);
+    const DeviceStatus &h = *reinterpret_cast<const DeviceStatus *>(stat);
+    const GraphStatus *h_gs = reinterpret_cast<const GraphStatus *>(stat + STAT_GS_OFFSET);
     if (h.err || h.invalid_keys)
         buf.dirty = true;  // the kernel stopped before (or during) its clean-up
     if (prof) {
         prof->kernel_launches += 1;  // the sort runs inside the update kernel
         prof->update_kernels++;
-        prof->update_kernel_ms += prof_elapsed(profiling, ev, 1, 2);
+        prof->update_kernel_ms += kernel_ms;
         // phase split from the kernel's own timeline (stamps of an early exit stay 0)
         const unsigned long long *t = h.stamp;
         auto span = [&](int a, int b) { return (t[a] && t[b] && t[b] >= t[a]) ? (t[b] - t[a]) * 1e-6 : 0.0; };
@@ -1709,6 +1710,36 @@ gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32
                                   s));
     }
     return GPMA_OK;
+}
+
+bool update_needs_host(const unsigned char *stat, uint32_t k) {
+    const DeviceStatus &h = *reinterpret_cast<const DeviceStatus *>(stat);
+    const GraphStatus *h_gs = reinterpret_cast<const GraphStatus *>(stat + STAT_GS_OFFSET);
+    if (h.err || h.invalid_keys || h.significant)
+        return true;
+    for (uint32_t i = 0; i < k; ++i)
+        if (h_gs[i].remaining > 0)
+            return true;
+    return false;
+}
+
+gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32_t k, BatchBuffers &buf, int sms,
+                          cudaStream_t s, bool check_keys, bool profiling, cudaEvent_t *ev, gpma_profile *prof) {
+    if (off[k] == 0)
+        return GPMA_OK;
+    size_t tab_bytes = 0;
+    KernelLaunch L;
+    GPMA_TRY(update_plan(graphs, off, k, buf, sms, check_keys, &tab_bytes, &L));
+    GPMA_CUDA(cudaMemcpyAsync(buf.d_tab, buf.h_tab, tab_bytes, cudaMemcpyHostToDevice, s));
+    GPMA_TRY(update_clear(buf, s));
+    prof_mark(profiling, ev, 1, s);
+    GPMA_CUDA(L.launch_cooperative(s));
+    prof_mark(profiling, ev, 2, s);
+    // one read-back: the status and this launch's per-graph results
+    GPMA_CUDA(cudaMemcpyAsync(buf.h_stat, buf.d_stat + buf.parity * buf.stat_slot, update_status_bytes(k),
+                              cudaMemcpyDeviceToHost, s));
+    GPMA_CUDA(cudaStreamSynchronize(s));
+    return update_finish(graphs, k, buf, buf.h_stat, s, prof, prof ? prof_elapsed(profiling, ev, 1, 2) : 0.0);
 }
 
 // Single-graph update of the n-key batch staged in g->buf.bkeys[0]/bvals[0].

@@ -119,6 +119,35 @@ GPMA_API gpma_status gpma_bfs_multi(gpma_graph *g, const uint32_t *srcs, uint32_
 GPMA_API gpma_status gpma_bfs_noalloc(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached,
                                       void *stream);
 
+/* ---- recorded update+BFS steps ------------------------------------------------
+ * One slide step of the reference's demo loop (gpma_bfs_demo.cu: update_gpma
+ * of the step's batch, then gpma_bfs from a source) whose device work is
+ * recorded once as a CUDA graph and replayed for every later step: table
+ * upload, update kernel, BFS clears and kernels, status read-back, one host
+ * synchronisation. The graph is rebuilt only when a buffer or the launch
+ * shape it holds changes; batch size and source may differ per step.
+ * gpma_step_run gives exactly the results of gpma_update(keys, values, n)
+ * followed by gpma_bfs(src, levels, reached) (levels may be NULL: the levels
+ * stay in the library; keys, values and levels may be host or device
+ * memory). When the update needs host work (root resize, the bulk rebuild of
+ * a large batch) the step finishes on the host and runs the BFS again.
+ * Destroy a step before its graph. No reference counterpart. */
+typedef struct gpma_step gpma_step;
+typedef struct gpma_step_stats {
+    uint64_t runs;           /* gpma_step_run calls */
+    uint64_t graph_launches; /* steps replayed as one graph launch */
+    uint64_t builds;         /* graph (re)builds */
+    uint64_t param_updates;  /* kernel nodes whose arguments were updated in place */
+    uint64_t host_runs;      /* steps whose BFS ran outside the graph (empty batch, root resize, bulk rebuild) */
+    double last_ms;          /* device time of the last graph launch (CUDA events) */
+    double total_ms;         /* summed over graph launches */
+} gpma_step_stats;
+GPMA_API gpma_status gpma_step_create(gpma_graph *g, gpma_step **out);
+GPMA_API gpma_status gpma_step_destroy(gpma_step *st);
+GPMA_API gpma_status gpma_step_run(gpma_step *st, const uint64_t *keys, const uint8_t *values, uint64_t n,
+                                   uint32_t src, uint32_t *levels, uint64_t *reached, void *stream);
+GPMA_API gpma_status gpma_step_get_stats(const gpma_step *st, gpma_step_stats *out);
+
 /* ---- analytics on the same array --------------------------------------------
  * No reference counterpart (the reference's only analytic is the BFS). Both
  * sweep every slot of the gapped array once per iteration; an edge is a

@@ -1,0 +1,97 @@
+"""Recorded update+BFS steps (CUDA graph replay) give exactly what
+update_gpma followed by gpma_bfs gives, step by step: levels, reachable
+count and the whole layout, through root resizes, batch-size and source
+changes, empty batches, host and device buffers, and a rejected batch."""
+import numpy as np
+import pytest
+
+from oracle.oracle import OracleGPMA
+
+pytestmark = pytest.mark.gpu
+
+
+def _same_layout(a, b):
+    return all(np.array_equal(x, y) for x, y in zip(a.export_layout(), b.export_layout()))
+
+
+def test_step_matches_update_then_bfs(built_lib):
+    import torch
+
+    import gpma_bfs_gb300 as G
+
+    scale = 12
+    n = 1 << scale
+    src, dst = G.gen_rmat(scale, 8, seed=31)
+    keys = G.edges_to_keys(src, dst)
+    rng = np.random.default_rng(5)
+    keys = keys[rng.permutation(len(keys))]
+    half = len(keys) // 2
+    eager, graphed = G.GPMA(n), G.GPMA(n)
+    o = OracleGPMA(n, threads=2)
+    step = G.Step(graphed)
+    ones = np.ones(half, np.uint8)
+    # the first step grows the array from the guards alone: root resize on the host
+    G.update_gpma(eager, keys[:half], ones)
+    want, want_r = G.gpma_bfs(eager, n, 0, 0)
+    got = np.zeros(n, np.uint32)
+    r = step.run(keys[:half], ones, 0, got)
+    o.update(keys[:half], ones)
+    assert r == want_r and np.array_equal(got, want) and _same_layout(eager, graphed)
+    assert step.stats()["host_runs"] >= 1
+    # sliding window: batch sizes and sources vary, host and device buffers
+    lo, hi = 0, half
+    dev_levels = torch.zeros(n, dtype=torch.int32, device="cuda")
+    for i in range(14):
+        w = [300, 300, 301, 1200, 64, 0, 300][i % 7]
+        ins, dele = keys[hi: hi + w], keys[lo: lo + w]
+        lo, hi = lo + w, hi + w
+        k = np.concatenate([ins, dele])
+        v = np.concatenate([np.ones(len(ins), np.uint8), np.zeros(len(dele), np.uint8)])
+        s0 = int(keys[hi - 1] >> np.uint64(32)) if i % 3 else 0
+        G.update_gpma(eager, k, v)
+        want, want_r = G.gpma_bfs(eager, n, 0, s0)
+        o.update(k, v)
+        if i % 2:
+            kd = torch.from_numpy(k.view(np.int64)).cuda()
+            vd = torch.from_numpy(v).cuda()
+            r = step.run(kd, vd, s0, dev_levels)
+            got = dev_levels.cpu().numpy().view(np.uint32)
+        else:
+            got = np.zeros(n, np.uint32)
+            r = step.run(k, v, s0, got)
+        assert r == want_r and np.array_equal(got, want), f"step {i}"
+        assert _same_layout(eager, graphed), f"step {i}"
+        ol, orr = o.bfs(s0)
+        assert np.array_equal(got, ol) and r == orr, f"step {i} against the oracle"
+    st = step.stats()
+    assert st["runs"] == 15 and st["graph_launches"] >= 10 and st["param_updates"] > 0
+    assert st["builds"] >= 1 and st["last_ms"] > 0
+    # levels=None keeps them inside the library; the count still matches
+    assert step.run(keys[:0], ones[:0], 0) == G.gpma_bfs(eager, n, 0, 0)[1]
+    step.close()
+    eager.close()
+    graphed.close()
+
+
+def test_step_rejected_batch_then_recovers(built_lib):
+    import gpma_bfs_gb300 as G
+
+    n = 1 << 10
+    src, dst = G.gen_rmat(10, 8, seed=7)
+    keys = G.edges_to_keys(src, dst)
+    eager, graphed = G.GPMA(n), G.GPMA(n)
+    ones = np.ones(len(keys), np.uint8)
+    G.update_gpma(eager, keys, ones)
+    with G.Step(graphed) as step:
+        step.run(keys, ones, 0)
+        bad = np.array([(3 << 32) | 0xFFFFFFFF], np.uint64)  # reserved column
+        with pytest.raises(G.GPMAError):
+            step.run(bad, np.ones(1, np.uint8), 0)
+        k = keys[:50]
+        G.update_gpma(eager, k, np.zeros(50, np.uint8))
+        want, want_r = G.gpma_bfs(eager, n, 0, 1)
+        got = np.zeros(n, np.uint32)
+        assert step.run(k, np.zeros(50, np.uint8), 1, got) == want_r
+        assert np.array_equal(got, want) and _same_layout(eager, graphed)
+    eager.close()
+    graphed.close()
