@@ -149,6 +149,25 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's figure; every rank calls it (NCCL on the GPUs, gloo
+    with device="cpu")."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank: float, time_s: float, world: int) -> float:
+    """Whole-job throughput of N replicas: all ranks' units over the slowest
+    rank's time (time_s already reduced with max_over_ranks)."""
+    return units_per_rank * world / time_s
+
+
 def live_out_degree_sum(g, levels):
     """Edges traversed by a BFS: live out-edges of the reached nodes."""
     keys, vals, ro = g.export_layout()
@@ -232,14 +251,10 @@ def run_gpu(args):
     step_ms = [a.elapsed_time(b) for a, b in ev]
     prof = g.profile()
     st1 = g.stats()
-    time_s = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([time_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        time_s = float(t.item())
+    time_s = max_over_ranks(sum(step_ms) / 1e3, world)
     batch = 2 * step
     updates = batch * args.steps * world
-    value = updates / time_s
+    value = replica_value(batch * args.steps, time_s, world)
     accepted_slots = (st1["accepted_slots"] - st0["accepted_slots"]) / args.steps
 
     # roofline of the dominant kernel (the persistent update kernel):
@@ -271,11 +286,7 @@ def run_gpu(args):
         G.update_gpma(g, hk[j], hv[j], stream)
         b.record(stream)
     torch.cuda.synchronize()
-    e2e_s = sum(a.elapsed_time(b) for a, b in e2e_ev) / 1e3
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(sum(a.elapsed_time(b) for a, b in e2e_ev) / 1e3, world)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -24,7 +24,7 @@ import numpy as np
 __all__ = [
     "GPMA", "GPMAError", "update_gpma", "gpma_bfs", "gpma_bfs_multi", "lib", "library_path",
     "KEY_NONE", "KEY_MAX", "COL_IDX_NONE", "VALUE_NONE", "gen_rmat", "gen_chung_lu", "edges_to_keys",
-    "read_edges_text", "write_edges_text", "Step",
+    "read_edges_text", "write_edges_text", "Step", "partition_rows", "shard_first_row",
 ]
 
 KEY_NONE = 0xFFFFFFFFFFFFFFFF  # gpma.cuh:15
@@ -166,6 +166,8 @@ def lib() -> ctypes.CDLL:
         "gpma_pagerank": (st, [P, ctypes.c_float, u32, ctypes.c_double, P, ctypes.POINTER(u32), P]),
         "gpma_components": (st, [P, P, ctypes.POINTER(u64), ctypes.POINTER(u32), P]),
         "gpma_load": (st, [ctypes.c_char_p, P, ctypes.POINTER(P)]),
+        "gpma_shard_first_row": (u32, [u32, u32, u32]),
+        "gpma_partition_rows": (st, [P, P, u64, u32, u32, ctypes.c_int, P, P, P]),
         "gpma_step_create": (st, [P, ctypes.POINTER(P)]),
         "gpma_step_destroy": (st, [P]),
         "gpma_step_run": (st, [P, P, P, u64, u32, P, ctypes.POINTER(u64), P]),
@@ -399,6 +401,28 @@ def gpma_bfs(gpma: GPMA, node_size: int, edge_size: int, start_node: int, result
     _check(lib().gpma_bfs(gpma.handle, int(start_node), rp, ctypes.byref(reached), _stream_ptr(stream)), "gpma_bfs")
     del keep
     return results, reached.value
+
+
+def shard_first_row(row_num: int, shards: int, s: int) -> int:
+    """First row of shard s when row_num rows are split into `shards` row
+    ranges (floor(row_num * s / shards))."""
+    return int(lib().gpma_shard_first_row(row_num, shards, s))
+
+
+def partition_rows(keys, values, row_num: int, shards: int, rebase: bool = True):
+    """Orders a host batch by the row-range shard of each key's source row,
+    stably; returns (keys, values, offsets) with shard s's part at
+    offsets[s]:offsets[s+1]. With rebase the source rows become shard-local.
+    The exchange step a graph sharded by row range needs per update."""
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    values = np.ascontiguousarray(values, dtype=np.uint8)
+    if len(keys) != len(values):
+        raise ValueError("Inconsistant kv size.")
+    ok, ov = np.empty_like(keys), np.empty_like(values)
+    off = np.zeros(shards + 1, np.uint64)
+    _check(lib().gpma_partition_rows(keys.ctypes.data, values.ctypes.data, len(keys), row_num, shards, int(rebase),
+                                     ok.ctypes.data, ov.ctypes.data, off.ctypes.data), "gpma_partition_rows")
+    return ok, ov, off
 
 
 class Step:

@@ -430,3 +430,50 @@ gpma_status gpma_read_edges_bin(const char *path, uint32_t *n_out, uint64_t *m_o
     fclose(f);
     return bad ? GPMA_ERR_IO : GPMA_OK;
 }
+
+/* ---- row-range shards ------------------------------------------------------- */
+
+uint32_t gpma_shard_first_row(uint32_t row_num, uint32_t shards, uint32_t s) {
+    if (shards == 0)
+        return 0;
+    if (s > shards)
+        s = shards;
+    return (uint32_t)(((uint64_t)row_num * s) / shards);
+}
+
+/* Shard owning row r: the largest s with first_row(s) <= r, i.e.
+ * floor(row_num * s / shards) <= r  <=>  s <= ((r + 1) * shards - 1) / row_num. */
+static uint32_t shard_of_row(uint32_t r, uint32_t row_num, uint32_t shards) {
+    return (uint32_t)((((uint64_t)r + 1) * shards - 1) / row_num);
+}
+
+gpma_status gpma_partition_rows(const uint64_t *keys, const uint8_t *values, uint64_t n, uint32_t row_num,
+                                uint32_t shards, int rebase, uint64_t *out_keys, uint8_t *out_values,
+                                uint64_t *offsets) {
+    if (shards == 0 || row_num == 0 || !offsets || (n && (!keys || !values || !out_keys || !out_values)))
+        return GPMA_ERR_INVALID;
+    for (uint32_t s = 0; s <= shards; ++s)
+        offsets[s] = 0;
+    for (uint64_t i = 0; i < n; ++i) {
+        const uint32_t r = (uint32_t)(keys[i] >> 32);
+        if ((keys[i] >> 32) >= row_num)
+            return GPMA_ERR_INVALID;
+        offsets[shard_of_row(r, row_num, shards) + 1]++;
+    }
+    for (uint32_t s = 0; s < shards; ++s)
+        offsets[s + 1] += offsets[s];
+    uint64_t *cur = (uint64_t *)malloc(sizeof(uint64_t) * shards);
+    if (!cur)
+        return GPMA_ERR_NOMEM;
+    memcpy(cur, offsets, sizeof(uint64_t) * shards);
+    for (uint64_t i = 0; i < n; ++i) {
+        const uint32_t r = (uint32_t)(keys[i] >> 32);
+        const uint32_t s = shard_of_row(r, row_num, shards);
+        const uint64_t base = rebase ? gpma_shard_first_row(row_num, shards, s) : 0;
+        const uint64_t o = cur[s]++;
+        out_keys[o] = ((uint64_t)(r - base) << 32) | (keys[i] & 0xFFFFFFFFull);
+        out_values[o] = values[i];
+    }
+    free(cur);
+    return GPMA_OK;
+}

@@ -426,6 +426,22 @@ GPMA_API gpma_status gpma_write_edges_bin(const char *path, uint32_t n, const ui
 GPMA_API gpma_status gpma_read_edges_bin(const char *path, uint32_t *n_out, uint64_t *m_out, uint32_t *src,
                                          uint32_t *dst, uint64_t capacity);
 
+/* ---- row-range shards (host) --------------------------------------------------
+ * No reference counterpart. One graph split by source-row range: shard s of
+ * `shards` owns rows [gpma_shard_first_row(s), gpma_shard_first_row(s + 1)),
+ * first_row(s) = floor(row_num * s / shards). An update batch reaches its
+ * shards through one exchange step: gpma_partition_rows orders a host batch
+ * by the shard of each key's source row, stably (input order within a shard),
+ * into out_keys / out_values, with offsets[s]..offsets[s+1] the part of shard
+ * s (shards + 1 entries). With rebase != 0 the source row becomes
+ * shard-local (row - first_row(s)), so each shard is an ordinary graph of
+ * its own rows; destinations stay global. A key whose source row is >=
+ * row_num fails the call with GPMA_ERR_INVALID. */
+GPMA_API uint32_t gpma_shard_first_row(uint32_t row_num, uint32_t shards, uint32_t s);
+GPMA_API gpma_status gpma_partition_rows(const uint64_t *keys, const uint8_t *values, uint64_t n, uint32_t row_num,
+                                         uint32_t shards, int rebase, uint64_t *out_keys, uint8_t *out_values,
+                                         uint64_t *offsets);
+
 /* ---- snapshot ----------------------------------------------------------------
  * No reference counterpart. gpma_save writes the whole structure (geometry,
  * keys, values, row_offset) with a checksum; gpma_load creates a graph on the
