@@ -166,6 +166,7 @@ def lib() -> ctypes.CDLL:
         "gpma_pagerank": (st, [P, ctypes.c_float, u32, ctypes.c_double, P, ctypes.POINTER(u32), P]),
         "gpma_components": (st, [P, P, ctypes.POINTER(u64), ctypes.POINTER(u32), P]),
         "gpma_load": (st, [ctypes.c_char_p, P, ctypes.POINTER(P)]),
+        "gpma_validate": (st, [P, ctypes.POINTER(u64), P]),
         "gpma_shard_first_row": (u32, [u32, u32, u32]),
         "gpma_partition_rows": (st, [P, P, u64, u32, u32, ctypes.c_int, P, P, P]),
         "gpma_step_create": (st, [P, ctypes.POINTER(P)]),
@@ -292,6 +293,13 @@ class GPMA:
     @property
     def upper_element(self) -> np.ndarray:
         return self.thresholds()[1]
+
+    def validate(self, stream=None) -> int:
+        """Segments whose cached first key differs from the array (0 when
+        the structure is consistent)."""
+        bad = ctypes.c_uint64()
+        _check(lib().gpma_validate(self.handle, ctypes.byref(bad), _stream_ptr(stream)), "gpma_validate")
+        return bad.value
 
     def export_layout(self, stream=None) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
         """(keys, masked values, row_offset) as host arrays."""

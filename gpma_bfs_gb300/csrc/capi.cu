@@ -62,6 +62,7 @@ gpma_status copy_in(gpma_graph *g, void *dst_dev, const void *src, size_t bytes,
 void release(gpma_graph *g) {
     dev_free(g->keys);
     dev_free(g->values);
+    dev_free(g->heads);
     dev_free(g->row_offset);
     dev_free(g->skeys);
     dev_free(g->svals);
@@ -238,6 +239,7 @@ gpma_status gpma_create(uint32_t row_num, void *stream, gpma_graph **out) {
         g->geo.seg = 2;
         g->geo.height = 1;
         recalculate_density(g->geo);
+        GPMA_TRY(refresh_heads(g, s));
         if (row_num == 0)
             return GPMA_OK;
         GPMA_TRY(ensure_buffers(g->buf, row_num, 1));
@@ -299,6 +301,14 @@ gpma_status gpma_bfs(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *re
     GPMA_TRY(copy_any(levels, g->bfs_levels, sizeof(uint32_t) * g->row_num, s));
     GPMA_CUDA(cudaStreamSynchronize(s));
     return GPMA_OK;
+}
+
+gpma_status gpma_validate(gpma_graph *g, uint64_t *bad, void *stream) {
+    if (!g || !bad) {
+        set_error("gpma_validate: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    return count_bad_heads(g, (cudaStream_t)stream, bad);
 }
 
 gpma_status gpma_bfs_noalloc(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached, void *stream) {
@@ -773,6 +783,7 @@ gpma_status gpma_load(const char *path, void *stream, gpma_graph **out) {
         GPMA_CUDA(cudaMemcpyAsync(g->keys, keys.data(), size * 8ull, cudaMemcpyHostToDevice, s));
         GPMA_CUDA(cudaMemcpyAsync(g->values, payload.data() + size * 8ull, size, cudaMemcpyHostToDevice, s));
         GPMA_CUDA(cudaMemcpyAsync(g->row_offset, ro.data(), ro_n * 4, cudaMemcpyHostToDevice, s));
+        GPMA_TRY(refresh_heads(g, s));
         GPMA_CUDA(cudaStreamSynchronize(s));
         return GPMA_OK;
     }();

@@ -80,6 +80,7 @@ struct GraphDesc {
     uint32_t *row_offset;
     uint64_t *skeys;  // scratch of `size` slots
     uint8_t *svals;
+    uint64_t *heads;  // heads[s] == keys[s * seg]: the keys the locate descent compares
     uint32_t row_num, size, seg, log2seg, height;
     uint32_t pad[3];
     uint32_t lower[MAX_LEVELS];
@@ -171,6 +172,8 @@ struct gpma_graph {
     uint64_t *skeys = nullptr;        // scratch for wide windows and resizes
     uint8_t *svals = nullptr;
     uint32_t *chunk_cnt = nullptr;    // scratch_cap / CHUNK + 2 entries (root rebuild)
+    uint64_t *heads = nullptr;        // first key of every segment (size / seg entries), kept by every writer
+    uint32_t heads_cap = 0;
     gpma::BatchBuffers buf;           // single-graph update buffers
     // BFS state
     uint32_t bfs_cap = 0;
@@ -323,6 +326,11 @@ struct KernelLaunch {
 gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs);
 void free_buffers(BatchBuffers &b);
 gpma_status ensure_scratch(gpma_graph *g, uint32_t slots);
+// Recomputes heads[s] = keys[s * seg] over the whole array (after the array
+// was written outside the level loop: creation, root rebuild, load).
+gpma_status refresh_heads(gpma_graph *g, cudaStream_t s);
+// Segments whose heads entry differs from the array (0 when consistent).
+gpma_status count_bad_heads(gpma_graph *g, cudaStream_t s, uint64_t *bad);
 // One launch updating graphs[0..k) with the batches already staged in
 // buf.bkeys[0]/bvals[0] at offsets off[0..k]. Graphs must be ordered by
 // segment length. check_keys=false only for the internal guard insertion.

@@ -176,14 +176,17 @@ __device__ __forceinline__ void locate_keys(const UpdateArgs &A, const uint64_t 
             }
         }
     }
-    // the remaining levels of the reference's descent (gpma.cuh:209-216), interleaved
+    // the remaining levels of the reference's descent (gpma.cuh:209-216),
+    // interleaved. Every probed slot starts a segment (prefix and bit are
+    // multiples of seg), so its key is read from the dense heads array.
     for (;;) {
         uint64_t probe[LOC_ILP];
         bool any = false;
 #pragma unroll
         for (int j = 0; j < LOC_ILP; ++j) {
-            const bool live = idx[j] < A.n && A.gd[g[j]].seg <= bit[j];
-            probe[j] = live ? A.gd[g[j]].keys[prefix[j] | bit[j]] : 0;
+            const GraphDesc &D = A.gd[g[j]];
+            const bool live = idx[j] < A.n && D.seg <= bit[j];
+            probe[j] = live ? D.heads[(prefix[j] | bit[j]) >> D.log2seg] : 0;
             any |= live;
         }
         if (!any)
@@ -239,8 +242,8 @@ __device__ __forceinline__ void cta_prefix(const uint32_t *cnt, uint32_t &base, 
 // (s, lane) gets element first(s)+lane of the stable merge of live[0..L) and
 // pend[0..P) (ties: live first), or gap_key/0 if the segment holds fewer.
 // len is a multiple of the segment length; mk/mv hold len entries.
-__device__ void redispatch_chunk(uint64_t *keys, uint8_t *vals, uint32_t *row_offset, uint32_t row_num, uint32_t node,
-                                 uint32_t log2seg, uint32_t log2F, uint32_t t0, uint32_t len, const uint64_t *lk,
+__device__ void redispatch_chunk(uint64_t *keys, uint8_t *vals, uint64_t *heads, uint32_t *row_offset,
+                                 uint32_t row_num, uint32_t node, uint32_t log2seg, uint32_t log2F, uint32_t t0, uint32_t len, const uint64_t *lk,
                                  const uint8_t *lv, uint32_t L, const uint64_t *pk, const uint8_t *pv, uint32_t P,
                                  uint64_t gap_key, uint64_t *mk, uint8_t *mv) {
     const uint64_t M = (uint64_t)L + P;
@@ -289,6 +292,8 @@ __device__ void redispatch_chunk(uint64_t *keys, uint8_t *vals, uint32_t *row_of
         }
         keys[node + slot] = k;
         vals[node + slot] = v;
+        if (ln == 0)
+            heads[(node + slot) >> log2seg] = k;
         if (is_guard(k)) {
             uint32_t row = (uint32_t)(k >> 32);
             if (row < row_num)
@@ -449,6 +454,8 @@ __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
                     k[j] = mk[f0 + ln];
                     v[j] = mv[f0 + ln];
                 }
+                if (ln == 0)
+                    D.heads[(node >> log2seg) + s] = k[j];
                 if (is_guard(k[j])) {
                     const uint32_t row = (uint32_t)(k[j] >> 32);
                     if (row < D.row_num)
@@ -549,6 +556,8 @@ __device__ void cta_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32_
                 }
                 D.keys[node + t] = k;
                 D.vals[node + t] = v;
+                if (ln == 0)
+                    D.heads[(node + t) >> log2seg] = k;
                 if (is_guard(k)) {
                     uint32_t row = (uint32_t)(k >> 32);
                     if (row < D.row_num)
@@ -651,7 +660,7 @@ __device__ bool grid_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
         const GraphDesc &D = A.gd[L.graph[w]];
         const uint32_t node = L.node[w], a = L.a[w];
         const uint32_t log2F = (31 - __clz(W)) - D.log2seg;
-        redispatch_chunk(D.keys, D.vals, D.row_offset, D.row_num, node, D.log2seg, log2F, k * CHUNK, CHUNK,
+        redispatch_chunk(D.keys, D.vals, D.heads, D.row_offset, D.row_num, node, D.log2seg, log2F, k * CHUNK, CHUNK,
                          D.skeys + node, D.svals + node, A.wlive[w], pk + a, pv + a, L.b[w] - a, KEY_NONE, mk, mv);
     }
     return true;
@@ -753,9 +762,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             const uint32_t segs = D.size >> D.log2seg;
             const uint32_t cached = segs < LOCATE_CACHE ? segs : LOCATE_CACHE;
             log2stride = 31 - __clz(D.size / cached);
+            const uint32_t hstep = log2stride - D.log2seg;  // stride >= seg
             uint64_t *f = reinterpret_cast<uint64_t *>(smem);
             for (uint32_t j = threadIdx.x; j < cached; j += BLOCK)
-                f[j] = D.keys[(size_t)j << log2stride];
+                f[j] = D.heads[(size_t)j << hstep];
             __syncthreads();
             fk = f;
         }
@@ -1249,6 +1259,20 @@ __global__ void compacted_layout_kernel(uint64_t *keys, uint8_t *vals, uint32_t 
     }
 }
 
+__global__ void heads_kernel(const uint64_t *keys, uint64_t *heads, uint32_t segs, uint32_t log2seg) {
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < segs; s += gridDim.x * blockDim.x)
+        heads[s] = keys[(size_t)s << log2seg];
+}
+
+__global__ void heads_check_kernel(const uint64_t *keys, const uint64_t *heads, uint32_t segs, uint32_t log2seg,
+                                   unsigned long long *bad) {
+    unsigned long long c = 0;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < segs; s += gridDim.x * blockDim.x)
+        c += heads[s] != keys[(size_t)s << log2seg];
+    if (c)
+        atomicAdd(bad, c);
+}
+
 int grid_for(uint64_t work, int sms, int per_sm) {
     uint64_t g = (work + BLOCK - 1) / BLOCK;
     return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, (uint64_t)sms * per_sm));
@@ -1350,8 +1374,9 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k
         g->stats.root_resizes++;
     }
     GPMA_CUDA(cudaGetLastError());
-    prof_mark(g, 1, s);
     g->geo = geo;
+    GPMA_TRY(refresh_heads(g, s));
+    prof_mark(g, 1, s);
     GPMA_CUDA(cudaStreamSynchronize(s));
     g->prof.rebuild_ms += prof_elapsed(g, 0, 1);
     // the scratch must cover the whole array for later wide windows
@@ -1366,6 +1391,7 @@ GraphDesc describe(const gpma_graph *g) {
     d.row_offset = g->row_offset;
     d.skeys = g->skeys;
     d.svals = g->svals;
+    d.heads = g->heads;
     d.row_num = g->row_num;
     d.size = g->geo.size;
     d.seg = g->geo.seg;
@@ -1394,6 +1420,40 @@ const void *update_kernel_ptr(int variant) {
 }
 
 }  // namespace
+
+gpma_status refresh_heads(gpma_graph *g, cudaStream_t s) {
+    const uint32_t log2seg = fls32(g->geo.seg) - 1;
+    const uint32_t segs = g->geo.size >> log2seg;
+    if (segs > g->heads_cap || !g->heads) {
+        dev_free(g->heads);
+        g->heads_cap = 0;
+        GPMA_TRY(dev_alloc(&g->heads, segs));
+        g->heads_cap = segs;
+    }
+    heads_kernel<<<grid_for(segs, g->sms, 8), BLOCK, 0, s>>>(g->keys, g->heads, segs, log2seg);
+    GPMA_CUDA(cudaGetLastError());
+    g->prof.kernel_launches += 1;
+    return GPMA_OK;
+}
+
+gpma_status count_bad_heads(gpma_graph *g, cudaStream_t s, uint64_t *bad) {
+    const uint32_t log2seg = fls32(g->geo.seg) - 1;
+    const uint32_t segs = g->geo.size >> log2seg;
+    unsigned long long *d = nullptr;
+    GPMA_TRY(dev_alloc(&d, 1));
+    gpma_status st = [&]() -> gpma_status {
+        GPMA_CUDA(cudaMemsetAsync(d, 0, sizeof(*d), s));
+        heads_check_kernel<<<grid_for(segs, g->sms, 8), BLOCK, 0, s>>>(g->keys, g->heads, segs, log2seg, d);
+        GPMA_CUDA(cudaGetLastError());
+        unsigned long long h = 0;
+        GPMA_CUDA(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
+        GPMA_CUDA(cudaStreamSynchronize(s));
+        *bad = h;
+        return GPMA_OK;
+    }();
+    dev_free(d);
+    return st;
+}
 
 Tuning g_tuning;
 

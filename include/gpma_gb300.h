@@ -334,6 +334,12 @@ GPMA_API gpma_status gpma_device_arrays(gpma_graph *g, const uint64_t **keys, co
 
 GPMA_API gpma_status gpma_get_stats(const gpma_graph *g, gpma_stats *out);
 
+/* Consistency check (no reference counterpart). The locate search compares
+ * keys at segment starts, read from a dense copy that every writer of the
+ * array keeps (one key per segment); *bad receives the number of segments
+ * whose copy differs from the array: 0 for a consistent structure. */
+GPMA_API gpma_status gpma_validate(gpma_graph *g, uint64_t *bad, void *stream);
+
 /* ---- profiling -------------------------------------------------------------
  * With profiling on, CUDA events recorded on the caller's stream time each
  * phase; times accumulate until gpma_reset_profile. kernel_launches counts

@@ -138,6 +138,7 @@ def test_batched_sliding_windows_mixed_segment_lengths(built_lib):
         for i in range(len(specs)):
             x, y = gb[i].export_layout(), gp[i].export_layout()
             assert all(np.array_equal(p, q) for p, q in zip(x, y)), f"step {step} graph {i}"
+            assert gb[i].validate() == 0 and gp[i].validate() == 0, f"step {step} graph {i}: segment heads"
     for i in rng.choice(len(specs), 4, replace=False):
         orc = OracleGPMA(specs[i][0], threads=4)
         for k, v in history[i]:

@@ -39,6 +39,7 @@ def _compare_full(gpu, orc, ctx):
     assert np.array_equal(gk, ok), ctx + ": key layout"
     assert np.array_equal(gv, ov), ctx + ": values"
     assert np.array_equal(gr, orow), ctx + ": row_offset"
+    assert gpu.g.validate() == 0, ctx + ": segment heads differ from the array"
 
 
 @pytest.mark.parametrize("seed", range(100, 112))

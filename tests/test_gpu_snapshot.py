@@ -26,6 +26,7 @@ def test_save_load_resume_is_layout_exact(built_lib, tmp_path):
     assert r.geometry() == g.geometry() and r.row_num == n
     assert all(np.array_equal(x, y) for x, y in zip(r.thresholds(), g.thresholds()))
     assert all(np.array_equal(x, y) for x, y in zip(r.export_layout(), g.export_layout()))
+    assert r.validate() == 0
     rest = keys[len(keys) // 2:]
     for i in range(0, len(rest), 3000):
         k = rest[i:i + 3000]
