@@ -71,6 +71,7 @@ struct UpdateArgs {
     GraphStatus *gs;
     uint32_t G;
     uint32_t max_height;
+    uint32_t min_height;    // below it no graph has a root window
     const uint32_t *boff;   // batch offsets, G + 1
     const uint32_t *toff;   // sort tile offsets, G + 1
     uint32_t n;
@@ -973,6 +974,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         uint32_t nw_next, base_i, total_i;
         cta_prefix(CNT(scan_id), base, nw_next, tmp);
         cta_prefix(CNTI(scan_id), base_i, total_i, tmp);
+        if (nw_next == 0 && level < A.min_height) {
+            // every window of this level was accepted and none can be a root
+            // window: nothing to carry, no next level (counted as the loop's
+            // own exit would count it)
+            nw = 0;
+            ++level;
+            break;
+        }
         for (uint32_t w0 = lo; w0 < hi; w0 += BLOCK) {
             const uint32_t w = w0 + threadIdx.x;
             const bool rej = w < hi && !A.wflag[w];
@@ -1624,11 +1633,12 @@ gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t
     GraphDesc *h_gd = reinterpret_cast<GraphDesc *>(buf.h_tab);
     uint32_t *h_boff = reinterpret_cast<uint32_t *>(buf.h_tab + sizeof(GraphDesc) * buf.gcap);
     uint32_t *h_toff = h_boff + buf.gcap + 1;
-    uint32_t max_height = 0;
+    uint32_t max_height = 0, min_height = UINT32_MAX;
     uint64_t chunk_need = 1;
     for (uint32_t i = 0; i < k; ++i) {
         h_gd[i] = describe(graphs[i]);
         max_height = std::max(max_height, graphs[i]->geo.height);
+        min_height = std::min(min_height, graphs[i]->geo.height);
         chunk_need += graphs[i]->geo.size / CHUNK + 1;
         if (i > 0 && graphs[i]->geo.seg < graphs[i - 1]->geo.seg) {
             set_error("update_graphs: graphs must be ordered by segment length");
@@ -1673,6 +1683,7 @@ gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t
     A.gs = reinterpret_cast<GraphStatus *>(slot + STAT_GS_OFFSET);
     A.G = k;
     A.max_height = max_height;
+    A.min_height = min_height;
     A.boff = buf.boff;
     A.toff = buf.toff;
     A.n = (uint32_t)n;
