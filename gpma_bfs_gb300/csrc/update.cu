@@ -151,8 +151,11 @@ __device__ __forceinline__ uint32_t leaf_find(const GraphDesc &D, uint32_t leaf,
 // LOC_ILP dependent chains in flight instead of one.
 constexpr int LOC_ILP = 4;
 
-__device__ __forceinline__ void locate_keys(const UpdateArgs &A, const uint64_t *bk, const uint8_t *bv,
-                                            uint32_t i0, uint32_t stride, const uint64_t *fk, uint32_t log2stride) {
+// Keys i0 + j * stride (j < LOC_ILP) below `end`; returns how many of them
+// are insertions (leaf set).
+__device__ __forceinline__ uint32_t locate_keys(const UpdateArgs &A, const uint64_t *bk, const uint8_t *bv,
+                                                uint32_t i0, uint32_t stride, uint32_t end, const uint64_t *fk,
+                                                uint32_t log2stride) {
     uint32_t idx[LOC_ILP], prefix[LOC_ILP], bit[LOC_ILP], g[LOC_ILP];
     uint64_t key[LOC_ILP];
 #pragma unroll
@@ -162,7 +165,7 @@ __device__ __forceinline__ void locate_keys(const UpdateArgs &A, const uint64_t 
         bit[j] = 0;
         g[j] = 0;
         key[j] = 0;
-        if (idx[j] < A.n) {
+        if (idx[j] < end) {
             g[j] = graph_of(A, idx[j]);
             const GraphDesc &D = A.gd[g[j]];
             key[j] = bk[idx[j]];
@@ -186,7 +189,7 @@ __device__ __forceinline__ void locate_keys(const UpdateArgs &A, const uint64_t 
 #pragma unroll
         for (int j = 0; j < LOC_ILP; ++j) {
             const GraphDesc &D = A.gd[g[j]];
-            const bool live = idx[j] < A.n && D.seg <= bit[j];
+            const bool live = idx[j] < end && D.seg <= bit[j];
             probe[j] = live ? D.heads[(prefix[j] | bit[j]) >> D.log2seg] : 0;
             any |= live;
         }
@@ -194,16 +197,17 @@ __device__ __forceinline__ void locate_keys(const UpdateArgs &A, const uint64_t 
             break;
 #pragma unroll
         for (int j = 0; j < LOC_ILP; ++j) {
-            if (idx[j] < A.n && A.gd[g[j]].seg <= bit[j]) {
+            if (idx[j] < end && A.gd[g[j]].seg <= bit[j]) {
                 if (probe[j] <= key[j])
                     prefix[j] |= bit[j];
                 bit[j] >>= 1;
             }
         }
     }
+    uint32_t inserts = 0;
 #pragma unroll
     for (int j = 0; j < LOC_ILP; ++j) {
-        if (idx[j] >= A.n)
+        if (idx[j] >= end)
             continue;
         const GraphDesc &D = A.gd[g[j]];
         const uint8_t value = bv[idx[j]];
@@ -214,7 +218,9 @@ __device__ __forceinline__ void locate_keys(const UpdateArgs &A, const uint64_t 
             leaf = SIZE_NONE;
         }
         A.leaf[idx[j]] = leaf;
+        inserts += leaf != SIZE_NONE;
     }
+    return inserts;
 }
 
 // ---- grid-wide exclusive scan helpers ------------------------------------
@@ -770,10 +776,25 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             __syncthreads();
             fk = f;
         }
-        const uint32_t stride = G * BLOCK;
-        for (uint32_t i0 = blockIdx.x * BLOCK + threadIdx.x; i0 < A.n; i0 += LOC_ILP * stride)
-            locate_keys(A, bk, bv, i0, stride, fk, log2stride);
-        __syncthreads();
+        if (A.G == 1) {
+            // one graph: each CTA takes a contiguous range (neighbouring keys
+            // share descent paths in L1) and counts its insertions for the
+            // compaction after the barrier
+            uint32_t lo, hi, mine = 0;
+            cta_range(A.n, lo, hi);
+            for (uint32_t i0 = lo + threadIdx.x; i0 < hi; i0 += LOC_ILP * BLOCK)
+                mine += locate_keys(A, bk, bv, i0, BLOCK, hi, fk, log2stride);
+            const uint32_t t = block_sum(mine, tmp);
+            if (threadIdx.x == 0)
+                CNT(scan_id)[blockIdx.x] = t;
+        } else {
+            // many graphs: keys interleaved over the grid (measured faster
+            // than contiguous ranges, which mix trees of unequal height)
+            const uint32_t stride = G * BLOCK;
+            for (uint32_t i0 = blockIdx.x * BLOCK + threadIdx.x; i0 < A.n; i0 += LOC_ILP * stride)
+                locate_keys(A, bk, bv, i0, stride, A.n, fk, log2stride);
+            __syncthreads();
+        }
     }
     if (!grid_barrier(&st->bar, &st->err))
         return;
@@ -793,21 +814,24 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
     if (stamper)
         st->stamp[2] = globaltimer_ns();
 
-    // P2: stable compaction of the insertions (with their graph).
+    // P2: stable compaction of the insertions (with their graph), each CTA
+    // writing the insertions of its locate range; then it counts the
+    // run-length heads of its own output (its first insertion counted as one).
     uint32_t lo, hi;
     cta_range(A.n, lo, hi);
-    {
+    if (A.G > 1) {
         uint32_t cl = 0;
         for (uint32_t i = lo + threadIdx.x; i < hi; i += BLOCK)
             cl += A.leaf[i] != SIZE_NONE;
-        uint32_t t = block_sum(cl, tmp);
+        const uint32_t t = block_sum(cl, tmp);
         if (threadIdx.x == 0)
             CNT(scan_id)[blockIdx.x] = t;
+        if (!grid_barrier(&st->bar, &st->err))
+            return;
     }
-    if (!grid_barrier(&st->bar, &st->err))
-        return;
     uint32_t base, m;
     cta_prefix(CNT(scan_id), base, m, tmp);
+    const uint32_t out_lo = base;
     for (uint32_t i0 = lo; i0 < hi; i0 += BLOCK) {
         uint32_t i = i0 + threadIdx.x;
         uint32_t f = (i < hi && A.leaf[i] != SIZE_NONE) ? 1u : 0u;
@@ -821,7 +845,16 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         }
         base += tot;
     }
-    scan_id ^= 1;
+    const uint32_t out_hi = base;
+    __syncthreads();  // this CTA's output is visible to all its threads
+    {
+        uint32_t h = 0;
+        for (uint32_t j = out_lo + threadIdx.x; j < out_hi; j += BLOCK)
+            h += (j == out_lo || A.ileaf[j] != A.ileaf[j - 1] || A.igraph[j] != A.igraph[j - 1]);
+        const uint32_t t = block_sum(h, tmp);
+        if (threadIdx.x == 0)
+            CNT(scan_id ^ 1)[blockIdx.x] = t;
+    }
     if (!grid_barrier(&st->bar, &st->err))
         return;
     if (A.G == 1 && m >= SIGNIFICANT_INSERTS) {
@@ -835,23 +868,36 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
     }
 
     // P3: run-length grouping of the insertions by (graph, leaf) -> level-0
-    // windows; also each graph's first insertion and its count.
-    cta_range(m, lo, hi);
+    // windows; also each graph's first insertion and its count. A CTA whose
+    // first insertion continues the run of the previous output counted one
+    // head too many: the window offsets subtract those.
+    uint32_t nw = 0;
     {
-        uint32_t cl = 0;
-        for (uint32_t j = lo + threadIdx.x; j < hi; j += BLOCK)
-            cl += (j == 0 || A.ileaf[j] != A.ileaf[j - 1] || A.igraph[j] != A.igraph[j - 1]);
-        uint32_t t = block_sum(cl, tmp);
-        if (threadIdx.x == 0)
-            CNT(scan_id)[blockIdx.x] = t;
+        const uint32_t *ins_cnt = CNT(scan_id);
+        const uint32_t *head_cnt = CNT(scan_id ^ 1);
+        uint32_t carry = 0, before = 0, all = 0;
+        for (uint32_t c0 = 0; c0 < G; c0 += BLOCK) {
+            const uint32_t c = c0 + threadIdx.x;
+            const uint32_t n_c = c < G ? ld_volatile(ins_cnt + c) : 0u;
+            uint32_t tot;
+            const uint32_t b_c = carry + block_excl_scan(n_c, &tot, tmp);  // first output of CTA c
+            carry += tot;
+            uint32_t h = 0;
+            if (c < G && n_c) {
+                h = ld_volatile(head_cnt + c);
+                if (b_c > 0 && A.ileaf[b_c] == A.ileaf[b_c - 1] && A.igraph[b_c] == A.igraph[b_c - 1])
+                    --h;
+            }
+            all += h;
+            if (c < blockIdx.x)
+                before += h;
+        }
+        nw = block_sum(all, tmp);
+        base = block_sum(before, tmp);
     }
-    if (!grid_barrier(&st->bar, &st->err))
-        return;
-    uint32_t nw;
-    cta_prefix(CNT(scan_id), base, nw, tmp);
-    for (uint32_t j0 = lo; j0 < hi; j0 += BLOCK) {
+    for (uint32_t j0 = out_lo; j0 < out_hi; j0 += BLOCK) {
         uint32_t j = j0 + threadIdx.x;
-        bool in = j < hi;
+        bool in = j < out_hi;
         uint32_t head = 0;
         if (in) {
             const uint32_t gj = A.igraph[j];
@@ -865,6 +911,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         uint32_t tot;
         uint32_t ex = block_excl_scan(head, &tot, tmp);
         if (in) {
+            // a run continued from the previous CTA's output extends window base - 1
             uint32_t e = base + ex;
             if (head) {
                 A.wnode[0][e] = A.ileaf[j];
