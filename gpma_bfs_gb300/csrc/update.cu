@@ -1225,8 +1225,9 @@ __global__ void merge_split_kernel(const uint64_t *lk, uint32_t L, const uint64_
 // chunk c's merged elements come from live[split[c] .. split[c+1]) and the
 // matching pending range; both are staged in shared memory (coalesced) and
 // merged there, then every slot of the chunk is written once, coalesced.
-__global__ void __launch_bounds__(BLOCK) rebuild_kernel(uint64_t *keys, uint8_t *vals, uint32_t *row_offset,
-                                                        uint32_t row_num, uint32_t size, uint32_t log2seg,
+__global__ void __launch_bounds__(BLOCK) rebuild_kernel(uint64_t *keys, uint8_t *vals, uint64_t *heads,
+                                                        uint32_t *row_offset, uint32_t row_num, uint32_t size,
+                                                        uint32_t log2seg,
                                                         uint32_t log2F, const uint64_t *lk, const uint8_t *lv,
                                                         uint32_t L, const uint64_t *pk, const uint8_t *pv, uint32_t P,
                                                         const uint32_t *split, uint64_t gap_key) {
@@ -1295,6 +1296,8 @@ __global__ void __launch_bounds__(BLOCK) rebuild_kernel(uint64_t *keys, uint8_t 
             }
             keys[slot] = k;
             vals[slot] = v;
+            if (ln == 0)
+                heads[s] = k;
             if (is_guard(k)) {
                 const uint32_t row = (uint32_t)(k >> 32);
                 if (row < row_num)
@@ -1307,11 +1310,14 @@ __global__ void __launch_bounds__(BLOCK) rebuild_kernel(uint64_t *keys, uint8_t 
 
 // keys[0..L) = live, keys[L..size) = KEY_NONE (values 0): the layout
 // resize_gpma leaves when the root rebalance that follows it is rejected.
-__global__ void compacted_layout_kernel(uint64_t *keys, uint8_t *vals, uint32_t size, const uint64_t *lk,
-                                        const uint8_t *lv, uint32_t L) {
+__global__ void compacted_layout_kernel(uint64_t *keys, uint8_t *vals, uint64_t *heads, uint32_t log2seg,
+                                        uint32_t size, const uint64_t *lk, const uint8_t *lv, uint32_t L) {
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < size; t += gridDim.x * blockDim.x) {
-        keys[t] = t < L ? lk[t] : KEY_NONE;
+        const uint64_t k = t < L ? lk[t] : KEY_NONE;
+        keys[t] = k;
         vals[t] = t < L ? lv[t] : 0;
+        if ((t & ((1u << log2seg) - 1)) == 0)
+            heads[t >> log2seg] = k;
     }
 }
 
@@ -1388,6 +1394,13 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k
     const uint32_t log2seg = fls32(geo.seg) - 1;
     const uint32_t log2F = fls32(geo.size) - 1 - log2seg;
     const uint32_t out_chunks = (geo.size + CHUNK - 1) / CHUNK;
+    // the rebuild kernels write the segment heads of the new geometry
+    if ((geo.size >> log2seg) > g->heads_cap || !g->heads) {
+        dev_free(g->heads);
+        g->heads_cap = 0;
+        GPMA_TRY(dev_alloc(&g->heads, geo.size >> log2seg));
+        g->heads_cap = geo.size >> log2seg;
+    }
     const int rgrid = grid_for((uint64_t)out_chunks * BLOCK, g->sms, 4);
     const size_t rsmem = 2ull * CHUNK * 9;  // staged sources + merged chunk
     // merge splits at every chunk boundary of the new array: the chunk counts
@@ -1406,9 +1419,9 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k
     if (significant) {
         // significant_insert: everything redispatched, gaps are key 0 / value 0
         splits();
-        rebuild_kernel<<<rgrid, BLOCK, rsmem, s>>>(g->keys, g->values, g->row_offset, g->row_num, geo.size, log2seg,
-                                                    log2F, g->skeys, g->svals, live, pend_k, pend_v, pend_n, split,
-                                                    0ull);
+        rebuild_kernel<<<rgrid, BLOCK, rsmem, s>>>(g->keys, g->values, g->heads, g->row_offset, g->row_num, geo.size,
+                                                    log2seg, log2F, g->skeys, g->svals, live, pend_k, pend_v, pend_n,
+                                                    split, 0ull);
         g->stats.significant++;
         g->stats.accepted_windows++;
         g->stats.accepted_slots += geo.size;
@@ -1416,22 +1429,21 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k
         const uint32_t h = geo.height;
         if (geo.lower[h] <= merge && merge <= geo.upper[h]) {
             splits();
-            rebuild_kernel<<<rgrid, BLOCK, rsmem, s>>>(g->keys, g->values, g->row_offset, g->row_num, geo.size,
-                                                        log2seg, log2F, g->skeys, g->svals, live, pend_k, pend_v,
-                                                        pend_n, split, KEY_NONE);
+            rebuild_kernel<<<rgrid, BLOCK, rsmem, s>>>(g->keys, g->values, g->heads, g->row_offset, g->row_num,
+                                                        geo.size, log2seg, log2F, g->skeys, g->svals, live, pend_k,
+                                                        pend_v, pend_n, split, KEY_NONE);
             g->stats.accepted_windows++;
             g->stats.accepted_slots += geo.size;
         } else {
             // the reference drops the insertions and keeps the compacted array
-            compacted_layout_kernel<<<grid_for(geo.size, g->sms, 8), BLOCK, 0, s>>>(g->keys, g->values, geo.size,
-                                                                                     g->skeys, g->svals, live);
+            compacted_layout_kernel<<<grid_for(geo.size, g->sms, 8), BLOCK, 0, s>>>(
+                g->keys, g->values, g->heads, log2seg, geo.size, g->skeys, g->svals, live);
             g->stats.root_drops++;
         }
         g->stats.root_resizes++;
     }
     GPMA_CUDA(cudaGetLastError());
     g->geo = geo;
-    GPMA_TRY(refresh_heads(g, s));
     prof_mark(g, 1, s);
     GPMA_CUDA(cudaStreamSynchronize(s));
     g->prof.rebuild_ms += prof_elapsed(g, 0, 1);
