@@ -530,6 +530,40 @@ def run_batched(args, stream):
 
     plain_bfs()
     tpb = timed(plain_bfs)
+
+    # recorded steps: each step's packed update of every graph and its 64-source
+    # BFS, as the two eager calls on the batched copy and as one CUDA graph launch
+    # (gpma_batch_step) on the plain copy, which holds the same layouts now
+    b2 = G.Batch()
+    rec = b2.step(graphs_p)
+    te, tr, same_reached = [], [], True
+    for j in range(args.warmup + args.batched_steps):
+        sizes = np.exp(rng.uniform(np.log(100), np.log(200_000), k)).astype(np.int64)
+        parts = [s.step(int(z)) for s, z in zip(streams, sizes)]
+        for sp, z in zip(streams_p, sizes):
+            sp.step(int(z))
+        o = np.concatenate([[0], np.cumsum([len(p[0]) for p in parts])]).astype(np.uint64)
+        dk = torch.from_numpy(np.concatenate([p[0] for p in parts]).view(np.int64)).cuda()
+        dv = torch.from_numpy(np.concatenate([p[1] for p in parts])).cuda()
+        got = {}
+
+        def eager():
+            b.update_packed(graphs_b, dk, dv, o, stream)
+            got["e"] = b.bfs_multi(graphs_b, sources, stream=stream)[1]
+
+        def recorded():
+            got["r"] = rec.run(dk, dv, o, sources, stream=stream)
+
+        t_e, t_r = timed(eager), timed(recorded)
+        same_reached = same_reached and all(np.array_equal(x, y) for x, y in zip(got["e"], got["r"]))
+        if j >= args.warmup:
+            te.append(t_e)
+            tr.append(t_r)
+    same_steps = same_reached and all(
+        np.array_equal(x.export_layout()[0], y.export_layout()[0]) for x, y in zip(graphs_b, graphs_p))
+    rec_stats = rec.stats()
+    rec.close()
+    b2.close()
     b.close()
     total_edges = int(sum(len(kk) for _, kk in specs))
     for x in graphs_b + graphs_p:
@@ -547,6 +581,9 @@ def run_batched(args, stream):
         "bfs": {"sources_per_graph": 64, "edges_traversed": edges_b, "autotune": tuned,
                 "batched_ms": tbb, "batched_gteps": edges_b / (tbb * 1e-3) / 1e9,
                 "plain_ms": tpb, "plain_gteps": edges_b / (tpb * 1e-3) / 1e9, "speedup": tpb / tbb},
+        "update_bfs_steps": {"eager_ms": statistics.median(te), "graph_ms": statistics.median(tr),
+                             "identical": same_steps, "graph_launches": rec_stats["graph_launches"],
+                             "graph_builds": rec_stats["builds"], "host_runs": rec_stats["host_runs"]},
         "setup_s": {"generate": gen_s},
     }
 

@@ -173,6 +173,10 @@ def lib() -> ctypes.CDLL:
         "gpma_step_destroy": (st, [P]),
         "gpma_step_run": (st, [P, P, P, u64, u32, P, ctypes.POINTER(u64), P]),
         "gpma_step_get_stats": (st, [P, ctypes.POINTER(_StepStats)]),
+        "gpma_batch_step_create": (st, [P, P, u32, ctypes.POINTER(P)]),
+        "gpma_batch_step_destroy": (st, [P]),
+        "gpma_batch_step_run": (st, [P, P, P, P, P, P, P, P]),
+        "gpma_batch_step_get_stats": (st, [P, ctypes.POINTER(_StepStats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -725,6 +729,68 @@ class Batch:
 
     def reset_profile(self) -> None:
         _check(lib().gpma_batch_reset_profile(self._h), "gpma_batch_reset_profile")
+
+    def step(self, graphs) -> "BatchStep":
+        """A recorded step over these graphs: update_packed + bfs_multi as one CUDA graph."""
+        return BatchStep(self, graphs)
+
+
+class BatchStep:
+    """The batched form's step (gpma_batch_step_*): one packed update of every
+    graph and one multi-source BFS over all of them, recorded as a CUDA graph
+    and replayed per step; results equal Batch.update_packed followed by
+    Batch.bfs_multi (without levels). Close it before its batch and graphs."""
+
+    def __init__(self, batch: Batch, graphs):
+        self.batch, self.graphs = batch, list(graphs)
+        k = len(self.graphs)
+        hs = (ctypes.c_void_p * k)(*[g.handle.value for g in self.graphs])
+        h = ctypes.c_void_p()
+        _check(lib().gpma_batch_step_create(batch._h, hs, k, ctypes.byref(h)), "gpma_batch_step_create")
+        self.handle = h
+
+    def run(self, keys, values, offsets, sources, stream=None):
+        """Applies the packed batches (graph i gets keys[offsets[i]:offsets[i+1]])
+        and returns the reached counts per graph of the multi-source BFS."""
+        k = len(self.graphs)
+        off = np.ascontiguousarray(np.asarray(offsets, np.uint64))
+        if len(off) != k + 1 or len(keys) != len(values) or int(off[-1]) > len(keys) or len(sources) != k:
+            raise ValueError("offsets must have len(graphs) + 1 entries within the key array, one source list per graph")
+        if isinstance(keys, np.ndarray):
+            keys = np.ascontiguousarray(keys, dtype=np.uint64)
+        if isinstance(values, np.ndarray):
+            values = np.ascontiguousarray(values).view(np.uint8) if values.dtype.itemsize == 1 \
+                else np.ascontiguousarray(values, dtype=np.uint8)
+        kp, kk = _ptr(keys)
+        vp, vk = _ptr(values)
+        srcs = [np.ascontiguousarray(np.asarray(x, np.uint32)) for x in sources]
+        sp = (ctypes.c_void_p * k)(*[x.ctypes.data for x in srcs])
+        ns = (ctypes.c_uint32 * k)(*[len(x) for x in srcs])
+        reached = np.zeros(sum(len(x) for x in srcs), np.uint64)
+        _check(lib().gpma_batch_step_run(self.handle, kp, vp, off.ctypes.data, sp, ns, reached.ctypes.data,
+                                         _stream_ptr(stream)), "gpma_batch_step_run")
+        del kk, vk
+        parts, o = [], 0
+        for x in srcs:
+            parts.append(reached[o:o + len(x)])
+            o += len(x)
+        return parts
+
+    def stats(self) -> dict:
+        st = _StepStats()
+        _check(lib().gpma_batch_step_get_stats(self.handle, ctypes.byref(st)), "gpma_batch_step_get_stats")
+        return {n: getattr(st, n) for n, _ in _StepStats._fields_}
+
+    def close(self) -> None:
+        if self.handle:
+            lib().gpma_batch_step_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 PLAN_ONLY = 1

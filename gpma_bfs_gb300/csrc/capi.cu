@@ -157,21 +157,29 @@ __global__ void gather_live_kernel(const uint64_t *keys, const uint8_t *vals, ui
 
 // Destination segment j (dst_off[j] .. dst_off[j+1]) copied from the source
 // starting at src_start[j]: stages batches in segment-length order.
-__global__ void gather_segments_kernel(uint64_t *dk, uint8_t *dv, const uint64_t *sk, const uint8_t *sv,
-                                       const uint64_t *dst_off, const uint64_t *src_start, uint32_t m) {
-    const uint64_t n = dst_off[m];
+struct GatherArgs {
+    uint64_t *dk;
+    uint8_t *dv;
+    const uint64_t *sk;
+    const uint8_t *sv;
+    const uint64_t *dst_off;    // m + 1
+    const uint64_t *src_start;  // m
+    uint32_t m;
+};
+__global__ void gather_segments_kernel(GatherArgs A) {
+    const uint64_t n = A.dst_off[A.m];
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t lo = 0, hi = m;
+        uint32_t lo = 0, hi = A.m;
         while (hi - lo > 1) {
             uint32_t mid = (lo + hi) >> 1;
-            if (dst_off[mid] <= t)
+            if (A.dst_off[mid] <= t)
                 lo = mid;
             else
                 hi = mid;
         }
-        const uint64_t src = src_start[lo] + (t - dst_off[lo]);
-        dk[t] = sk[src];
-        dv[t] = sv[src];
+        const uint64_t src = A.src_start[lo] + (t - A.dst_off[lo]);
+        A.dk[t] = A.sk[src];
+        A.dv[t] = A.sv[src];
     }
 }
 
@@ -179,6 +187,89 @@ int small_grid(uint64_t work, int sms) {
     uint64_t g = (work + BLOCK - 1) / BLOCK;
     return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, (uint64_t)sms * 8));
 }
+
+}  // namespace
+
+gpma_status packed_plan(gpma_batch *b, gpma_graph *const *graphs, const uint64_t *keys, const uint8_t *values,
+                        const uint64_t *offsets, uint32_t k, PackedPlan *P) {
+    static_assert(sizeof(GatherArgs) <= KernelLaunch::ARG_BYTES, "gather arguments exceed the launch record");
+    const uint64_t all = k ? offsets[k] - offsets[0] : 0;
+    std::vector<uint32_t> order;
+    uint64_t total = 0;
+    P->bulk.clear();
+    for (uint32_t i = 0; i < k; ++i) {
+        const uint64_t c = offsets[i + 1] - offsets[i];
+        if (c == 0)
+            continue;
+        if (c >= SIGNIFICANT_INSERTS) {
+            P->bulk.push_back(i);
+            continue;
+        }
+        order.push_back(i);
+        total += c;
+    }
+    P->m = (uint32_t)order.size();
+    P->gs.assign(P->m, nullptr);
+    P->off.assign(P->m + 1, 0);
+    if (P->m == 0)
+        return GPMA_OK;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint32_t x, uint32_t y) { return graphs[x]->geo.seg < graphs[y]->geo.seg; });
+    GPMA_TRY(ensure_buffers(b->buf, std::max<uint64_t>(total, all), P->m));
+    P->upload = !(is_device_pointer(keys) && is_device_pointer(values));
+    P->all_keys = all;
+    const uint64_t src_base = P->upload ? offsets[0] : 0;
+    const uint32_t m = P->m;
+    if (m > b->gather_cap || !b->gather_tab) {
+        dev_free(b->gather_tab);
+        if (b->h_gather_tab)
+            cudaFreeHost(b->h_gather_tab);
+        b->h_gather_tab = nullptr;
+        b->gather_cap = 0;
+        GPMA_TRY(dev_alloc(&b->gather_tab, 2ull * m + 1));
+        GPMA_CUDA(cudaMallocHost((void **)&b->h_gather_tab, sizeof(uint64_t) * (2ull * m + 1)));
+        b->gather_cap = m;
+    }
+    // destination offsets [0..m], then the source start of each destination segment
+    uint64_t *tab = b->h_gather_tab;
+    tab[0] = 0;
+    for (uint32_t j = 0; j < m; ++j) {
+        const uint32_t i = order[j];
+        P->gs[j] = graphs[i];
+        P->off[j + 1] = P->off[j] + (offsets[i + 1] - offsets[i]);
+        tab[j + 1] = P->off[j + 1];
+        tab[m + 1 + j] = offsets[i] - src_base;
+    }
+    P->gtab_bytes = sizeof(uint64_t) * (2ull * m + 1);
+    GatherArgs A;
+    memset(&A, 0, sizeof(A));
+    A.dk = b->buf.bkeys[0];
+    A.dv = b->buf.bvals[0];
+    A.sk = P->upload ? b->buf.bkeys[1] : keys;
+    A.sv = P->upload ? b->buf.bvals[1] : values;
+    A.dst_off = b->gather_tab;
+    A.src_start = b->gather_tab + m + 1;
+    A.m = m;
+    P->gather.set((const void *)gather_segments_kernel, small_grid(total, b->sms), 0, &A, sizeof(A));
+    return GPMA_OK;
+}
+
+gpma_status packed_stage(gpma_batch *b, const PackedPlan &P, const uint64_t *keys, const uint8_t *values,
+                         const uint64_t *offsets, cudaStream_t s, bool with_table) {
+    (void)P;
+    if (P.upload) {
+        // one upload of the packed range into the second sort buffer
+        const uint64_t first = offsets[0];
+        const uint64_t all = P.all_keys;
+        GPMA_TRY(copy_any(b->buf.bkeys[1], keys + first, all * sizeof(uint64_t), s));
+        GPMA_TRY(copy_any(b->buf.bvals[1], values + first, all, s));
+    }
+    if (with_table)
+        GPMA_CUDA(cudaMemcpyAsync(b->gather_tab, b->h_gather_tab, P.gtab_bytes, cudaMemcpyHostToDevice, s));
+    return GPMA_OK;
+}
+
+namespace {
 
 }  // namespace
 }  // namespace gpma
@@ -393,6 +484,9 @@ gpma_status gpma_batch_destroy(gpma_batch *b) {
     free_buffers(b->buf);
     free_batch_bfs(b);
     dev_free(b->gather_tab);
+    if (b->h_gather_tab)
+        cudaFreeHost(b->h_gather_tab);
+    b->h_gather_tab = nullptr;
     for (auto &e : b->ev)
         if (e)
             cudaEventDestroy(e);
@@ -486,64 +580,26 @@ gpma_status gpma_batch_update_packed(gpma_batch *b, gpma_graph *const *graphs, c
         set_error("gpma_batch_update_packed: %llu keys in one call exceed 2^31", (unsigned long long)all);
         return GPMA_ERR_CAPACITY;
     }
-    const bool on_device = is_device_pointer(keys) && is_device_pointer(values);
-    std::vector<uint32_t> order;
-    uint64_t total = 0;
     for (uint32_t i = 0; i < k; ++i) {
-        const uint64_t c = offsets[i + 1] - offsets[i];
         graphs[i]->stats.updates++;
-        graphs[i]->stats.submitted += c;
-        if (c == 0)
-            continue;
-        if (c >= SIGNIFICANT_INSERTS) {
-            // a possible bulk rebuild: the single-graph path, on the graph's own buffers
-            GPMA_TRY(ensure_buffers(graphs[i]->buf, c, 1));
-            GPMA_TRY(copy_any(graphs[i]->buf.bkeys[0], keys + offsets[i], c * sizeof(uint64_t), s));
-            GPMA_TRY(copy_any(graphs[i]->buf.bvals[0], values + offsets[i], c, s));
-            GPMA_TRY(update_device(graphs[i], c, s));
-            continue;
-        }
-        order.push_back(i);
-        total += c;
+        graphs[i]->stats.submitted += offsets[i + 1] - offsets[i];
     }
-    if (order.empty())
+    PackedPlan P;
+    GPMA_TRY(packed_plan(b, graphs, keys, values, offsets, k, &P));
+    for (uint32_t i : P.bulk) {
+        // a possible bulk rebuild: the single-graph path, on the graph's own buffers
+        const uint64_t c = offsets[i + 1] - offsets[i];
+        GPMA_TRY(ensure_buffers(graphs[i]->buf, c, 1));
+        GPMA_TRY(copy_any(graphs[i]->buf.bkeys[0], keys + offsets[i], c * sizeof(uint64_t), s));
+        GPMA_TRY(copy_any(graphs[i]->buf.bvals[0], values + offsets[i], c, s));
+        GPMA_TRY(update_device(graphs[i], c, s));
+    }
+    if (P.m == 0)
         return GPMA_OK;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](uint32_t x, uint32_t y) { return graphs[x]->geo.seg < graphs[y]->geo.seg; });
-    GPMA_TRY(ensure_buffers(b->buf, std::max<uint64_t>(total, all), (uint32_t)order.size()));
-    const uint64_t *src_k = keys;
-    const uint8_t *src_v = values;
-    uint64_t src_base = 0;
-    if (!on_device) {
-        // one upload of the packed range into the second sort buffer
-        GPMA_TRY(copy_any(b->buf.bkeys[1], keys + offsets[0], all * sizeof(uint64_t), s));
-        GPMA_TRY(copy_any(b->buf.bvals[1], values + offsets[0], all, s));
-        src_k = b->buf.bkeys[1];
-        src_v = b->buf.bvals[1];
-        src_base = offsets[0];
-    }
-    const uint32_t m = (uint32_t)order.size();
-    if (m > b->gather_cap || !b->gather_tab) {
-        dev_free(b->gather_tab);
-        b->gather_cap = 0;
-        GPMA_TRY(dev_alloc(&b->gather_tab, 2ull * m + 1));
-        b->gather_cap = m;
-    }
-    std::vector<gpma_graph *> gs(m);
-    std::vector<uint64_t> off(m + 1, 0), tab(2ull * m + 1, 0);
-    for (uint32_t j = 0; j < m; ++j) {
-        const uint32_t i = order[j];
-        gs[j] = graphs[i];
-        off[j + 1] = off[j] + (offsets[i + 1] - offsets[i]);
-        tab[m + 1 + j] = offsets[i] - src_base;  // source start of destination segment j
-    }
-    std::copy(off.begin(), off.end(), tab.begin());
-    GPMA_CUDA(cudaMemcpyAsync(b->gather_tab, tab.data(), sizeof(uint64_t) * tab.size(), cudaMemcpyHostToDevice, s));
-    gather_segments_kernel<<<small_grid(total, b->sms), BLOCK, 0, s>>>(b->buf.bkeys[0], b->buf.bvals[0], src_k, src_v,
-                                                                      b->gather_tab, b->gather_tab + m + 1, m);
-    GPMA_CUDA(cudaGetLastError());
+    GPMA_TRY(packed_stage(b, P, keys, values, offsets, s));
+    GPMA_CUDA(P.gather.launch(s));
     b->prof.kernel_launches += 1;
-    return update_graphs(gs.data(), off.data(), m, b->buf, b->sms, s, true, b->profiling, b->ev, &b->prof);
+    return update_graphs(P.gs.data(), P.off.data(), P.m, b->buf, b->sms, s, true, b->profiling, b->ev, &b->prof);
 }
 
 gpma_status gpma_batch_bfs_multi(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs,

@@ -206,19 +206,20 @@ struct gpma_batch {
     // multi-source BFS state over all graphs of a call
     uint64_t ms_cap = 0;               // nodes
     uint64_t *ms_mask[3] = {nullptr, nullptr, nullptr};
-    uint32_t *ms_voff = nullptr;       // node offsets, graphs + 1
-    uint64_t *ms_soff = nullptr;       // slot offsets of the concatenated arrays, graphs + 1
-    uint32_t *ms_src = nullptr;        // sources, graphs * 64
-    uint32_t *ms_nsrc = nullptr;       // sources per graph
+    // per-call graph table (node and slot offsets, sources, descriptors), one
+    // upload from its pinned mirror
+    unsigned char *ms_tab = nullptr;
+    unsigned char *h_ms_tab = nullptr;
     uint32_t *ms_ctl = nullptr;
     uint32_t *h_ms_ctl = nullptr;      // pinned
-    void *ms_gdesc = nullptr;          // BFS graph table
-    uint64_t *ms_reached = nullptr;    // graphs * 64
+    uint64_t *ms_reached = nullptr;    // graphs * 64 reached counts + the traversed-edge total
+    unsigned long long *h_ms_reached = nullptr;  // pinned
     uint2 *ms_chunks = nullptr;
     uint64_t ms_chunk_cap = 0;         // entries (uint4): total slots / 32 + 1024
     uint32_t ms_gcap = 0;
     uint64_t last_traversed = 0;       // edges scanned by the last multi-source BFS, all lanes
     uint64_t *gather_tab = nullptr;    // packed-update staging table (2 * graphs + 1)
+    uint64_t *h_gather_tab = nullptr;  // its pinned mirror
     uint32_t gather_cap = 0;
 };
 
@@ -301,6 +302,10 @@ struct KernelLaunch {
         arg_bytes = bytes;
         memcpy(args, a, bytes);
     }
+    cudaError_t launch(cudaStream_t s) {
+        params[0] = args;
+        return cudaLaunchKernel(func, grid, block, params, smem, s);
+    }
     cudaError_t launch_cooperative(cudaStream_t s) {
         params[0] = args;
         return cudaLaunchCooperativeKernel(func, grid, block, params, smem, s);
@@ -381,6 +386,44 @@ gpma_status bfs_finish(gpma_graph *g, uint64_t *reached);
 gpma_status bfs_noalloc_run(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached, cudaStream_t s);
 gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs, const uint32_t *nsrc,
                           uint32_t k, uint32_t *const *levels, uint64_t *reached, cudaStream_t s);
+// The host parts of batch_bfs_run: batch_bfs_plan sizes the buffers, fills
+// the pinned table (tab_bytes of b->h_ms_tab to upload to b->ms_tab), lists
+// the buffers to zero and records the cooperative kernel launch (levels go
+// to stage[i] when stage is non-null); batch_bfs_enqueue_readback copies the
+// control words and counts back; batch_bfs_finish checks and reports them.
+struct BatchBfsPlan {
+    static constexpr int CLEARS = 5;
+    size_t tab_bytes;
+    void *clear_ptr[CLEARS];
+    size_t clear_bytes[CLEARS];
+    KernelLaunch main;
+    size_t ctl_bytes;
+    size_t reached_bytes;
+};
+// Host part of a packed update of graphs[0..k) (batch i at [offsets[i],
+// offsets[i+1]) of keys/values, host or device): graphs with batches of
+// SIGNIFICANT_INSERTS or more are listed in `bulk` for the single-graph path;
+// the others, ordered by segment length (gs, batch offsets off), get the
+// gather launch that stages their batches in that order. packed_stage uploads
+// a host batch into the second sort buffer and (with_table) the gather table.
+struct PackedPlan {
+    std::vector<uint32_t> bulk;
+    uint32_t m = 0;
+    std::vector<gpma_graph *> gs;
+    std::vector<uint64_t> off;
+    bool upload = false;
+    uint64_t all_keys = 0;
+    size_t gtab_bytes = 0;
+    KernelLaunch gather;
+};
+gpma_status packed_plan(gpma_batch *b, gpma_graph *const *graphs, const uint64_t *keys, const uint8_t *values,
+                        const uint64_t *offsets, uint32_t k, PackedPlan *P);
+gpma_status packed_stage(gpma_batch *b, const PackedPlan &P, const uint64_t *keys, const uint8_t *values,
+                         const uint64_t *offsets, cudaStream_t s, bool with_table = true);
+gpma_status batch_bfs_plan(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs,
+                           const uint32_t *nsrc, uint32_t k, uint32_t *const *stage, BatchBfsPlan *P);
+gpma_status batch_bfs_enqueue_readback(gpma_batch *b, const BatchBfsPlan &P, cudaStream_t s);
+gpma_status batch_bfs_finish(gpma_batch *b, const uint32_t *nsrc, uint32_t k, uint64_t *reached);
 void free_bfs(gpma_graph *g);
 void free_batch_bfs(gpma_batch *b);
 int update_grid_size(int sms, uint64_t n);

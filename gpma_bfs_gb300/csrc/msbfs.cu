@@ -359,13 +359,15 @@ int ms_grid_size(int sms) {
 void free_batch_bfs(gpma_batch *b) {
     for (int i = 0; i < 3; ++i)
         dev_free(b->ms_mask[i]);
-    dev_free(b->ms_voff);
-    dev_free(b->ms_soff);
-    dev_free(b->ms_src);
-    dev_free(b->ms_nsrc);
+    dev_free(b->ms_tab);
+    if (b->h_ms_tab)
+        cudaFreeHost(b->h_ms_tab);
+    b->h_ms_tab = nullptr;
     dev_free(b->ms_ctl);
-    dev_free(b->ms_gdesc);
     dev_free(b->ms_reached);
+    if (b->h_ms_reached)
+        cudaFreeHost(b->h_ms_reached);
+    b->h_ms_reached = nullptr;
     dev_free(b->ms_chunks);
     b->ms_chunk_cap = 0;
     if (b->h_ms_ctl)
@@ -375,24 +377,38 @@ void free_batch_bfs(gpma_batch *b) {
     b->ms_gcap = 0;
 }
 
-// Multi-source BFS of graphs[0..k) with nsrc[i] sources each. Levels (when
-// levels != NULL) are written through device staging and copied to the
-// caller's pointers; reached receives sum(nsrc) counts. Also returns the
-// traversed-edge total through *traversed_out when non-null.
-gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs, const uint32_t *nsrc,
-                          uint32_t k, uint32_t *const *levels, uint64_t *reached, cudaStream_t s) {
+namespace {
+
+// Byte layout of the per-call graph table (device copy and pinned mirror):
+// node offsets (k + 1 u32), slot offsets (k + 1 u64), sources (64 k u32),
+// graph descriptors (k MsGraph), each part 16-byte aligned.
+struct MsTabLayout {
+    size_t voff, soff, src, gdesc, bytes;
+    explicit MsTabLayout(uint32_t k) {
+        auto up = [](size_t x) { return (x + 15) & ~size_t(15); };
+        voff = 0;
+        soff = up(voff + 4ull * (k + 1));
+        src = up(soff + 8ull * (k + 1));
+        gdesc = up(src + 4ull * 64 * k);
+        bytes = up(gdesc + sizeof(MsGraph) * k);
+    }
+};
+
+}  // namespace
+
+gpma_status batch_bfs_plan(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs,
+                           const uint32_t *nsrc, uint32_t k, uint32_t *const *stage, BatchBfsPlan *P) {
+    static_assert(sizeof(MsArgs) <= KernelLaunch::ARG_BYTES, "multi-source BFS arguments exceed the launch record");
     const int grid = ms_grid_size(b->sms);
     if (grid == 0) {
         set_error("multi-source BFS kernel cannot be resident");
         return GPMA_ERR_CUDA;
     }
-    std::vector<uint32_t> voff(k + 1, 0);
-    std::vector<uint64_t> soff(k + 1, 0);
+    uint64_t N = 0, slots = 0;
     for (uint32_t i = 0; i < k; ++i) {
-        voff[i + 1] = voff[i] + graphs[i]->row_num;
-        soff[i + 1] = soff[i] + graphs[i]->geo.size;  // sizes are powers of two >= 4
+        N += graphs[i]->row_num;
+        slots += graphs[i]->geo.size;  // sizes are powers of two >= 4
     }
-    const uint64_t N = voff[k];
     if (N > b->ms_cap || !b->ms_mask[0]) {
         for (int i = 0; i < 3; ++i)
             dev_free(b->ms_mask[i]);
@@ -401,25 +417,23 @@ gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32
             GPMA_TRY(dev_alloc(&b->ms_mask[i], std::max<uint64_t>(N, 1)));
         b->ms_cap = std::max<uint64_t>(N, 1);
     }
-    if (k > b->ms_gcap || !b->ms_voff) {
-        dev_free(b->ms_voff);
-        dev_free(b->ms_soff);
-        dev_free(b->ms_src);
-        dev_free(b->ms_gdesc);
+    const MsTabLayout lay(k);
+    if (k > b->ms_gcap || !b->ms_tab) {
+        dev_free(b->ms_tab);
         dev_free(b->ms_reached);
+        if (b->h_ms_tab)
+            cudaFreeHost(b->h_ms_tab);
+        if (b->h_ms_reached)
+            cudaFreeHost(b->h_ms_reached);
+        b->h_ms_tab = nullptr;
+        b->h_ms_reached = nullptr;
         b->ms_gcap = 0;
-        GPMA_TRY(dev_alloc(&b->ms_voff, k + 1));
-        GPMA_TRY(dev_alloc(&b->ms_soff, k + 1));
-        GPMA_TRY(dev_alloc(&b->ms_src, 64ull * k));
-        uint8_t *gd = nullptr;
-        GPMA_TRY(dev_alloc(&gd, sizeof(MsGraph) * k));
-        b->ms_gdesc = gd;
+        GPMA_TRY(dev_alloc(&b->ms_tab, lay.bytes));
         GPMA_TRY(dev_alloc(&b->ms_reached, 64ull * k + 1));
+        GPMA_CUDA(cudaMallocHost((void **)&b->h_ms_tab, lay.bytes));
+        GPMA_CUDA(cudaMallocHost((void **)&b->h_ms_reached, sizeof(unsigned long long) * (64ull * k + 1)));
         b->ms_gcap = k;
     }
-    uint64_t slots = 0;
-    for (uint32_t i = 0; i < k; ++i)
-        slots += graphs[i]->geo.size;
     if (ms_chunk_need(slots) > b->ms_chunk_cap) {
         dev_free(b->ms_chunks);
         b->ms_chunk_cap = 0;
@@ -428,97 +442,124 @@ gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32
     }
     if (!b->ms_ctl) {
         GPMA_TRY(dev_alloc(&b->ms_ctl, MS_CTL_WORDS));
-        cudaError_t e = cudaMallocHost((void **)&b->h_ms_ctl, sizeof(uint32_t) * MS_CTL_WORDS);
-        if (e != cudaSuccess)
-            return cuda_fail(e, "cudaMallocHost(ms ctl)");
+        GPMA_CUDA(cudaMallocHost((void **)&b->h_ms_ctl, sizeof(uint32_t) * MS_CTL_WORDS));
     }
-    // per-graph level staging, only when levels are requested
-    std::vector<uint32_t *> stage(k, nullptr);
-    std::vector<MsGraph> gr(k);
-    std::vector<uint32_t> hsrc(64ull * k, 0);
-    gpma_status st = GPMA_OK;
+    // the table, in the pinned mirror (the previous call's upload has finished)
+    uint32_t *voff = reinterpret_cast<uint32_t *>(b->h_ms_tab + lay.voff);
+    uint64_t *soff = reinterpret_cast<uint64_t *>(b->h_ms_tab + lay.soff);
+    uint32_t *src = reinterpret_cast<uint32_t *>(b->h_ms_tab + lay.src);
+    MsGraph *gr = reinterpret_cast<MsGraph *>(b->h_ms_tab + lay.gdesc);
+    voff[0] = 0;
+    soff[0] = 0;
+    memset(src, 0, 4ull * 64 * k);
     for (uint32_t i = 0; i < k; ++i) {
-        gpma_graph *g = graphs[i];
+        const gpma_graph *g = graphs[i];
+        voff[i + 1] = voff[i] + g->row_num;
+        soff[i + 1] = soff[i] + g->geo.size;
         gr[i].keys = g->keys;
         gr[i].vals = g->values;
         gr[i].ro = g->row_offset;
         gr[i].n = g->row_num;
         gr[i].size = g->geo.size;
         gr[i].nsrc = nsrc[i];
-        gr[i].levels = nullptr;
-        if (levels && levels[i]) {
-            st = dev_alloc(&stage[i], (uint64_t)nsrc[i] * g->row_num);
-            if (st != GPMA_OK)
-                break;
-            gr[i].levels = stage[i];
-            cudaMemsetAsync(stage[i], 0, sizeof(uint32_t) * nsrc[i] * (uint64_t)g->row_num, s);
-        }
+        gr[i].pad = 0;
+        gr[i].levels = stage ? stage[i] : nullptr;
         for (uint32_t j = 0; j < nsrc[i]; ++j)
-            hsrc[64ull * i + j] = srcs[i][j];
+            src[64ull * i + j] = srcs[i][j];
     }
+    P->tab_bytes = lay.bytes;
+    void *ptr[BatchBfsPlan::CLEARS] = {b->ms_mask[0], b->ms_mask[1], b->ms_mask[2], b->ms_ctl, b->ms_reached};
+    const size_t bytes[BatchBfsPlan::CLEARS] = {8 * N, 8 * N, 8 * N, sizeof(uint32_t) * MS_CTL_WORDS,
+                                                sizeof(unsigned long long) * (64ull * k + 1)};
+    for (int i = 0; i < BatchBfsPlan::CLEARS; ++i) {
+        P->clear_ptr[i] = ptr[i];
+        P->clear_bytes[i] = bytes[i];
+    }
+    MsArgs A;
+    memset(&A, 0, sizeof(A));  // padding too: launches are compared byte-wise
+    A.gr = reinterpret_cast<const MsGraph *>(b->ms_tab + lay.gdesc);
+    A.G = k;
+    A.voff = reinterpret_cast<const uint32_t *>(b->ms_tab + lay.voff);
+    A.src = reinterpret_cast<const uint32_t *>(b->ms_tab + lay.src);
+    A.soff = reinterpret_cast<const uint64_t *>(b->ms_tab + lay.soff);
+    A.dense_div = g_tuning.ms_dense_div;
+    A.visited = b->ms_mask[0];
+    A.frontier = b->ms_mask[1];
+    A.next = b->ms_mask[2];
+    A.chunks = reinterpret_cast<uint4 *>(b->ms_chunks);
+    A.chunk_cap = (uint32_t)std::min<uint64_t>(b->ms_chunk_cap, 0xFFFFFFFFull);
+    A.ctl = b->ms_ctl;
+    A.reached = reinterpret_cast<unsigned long long *>(b->ms_reached);
+    A.traversed = reinterpret_cast<unsigned long long *>(b->ms_reached) + 64ull * k;
+    P->main.set((const void *)msbfs_kernel, grid, 0, &A, sizeof(A));
+    P->ctl_bytes = sizeof(uint32_t) * MS_CTL_WORDS;
+    P->reached_bytes = sizeof(unsigned long long) * (64ull * k + 1);
+    return GPMA_OK;
+}
+
+gpma_status batch_bfs_enqueue_readback(gpma_batch *b, const BatchBfsPlan &P, cudaStream_t s) {
+    GPMA_CUDA(cudaMemcpyAsync(b->h_ms_ctl, b->ms_ctl, P.ctl_bytes, cudaMemcpyDeviceToHost, s));
+    GPMA_CUDA(cudaMemcpyAsync(b->h_ms_reached, b->ms_reached, P.reached_bytes, cudaMemcpyDeviceToHost, s));
+    return GPMA_OK;
+}
+
+gpma_status batch_bfs_finish(gpma_batch *b, const uint32_t *nsrc, uint32_t k, uint64_t *reached) {
+    b->prof.kernel_launches += 1;
+    b->prof.bfs_kernels++;
+    if (b->h_ms_ctl[MS_ERR]) {
+        set_error("device-side wait gave up in the multi-source BFS kernel (code %u)", b->h_ms_ctl[MS_ERR]);
+        return GPMA_ERR_TIMEOUT;
+    }
+    const unsigned long long *r = b->h_ms_reached;
+    if (reached) {
+        uint64_t o = 0;
+        for (uint32_t i = 0; i < k; ++i)
+            for (uint32_t j = 0; j < nsrc[i]; ++j)
+                reached[o++] = r[64ull * i + j];
+    }
+    b->last_traversed = r[64ull * k];
+    b->prof.bfs_edges += r[64ull * k];
+    return GPMA_OK;
+}
+
+// Multi-source BFS of graphs[0..k) with nsrc[i] sources each. Levels (when
+// levels != NULL) are written through device staging and copied to the
+// caller's pointers; reached receives sum(nsrc) counts.
+gpma_status batch_bfs_run(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs, const uint32_t *nsrc,
+                          uint32_t k, uint32_t *const *levels, uint64_t *reached, cudaStream_t s) {
+    // per-graph level staging, only when levels are requested
+    std::vector<uint32_t *> stage(k, nullptr);
     auto cleanup = [&]() {
         for (auto *p : stage)
             if (p)
                 cudaFree(p);
     };
-    if (st != GPMA_OK) {
-        cleanup();
-        return st;
-    }
-    auto step = [&]() -> gpma_status {
-        GPMA_CUDA(cudaMemcpyAsync(b->ms_voff, voff.data(), sizeof(uint32_t) * (k + 1), cudaMemcpyHostToDevice, s));
-        GPMA_CUDA(cudaMemcpyAsync(b->ms_soff, soff.data(), sizeof(uint64_t) * (k + 1), cudaMemcpyHostToDevice, s));
-        GPMA_CUDA(cudaMemcpyAsync(b->ms_src, hsrc.data(), sizeof(uint32_t) * 64 * k, cudaMemcpyHostToDevice, s));
-        GPMA_CUDA(cudaMemcpyAsync(b->ms_gdesc, gr.data(), sizeof(MsGraph) * k, cudaMemcpyHostToDevice, s));
-        for (int i = 0; i < 3; ++i)
-            GPMA_CUDA(cudaMemsetAsync(b->ms_mask[i], 0, sizeof(uint64_t) * N, s));
-        GPMA_CUDA(cudaMemsetAsync(b->ms_ctl, 0, sizeof(uint32_t) * MS_CTL_WORDS, s));
-        GPMA_CUDA(cudaMemsetAsync(b->ms_reached, 0, sizeof(unsigned long long) * (64ull * k + 1), s));
-        MsArgs A;
-        A.gr = static_cast<const MsGraph *>(b->ms_gdesc);
-        A.G = k;
-        A.voff = b->ms_voff;
-        A.src = b->ms_src;
-        A.soff = b->ms_soff;
-        A.dense_div = g_tuning.ms_dense_div;
-        A.visited = b->ms_mask[0];
-        A.frontier = b->ms_mask[1];
-        A.next = b->ms_mask[2];
-        A.chunks = reinterpret_cast<uint4 *>(b->ms_chunks);
-        A.chunk_cap = (uint32_t)std::min<uint64_t>(b->ms_chunk_cap, 0xFFFFFFFFull);
-        A.ctl = b->ms_ctl;
-        A.reached = reinterpret_cast<unsigned long long *>(b->ms_reached);
-        A.traversed = reinterpret_cast<unsigned long long *>(b->ms_reached) + 64ull * k;
-        void *params[] = {&A};
+    auto run = [&]() -> gpma_status {
+        if (levels) {
+            for (uint32_t i = 0; i < k; ++i) {
+                if (!levels[i])
+                    continue;
+                GPMA_TRY(dev_alloc(&stage[i], (uint64_t)nsrc[i] * graphs[i]->row_num));
+                GPMA_CUDA(cudaMemsetAsync(stage[i], 0, sizeof(uint32_t) * nsrc[i] * (uint64_t)graphs[i]->row_num, s));
+            }
+        }
+        BatchBfsPlan P;
+        GPMA_TRY(batch_bfs_plan(b, graphs, srcs, nsrc, k, levels ? stage.data() : nullptr, &P));
+        GPMA_CUDA(cudaMemcpyAsync(b->ms_tab, b->h_ms_tab, P.tab_bytes, cudaMemcpyHostToDevice, s));
+        for (int i = 0; i < BatchBfsPlan::CLEARS; ++i)
+            GPMA_CUDA(cudaMemsetAsync(P.clear_ptr[i], 0, P.clear_bytes[i], s));
         prof_mark(b->profiling, b->ev, 0, s);
-        GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)msbfs_kernel, dim3(grid), dim3(BLOCK), params, 0, s));
+        GPMA_CUDA(P.main.launch_cooperative(s));
         prof_mark(b->profiling, b->ev, 1, s);
-        GPMA_CUDA(cudaMemcpyAsync(b->h_ms_ctl, b->ms_ctl, sizeof(uint32_t) * MS_CTL_WORDS, cudaMemcpyDeviceToHost, s));
-        std::vector<unsigned long long> r(64ull * k + 1);
-        GPMA_CUDA(cudaMemcpyAsync(r.data(), b->ms_reached, sizeof(unsigned long long) * r.size(),
-                                  cudaMemcpyDeviceToHost, s));
+        GPMA_TRY(batch_bfs_enqueue_readback(b, P, s));
         for (uint32_t i = 0; i < k; ++i)
             if (stage[i])
                 GPMA_TRY(copy_any(levels[i], stage[i], sizeof(uint32_t) * nsrc[i] * (uint64_t)graphs[i]->row_num, s));
         GPMA_CUDA(cudaStreamSynchronize(s));
-        b->prof.kernel_launches += 1;
-        b->prof.bfs_kernels++;
         b->prof.bfs_ms += prof_elapsed(b->profiling, b->ev, 0, 1);
-        if (b->h_ms_ctl[MS_ERR]) {
-            set_error("device-side wait gave up in the multi-source BFS kernel (code %u)", b->h_ms_ctl[MS_ERR]);
-            return GPMA_ERR_TIMEOUT;
-        }
-        if (reached) {
-            uint64_t o = 0;
-            for (uint32_t i = 0; i < k; ++i)
-                for (uint32_t j = 0; j < nsrc[i]; ++j)
-                    reached[o++] = r[64ull * i + j];
-        }
-        b->last_traversed = r[64ull * k];
-        b->prof.bfs_edges += r[64ull * k];
-        return GPMA_OK;
+        return batch_bfs_finish(b, nsrc, k, reached);
     };
-    st = step();
+    const gpma_status st = run();
     cleanup();
     return st;
 }

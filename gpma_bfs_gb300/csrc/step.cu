@@ -21,6 +21,9 @@
 // are always those of update_gpma followed by gpma_bfs.
 #include "gpma_internal.cuh"
 
+#include <new>
+#include <vector>
+
 struct gpma_step {
     gpma_graph *g = nullptr;
     cudaGraph_t graph = nullptr;
@@ -87,6 +90,51 @@ gpma_status set_cooperative(cudaGraphNode_t node) {
     cudaLaunchAttributeValue v{};
     v.cooperative = 1;
     GPMA_CUDA(cudaGraphKernelNodeSetAttribute(node, cudaLaunchAttributeCooperative, &v));
+    return GPMA_OK;
+}
+
+// Appends nodes to a chain (each depends on the previous one).
+struct Chain {
+    cudaGraph_t graph;
+    cudaGraphNode_t prev = nullptr;
+    gpma_status copy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind) {
+        cudaGraphNode_t n;
+        GPMA_CUDA(cudaGraphAddMemcpyNode1D(&n, graph, prev ? &prev : nullptr, prev ? 1 : 0, dst, src, bytes, kind));
+        prev = n;
+        return GPMA_OK;
+    }
+    gpma_status zero(void *dst, size_t bytes) {  // bytes: a multiple of 4
+        cudaMemsetParams mp{};
+        mp.dst = dst;
+        mp.value = 0;
+        mp.elementSize = 4;
+        mp.width = bytes / 4;
+        mp.height = 1;
+        mp.pitch = 0;
+        cudaGraphNode_t n;
+        GPMA_CUDA(cudaGraphAddMemsetNode(&n, graph, prev ? &prev : nullptr, prev ? 1 : 0, &mp));
+        prev = n;
+        return GPMA_OK;
+    }
+    gpma_status kernel(KernelLaunch &L, bool cooperative, cudaGraphNode_t *out) {
+        cudaKernelNodeParams kp = L.node();
+        GPMA_CUDA(cudaGraphAddKernelNode(out, graph, prev ? &prev : nullptr, prev ? 1 : 0, &kp));
+        if (cooperative)
+            GPMA_TRY(set_cooperative(*out));
+        prev = *out;
+        return GPMA_OK;
+    }
+};
+
+// Updates a kernel node's arguments in place when they changed.
+gpma_status refresh_kernel(cudaGraphExec_t exec, cudaGraphNode_t node, KernelLaunch &now, KernelLaunch &built,
+                           uint64_t *updates) {
+    if (now.same(built))
+        return GPMA_OK;
+    cudaKernelNodeParams kp = now.node();
+    GPMA_CUDA(cudaGraphExecKernelNodeSetParams(exec, node, &kp));
+    built = now;
+    ++*updates;
     return GPMA_OK;
 }
 
@@ -257,6 +305,181 @@ gpma_status step_run(gpma_step *st, const uint64_t *keys, const uint8_t *values,
 
 }  // namespace gpma
 
+// ---- recorded steps of a batch of graphs ------------------------------------
+// The batched form's step: one packed update of every graph of the step (the
+// gather of the batches into segment-length order, then the persistent
+// update kernel) and one multi-source BFS over all of them, as one graph:
+//   gather table upload -> gather kernel -> update table upload -> update
+//   kernel (cooperative) -> BFS table upload -> 5 BFS clears -> multi-source
+//   BFS kernel (cooperative) -> status, control and count read-back.
+// A step whose batch holds an empty or a bulk-sized (>= 5M keys) part, or
+// whose update needs host work, runs or finishes through the eager calls,
+// which give the same results.
+
+struct gpma_batch_step {
+    gpma_batch *b = nullptr;
+    std::vector<gpma_graph *> graphs;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t n_gather = nullptr, n_update = nullptr, n_ms = nullptr;
+    gpma::KernelLaunch gather, upd, ms;
+    std::vector<unsigned char> baked;  // the pointers, sizes and launch shapes the nodes hold
+    unsigned char *h_stat = nullptr;   // pinned copy of both status slots
+    size_t h_stat_bytes = 0;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    gpma_step_stats stats{};
+};
+
+namespace gpma {
+namespace {
+
+void drop_batch_graph(gpma_batch_step *st) {
+    if (st->exec)
+        cudaGraphExecDestroy(st->exec);
+    if (st->graph)
+        cudaGraphDestroy(st->graph);
+    st->exec = nullptr;
+    st->graph = nullptr;
+}
+
+template <typename T>
+void put(std::vector<unsigned char> &v, const T &x) {
+    const unsigned char *p = reinterpret_cast<const unsigned char *>(&x);
+    v.insert(v.end(), p, p + sizeof(T));
+}
+
+std::vector<unsigned char> bake_batch(const gpma_batch *b, const PackedPlan &pp, size_t tab_bytes,
+                                      const KernelLaunch &upd, const BatchBfsPlan &bp) {
+    std::vector<unsigned char> v;
+    put(v, (const void *)b->h_gather_tab);
+    put(v, (const void *)b->gather_tab);
+    put(v, pp.gtab_bytes);
+    put(v, pp.gather.func);
+    put(v, pp.gather.grid.x);
+    put(v, (const void *)b->buf.h_tab);
+    put(v, (const void *)b->buf.d_tab);
+    put(v, tab_bytes);
+    put(v, upd.func);
+    put(v, upd.grid.x);
+    put(v, upd.smem);
+    put(v, (const void *)b->h_ms_tab);
+    put(v, (const void *)b->ms_tab);
+    put(v, bp.tab_bytes);
+    for (int i = 0; i < BatchBfsPlan::CLEARS; ++i) {
+        put(v, bp.clear_ptr[i]);
+        put(v, bp.clear_bytes[i]);
+    }
+    put(v, bp.main.func);
+    put(v, bp.main.grid.x);
+    put(v, (const void *)b->buf.d_stat);
+    put(v, b->buf.stat_slot);
+    put(v, (const void *)b->ms_ctl);
+    put(v, (const void *)b->h_ms_ctl);
+    put(v, (const void *)b->ms_reached);
+    put(v, (const void *)b->h_ms_reached);
+    put(v, bp.reached_bytes);
+    return v;
+}
+
+gpma_status build_batch_graph(gpma_batch_step *st, PackedPlan &pp, size_t tab_bytes, KernelLaunch &upd,
+                              BatchBfsPlan &bp) {
+    drop_batch_graph(st);
+    gpma_batch *b = st->b;
+    const size_t stat_bytes = 2 * b->buf.stat_slot;
+    if (stat_bytes > st->h_stat_bytes) {
+        if (st->h_stat)
+            cudaFreeHost(st->h_stat);
+        st->h_stat = nullptr;
+        st->h_stat_bytes = 0;
+        GPMA_CUDA(cudaMallocHost((void **)&st->h_stat, stat_bytes));
+        st->h_stat_bytes = stat_bytes;
+    }
+    GPMA_CUDA(cudaGraphCreate(&st->graph, 0));
+    Chain c{st->graph};
+    GPMA_TRY(c.copy(b->gather_tab, b->h_gather_tab, pp.gtab_bytes, cudaMemcpyHostToDevice));
+    GPMA_TRY(c.kernel(pp.gather, false, &st->n_gather));
+    GPMA_TRY(c.copy(b->buf.d_tab, b->buf.h_tab, tab_bytes, cudaMemcpyHostToDevice));
+    GPMA_TRY(c.kernel(upd, true, &st->n_update));
+    GPMA_TRY(c.copy(b->ms_tab, b->h_ms_tab, bp.tab_bytes, cudaMemcpyHostToDevice));
+    for (int i = 0; i < BatchBfsPlan::CLEARS; ++i)
+        GPMA_TRY(c.zero(bp.clear_ptr[i], bp.clear_bytes[i]));
+    GPMA_TRY(c.kernel(bp.main, true, &st->n_ms));
+    GPMA_TRY(c.copy(st->h_stat, b->buf.d_stat, stat_bytes, cudaMemcpyDeviceToHost));
+    GPMA_TRY(c.copy(b->h_ms_ctl, b->ms_ctl, bp.ctl_bytes, cudaMemcpyDeviceToHost));
+    GPMA_TRY(c.copy(b->h_ms_reached, b->ms_reached, bp.reached_bytes, cudaMemcpyDeviceToHost));
+    GPMA_CUDA(cudaGraphInstantiate(&st->exec, st->graph, 0));
+    st->gather = pp.gather;
+    st->upd = upd;
+    st->ms = bp.main;
+    st->baked = bake_batch(b, pp, tab_bytes, upd, bp);
+    st->stats.builds++;
+    return GPMA_OK;
+}
+
+}  // namespace
+
+gpma_status batch_step_run(gpma_batch_step *st, const uint64_t *keys, const uint8_t *values, const uint64_t *offsets,
+                           const uint32_t *const *srcs, const uint32_t *nsrc, uint64_t *reached, cudaStream_t s) {
+    gpma_batch *b = st->b;
+    gpma_graph *const *graphs = st->graphs.data();
+    const uint32_t k = (uint32_t)st->graphs.size();
+    st->stats.runs++;
+    bool eager = false;
+    for (uint32_t i = 0; i < k; ++i) {
+        const uint64_t c = offsets[i + 1] - offsets[i];
+        eager = eager || c == 0 || c >= SIGNIFICANT_INSERTS;
+    }
+    if (eager) {
+        st->stats.host_runs++;
+        GPMA_TRY(gpma_batch_update_packed(b, graphs, keys, values, offsets, k, s));
+        return batch_bfs_run(b, graphs, srcs, nsrc, k, nullptr, reached, s);
+    }
+    for (uint32_t i = 0; i < k; ++i) {
+        graphs[i]->stats.updates++;
+        graphs[i]->stats.submitted += offsets[i + 1] - offsets[i];
+    }
+    PackedPlan pp;
+    GPMA_TRY(packed_plan(b, graphs, keys, values, offsets, k, &pp));
+    GPMA_TRY(packed_stage(b, pp, keys, values, offsets, s, /*with_table=*/false));
+    size_t tab_bytes = 0;
+    KernelLaunch upd;
+    GPMA_TRY(update_plan(pp.gs.data(), pp.off.data(), pp.m, b->buf, b->sms, true, &tab_bytes, &upd));
+    BatchBfsPlan bp;
+    GPMA_TRY(batch_bfs_plan(b, graphs, srcs, nsrc, k, nullptr, &bp));
+    if (!st->exec || bake_batch(b, pp, tab_bytes, upd, bp) != st->baked) {
+        GPMA_TRY(build_batch_graph(st, pp, tab_bytes, upd, bp));
+    } else {
+        GPMA_TRY(refresh_kernel(st->exec, st->n_gather, pp.gather, st->gather, &st->stats.param_updates));
+        GPMA_TRY(refresh_kernel(st->exec, st->n_update, upd, st->upd, &st->stats.param_updates));
+        GPMA_TRY(refresh_kernel(st->exec, st->n_ms, bp.main, st->ms, &st->stats.param_updates));
+    }
+    GPMA_TRY(update_clear(b->buf, s));
+    const unsigned char *stat = st->h_stat + b->buf.parity * b->buf.stat_slot;
+    GPMA_CUDA(cudaEventRecord(st->ev[0], s));
+    GPMA_CUDA(cudaGraphLaunch(st->exec, s));
+    GPMA_CUDA(cudaEventRecord(st->ev[1], s));
+    GPMA_CUDA(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, st->ev[0], st->ev[1]) != cudaSuccess) {
+        cudaGetLastError();
+        ms = 0.f;
+    }
+    st->stats.last_ms = ms;
+    st->stats.total_ms += ms;
+    st->stats.graph_launches++;
+    b->prof.kernel_launches += 2;  // gather and update; the BFS is counted by its finish
+    const bool host_work = update_needs_host(stat, pp.m);
+    GPMA_TRY(update_finish(pp.gs.data(), pp.m, b->buf, stat, s, nullptr, 0.0));
+    if (host_work) {
+        // the arrays changed on the host after the recorded BFS ran: redo it
+        st->stats.host_runs++;
+        return batch_bfs_run(b, graphs, srcs, nsrc, k, nullptr, reached, s);
+    }
+    return batch_bfs_finish(b, nsrc, k, reached);
+}
+
+}  // namespace gpma
+
 extern "C" {
 
 gpma_status gpma_step_create(gpma_graph *g, gpma_step **out) {
@@ -315,6 +538,105 @@ gpma_status gpma_step_run(gpma_step *st, const uint64_t *keys, const uint8_t *va
 gpma_status gpma_step_get_stats(const gpma_step *st, gpma_step_stats *out) {
     if (!st || !out) {
         gpma::set_error("gpma_step_get_stats: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    *out = st->stats;
+    return GPMA_OK;
+}
+
+gpma_status gpma_batch_step_create(gpma_batch *b, gpma_graph *const *graphs, uint32_t k, gpma_batch_step **out) {
+    if (!b || !out || (k && !graphs) || k == 0) {
+        gpma::set_error("gpma_batch_step_create: null argument or no graphs");
+        return GPMA_ERR_INVALID;
+    }
+    *out = nullptr;
+    for (uint32_t i = 0; i < k; ++i) {
+        if (!graphs[i]) {
+            gpma::set_error("gpma_batch_step_create: graph %u is null", i);
+            return GPMA_ERR_INVALID;
+        }
+        for (uint32_t j = 0; j < i; ++j)
+            if (graphs[j] == graphs[i]) {
+                gpma::set_error("gpma_batch_step_create: graph %u appears twice", i);
+                return GPMA_ERR_INVALID;
+            }
+    }
+    gpma_batch_step *st = new (std::nothrow) gpma_batch_step();
+    if (!st) {
+        gpma::set_error("gpma_batch_step_create: out of host memory");
+        return GPMA_ERR_NOMEM;
+    }
+    st->b = b;
+    st->graphs.assign(graphs, graphs + k);
+    for (int i = 0; i < 2; ++i) {
+        cudaError_t e = cudaEventCreate(&st->ev[i]);
+        if (e != cudaSuccess) {
+            gpma_batch_step_destroy(st);
+            return gpma::cuda_fail(e, "cudaEventCreate");
+        }
+    }
+    *out = st;
+    return GPMA_OK;
+}
+
+gpma_status gpma_batch_step_destroy(gpma_batch_step *st) {
+    if (!st)
+        return GPMA_OK;
+    gpma::drop_batch_graph(st);
+    for (int i = 0; i < 2; ++i)
+        if (st->ev[i])
+            cudaEventDestroy(st->ev[i]);
+    if (st->h_stat)
+        cudaFreeHost(st->h_stat);
+    delete st;
+    return GPMA_OK;
+}
+
+gpma_status gpma_batch_step_run(gpma_batch_step *st, const uint64_t *keys, const uint8_t *values,
+                                const uint64_t *offsets, const uint32_t *const *srcs, const uint32_t *nsrc,
+                                uint64_t *reached, void *stream) {
+    if (!st || !offsets || !srcs || !nsrc) {
+        gpma::set_error("gpma_batch_step_run: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    const uint32_t k = (uint32_t)st->graphs.size();
+    if (offsets[k] > offsets[0] && (!keys || !values)) {
+        gpma::set_error("gpma_batch_step_run: null keys or values");
+        return GPMA_ERR_INVALID;
+    }
+    if (offsets[k] - offsets[0] >= (1ull << 31)) {
+        gpma::set_error("gpma_batch_step_run: %llu keys in one step exceed 2^31",
+                        (unsigned long long)(offsets[k] - offsets[0]));
+        return GPMA_ERR_CAPACITY;
+    }
+    uint64_t nodes = 0;
+    for (uint32_t i = 0; i < k; ++i) {
+        if (offsets[i + 1] < offsets[i]) {
+            gpma::set_error("gpma_batch_step_run: decreasing offsets at %u", i);
+            return GPMA_ERR_INVALID;
+        }
+        if (!srcs[i] || nsrc[i] == 0 || nsrc[i] > 64) {
+            gpma::set_error("gpma_batch_step_run: graph %u: null sources or source count not in 1..64", i);
+            return GPMA_ERR_INVALID;
+        }
+        for (uint32_t j = 0; j < nsrc[i]; ++j)
+            if (srcs[i][j] >= st->graphs[i]->row_num) {
+                gpma::set_error("gpma_batch_step_run: graph %u: source %u out of range (row_num %u)", i, srcs[i][j],
+                                st->graphs[i]->row_num);
+                return GPMA_ERR_INVALID;
+            }
+        nodes += st->graphs[i]->row_num;
+    }
+    if (nodes >= (1ull << 32)) {
+        gpma::set_error("gpma_batch_step_run: %llu nodes in one step exceed 2^32", (unsigned long long)nodes);
+        return GPMA_ERR_CAPACITY;
+    }
+    return gpma::batch_step_run(st, keys, values, offsets, srcs, nsrc, reached, (cudaStream_t)stream);
+}
+
+gpma_status gpma_batch_step_get_stats(const gpma_batch_step *st, gpma_step_stats *out) {
+    if (!st || !out) {
+        gpma::set_error("gpma_batch_step_get_stats: null argument");
         return GPMA_ERR_INVALID;
     }
     *out = st->stats;

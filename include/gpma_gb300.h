@@ -202,6 +202,24 @@ GPMA_API gpma_status gpma_batch_bfs_multi(gpma_batch *b, gpma_graph *const *grap
                                           const uint32_t *nsrc, uint32_t k, uint32_t *const *levels,
                                           uint64_t *reached, void *stream);
 
+/* The batched form's step (no reference counterpart): one packed update of
+ * every graph of the step (as gpma_batch_update_packed) and one multi-source
+ * BFS over all of them (as gpma_batch_bfs_multi without levels), recorded as
+ * one CUDA graph. The graphs are fixed at creation (order kept); keys/values
+ * are host or device memory, offsets (k + 1), srcs[i] (nsrc[i] in 1..64
+ * sources) and reached (optional, sum of nsrc) are host memory. A step with
+ * an empty or a bulk-sized (>= 5,000,000 keys) part, or whose update needs
+ * host work, runs or finishes through the eager calls; results are always
+ * those of the two calls. Destroy a step before its batch and graphs. */
+typedef struct gpma_batch_step gpma_batch_step;
+GPMA_API gpma_status gpma_batch_step_create(gpma_batch *b, gpma_graph *const *graphs, uint32_t k,
+                                            gpma_batch_step **out);
+GPMA_API gpma_status gpma_batch_step_destroy(gpma_batch_step *st);
+GPMA_API gpma_status gpma_batch_step_run(gpma_batch_step *st, const uint64_t *keys, const uint8_t *values,
+                                         const uint64_t *offsets, const uint32_t *const *srcs, const uint32_t *nsrc,
+                                         uint64_t *reached, void *stream);
+GPMA_API gpma_status gpma_batch_step_get_stats(const gpma_batch_step *st, gpma_step_stats *out);
+
 /* ---- served form ----------------------------------------------------------
  * No reference counterpart. A gpma_server keeps many graphs resident on the
  * current device and serves update batches and BFS queries against them with

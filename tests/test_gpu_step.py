@@ -95,3 +95,57 @@ def test_step_rejected_batch_then_recovers(built_lib):
         assert np.array_equal(got, want) and _same_layout(eager, graphed)
     eager.close()
     graphed.close()
+
+
+def test_batch_step_matches_eager_calls(built_lib):
+    """The batched form's recorded step equals update_packed + bfs_multi:
+    every graph's layout and every source's reach, step by step, including a
+    step with an empty part (eager fallback) and device-resident batches."""
+    import torch
+
+    import gpma_bfs_gb300 as G
+    from gpma_bfs_gb300.workloads import SlidingStream, batched_graphs
+
+    specs = batched_graphs(24, seed=9, min_edges=5_000, max_edges=200_000)
+    rng = np.random.default_rng(12)
+    ge = [G.GPMA(n) for n, _ in specs]
+    gr = [G.GPMA(n) for n, _ in specs]
+    se = [SlidingStream(k) for _, k in specs]
+    sr = [SlidingStream(k) for _, k in specs]
+    be, br = G.Batch(), G.Batch()
+    loads = [s.load() for s in se]
+    for s in sr:
+        s.load()
+    off = np.concatenate([[0], np.cumsum([len(x[0]) for x in loads])]).astype(np.uint64)
+    keys, vals = np.concatenate([x[0] for x in loads]), np.concatenate([x[1] for x in loads])
+    be.update_packed(ge, keys, vals, off)
+    br.update_packed(gr, keys, vals, off)
+    sources = [rng.choice(n, 16, replace=False).astype(np.uint32) for n, _ in specs]
+    step = br.step(gr)
+    for j in range(8):
+        sizes = np.exp(rng.uniform(np.log(50), np.log(40_000), len(specs))).astype(np.int64)
+        parts = [s.step(int(z)) for s, z in zip(se, sizes)]
+        for s, z in zip(sr, sizes):
+            s.step(int(z))
+        if j == 5:
+            parts[3] = (parts[3][0][:0], parts[3][1][:0])  # an empty part: the step runs the eager calls
+        o = np.concatenate([[0], np.cumsum([len(p[0]) for p in parts])]).astype(np.uint64)
+        k = np.concatenate([p[0] for p in parts])
+        v = np.concatenate([p[1] for p in parts])
+        if j % 2:
+            k, v = torch.from_numpy(k.view(np.int64)).cuda(), torch.from_numpy(v).cuda()
+        be.update_packed(ge, k, v, o)
+        want = be.bfs_multi(ge, sources)[1]
+        got = step.run(k, v, o, sources)
+        assert all(np.array_equal(x, y) for x, y in zip(want, got)), f"step {j}: reach"
+        for i in range(len(specs)):
+            assert all(np.array_equal(x, y) for x, y in zip(ge[i].export_layout(), gr[i].export_layout())), \
+                f"step {j} graph {i}"
+            assert gr[i].validate() == 0
+    st = step.stats()
+    assert st["runs"] == 8 and st["host_runs"] >= 1 and st["graph_launches"] >= 6 and st["builds"] >= 1
+    step.close()
+    be.close()
+    br.close()
+    for g in ge + gr:
+        g.close()
