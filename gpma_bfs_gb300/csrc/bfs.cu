@@ -190,12 +190,20 @@ __device__ __forceinline__ uint32_t frontier_pass(const BfsArgs &A, uint32_t *fr
                                                   uint32_t next_level, uint32_t words, uint32_t gwarp, uint32_t nwarps,
                                                   uint32_t lane, uint32_t &slots) {
     uint32_t fresh = 0;
-    for (uint32_t wi = gwarp; wi < words; wi += nwarps) {
-        const uint32_t f = front_cur[wi];
-        if (f == 0)
-            continue;
-        if (CLEAR && lane == 0)
-            front_cur[wi] = 0;
+    // warp gwarp owns words gwarp, gwarp + nwarps, ... (hub rows spread over
+    // the grid); it reads 32 of them at once, one per lane, and walks the
+    // non-empty ones, so a sparse frontier costs one load round per 32 words
+    for (uint32_t it = 0; gwarp + it * nwarps < words; it += 32) {
+      const uint32_t wl = gwarp + (it + lane) * nwarps;
+      const uint32_t mine = wl < words ? front_cur[wl] : 0u;
+      uint32_t pending = __ballot_sync(0xFFFFFFFFu, mine != 0u);
+      if (CLEAR && mine)
+          front_cur[wl] = 0;
+      while (pending) {
+        const uint32_t src = __ffs(pending) - 1;
+        pending &= pending - 1;
+        const uint32_t wi = gwarp + (it + src) * nwarps;
+        const uint32_t f = __shfl_sync(0xFFFFFFFFu, mine, src);
         uint32_t b = 0, e = 0, len = 0;
         if (f & (1u << lane)) {
             const uint32_t u = (wi << 5) + lane;
@@ -240,6 +248,7 @@ __device__ __forceinline__ uint32_t frontier_pass(const BfsArgs &A, uint32_t *fr
                 sl[j] = lb_slot(p0 + 32 * j + lane, total, b, excl);
             fresh += visit_slots(A, sl, next_level, front_next);
         }
+      }
     }
     return fresh;
 }
