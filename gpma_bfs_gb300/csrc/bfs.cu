@@ -53,16 +53,22 @@ enum : uint32_t {
 // every warp of the grid shares in a second phase of the level; shorter rows
 // of one frontier word are walked together by one warp. (With node ids
 // ordered by degree, one word can otherwise hold 32 heavy rows.)
-// A warp walks LANE_SLOTS slots per lane per step (build option), all loads
-// of a step issued before any claim; a chunk is one step of a warp.
+// A warp walks short rows LANE_SLOTS slots per lane per step and chunks
+// CHUNK_LANE_SLOTS per lane (build options), all loads of a step issued
+// before any claim; a chunk is one step of a warp.
 #ifndef GPMA_BFS_LANE_SLOTS
 #define GPMA_BFS_LANE_SLOTS 4
 #endif
+#ifndef GPMA_BFS_CHUNK_LANE_SLOTS
+#define GPMA_BFS_CHUNK_LANE_SLOTS 8
+#endif
 constexpr uint32_t LANE_SLOTS = GPMA_BFS_LANE_SLOTS;
-static_assert(LANE_SLOTS >= 1 && LANE_SLOTS <= 8, "BFS lane slots out of range");
+constexpr uint32_t CHUNK_LANE_SLOTS = GPMA_BFS_CHUNK_LANE_SLOTS;
+static_assert(LANE_SLOTS >= 1 && LANE_SLOTS <= 8 && CHUNK_LANE_SLOTS >= LANE_SLOTS && CHUNK_LANE_SLOTS <= 8,
+              "BFS lane slots out of range");
 constexpr uint32_t STEP_SLOTS = 32 * LANE_SLOTS;
 constexpr uint32_t BIG_ROW = STEP_SLOTS / 2;
-constexpr uint32_t CHUNK_SLOTS = STEP_SLOTS;
+constexpr uint32_t CHUNK_SLOTS = 32 * CHUNK_LANE_SLOTS;
 // Chunk list entries for an array of `size` slots: rows over BIG_ROW slots
 // yield at most len/64 + 1 chunks each and there are at most size/33 of them,
 // so one level queues fewer than size/64 + size/33 < size/16 chunks; the list
@@ -86,14 +92,15 @@ struct BfsArgs {
     unsigned long long *stamps;  // per-level profile (CTL_PROFILE_LEVELS stamps + info words) or null
 };
 
-// LANE_SLOTS edge slots of one lane (SIZE_NONE: absent): every key, value
-// and visited word is loaded before any claim, so each lane keeps several
+// N edge slots of one lane (SIZE_NONE: absent): every key, value and
+// visited word is loaded before any claim, so each lane keeps several
 // requests in flight. Returns the number of nodes this lane claimed.
-__device__ __forceinline__ uint32_t visit_slots(const BfsArgs &A, const uint32_t (&sl)[LANE_SLOTS],
-                                                uint32_t next_level, uint32_t *front_next) {
-    uint32_t w[LANE_SLOTS], seen[LANE_SLOTS];
+template <uint32_t N>
+__device__ __forceinline__ uint32_t visit_slots(const BfsArgs &A, const uint32_t (&sl)[N], uint32_t next_level,
+                                                uint32_t *front_next) {
+    uint32_t w[N], seen[N];
 #pragma unroll
-    for (uint32_t j = 0; j < LANE_SLOTS; ++j) {
+    for (uint32_t j = 0; j < N; ++j) {
         uint64_t k = KEY_NONE;
         uint8_t v = 0;
         if (sl[j] != SIZE_NONE) {
@@ -104,12 +111,12 @@ __device__ __forceinline__ uint32_t visit_slots(const BfsArgs &A, const uint32_t
         seen[j] = (w[j] != 0xFFFFFFFFu && v != 0 && w[j] < A.n) ? 0u : 0xFFFFFFFFu;
     }
 #pragma unroll
-    for (uint32_t j = 0; j < LANE_SLOTS; ++j)
+    for (uint32_t j = 0; j < N; ++j)
         if (!seen[j])
             seen[j] = A.visited[w[j] >> 5];
     uint32_t fresh = 0;
 #pragma unroll
-    for (uint32_t j = 0; j < LANE_SLOTS; ++j) {
+    for (uint32_t j = 0; j < N; ++j) {
         const uint32_t bit = 1u << (w[j] & 31);
         if (!(seen[j] & bit) && !(atomicOr(&A.visited[w[j] >> 5], bit) & bit)) {
             A.levels[w[j]] = next_level;
@@ -246,7 +253,7 @@ __device__ __forceinline__ uint32_t frontier_pass(const BfsArgs &A, uint32_t *fr
 #pragma unroll
             for (uint32_t j = 0; j < LANE_SLOTS; ++j)
                 sl[j] = lb_slot(p0 + 32 * j + lane, total, b, excl);
-            fresh += visit_slots(A, sl, next_level, front_next);
+            fresh += visit_slots<LANE_SLOTS>(A, sl, next_level, front_next);
         }
       }
     }
@@ -367,12 +374,12 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
             const uint32_t nloc = min(s_nch, LOCAL_CHUNKS);
             for (uint32_t c = threadIdx.x >> 5; c < nloc; c += BLOCK / 32) {
                 const uint2 ch = s_chunks[c];
-                for (uint32_t s0 = ch.x; s0 < ch.y; s0 += STEP_SLOTS) {
-                    uint32_t sl[LANE_SLOTS];
+                for (uint32_t s0 = ch.x; s0 < ch.y; s0 += CHUNK_SLOTS) {
+                    uint32_t sl[CHUNK_LANE_SLOTS];
 #pragma unroll
-                    for (uint32_t j = 0; j < LANE_SLOTS; ++j)
+                    for (uint32_t j = 0; j < CHUNK_LANE_SLOTS; ++j)
                         sl[j] = s0 + 32 * j + lane < ch.y ? s0 + 32 * j + lane : SIZE_NONE;
-                    fresh += visit_slots(A, sl, next_level, front_next);
+                    fresh += visit_slots<CHUNK_LANE_SLOTS>(A, sl, next_level, front_next);
                 }
             }
             added += level_count(A, i, fresh, lane);
@@ -385,16 +392,16 @@ __global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
             if (!grid_barrier(bar, err))
                 return;
         }
-        // Phase 2: long-row chunks, one warp per chunk (64 slots = one step).
+        // Phase 2: long-row chunks, one warp per chunk (one step).
         const uint32_t nch_all = min(cta_broadcast_read(chunk_cnt), A.chunk_cap);
         for (uint32_t c = gwarp; c < nch_all; c += nwarps) {
             const uint2 ch = A.chunks[c];
-            for (uint32_t s0 = ch.x; s0 < ch.y; s0 += STEP_SLOTS) {
-                uint32_t sl[LANE_SLOTS];
+            for (uint32_t s0 = ch.x; s0 < ch.y; s0 += CHUNK_SLOTS) {
+                uint32_t sl[CHUNK_LANE_SLOTS];
 #pragma unroll
-                for (uint32_t j = 0; j < LANE_SLOTS; ++j)
+                for (uint32_t j = 0; j < CHUNK_LANE_SLOTS; ++j)
                     sl[j] = s0 + 32 * j + lane < ch.y ? s0 + 32 * j + lane : SIZE_NONE;
-                fresh += visit_slots(A, sl, next_level, front_next);
+                fresh += visit_slots<CHUNK_LANE_SLOTS>(A, sl, next_level, front_next);
             }
         }
         added += level_count(A, i, fresh, lane);
