@@ -407,6 +407,7 @@ gpma_status gpma_server_run_round(gpma_server *s, double now, gpma_round_info *i
     // ---- execute -------------------------------------------------------------
     gpma_status st = GPMA_OK;
     std::vector<uint64_t> reached;
+    double upd_seconds = 0.0;
     if (!s->plan_only) {
         gpma_profile p0{};
         gpma_batch_get_profile(s->batch, &p0);
@@ -424,6 +425,9 @@ gpma_status gpma_server_run_round(gpma_server *s, double now, gpma_round_info *i
             if (st == GPMA_OK)
                 st = gpma_batch_update_packed(s->batch, gs.data(), s->h_keys, s->h_vals, off.data(),
                                               (uint32_t)gs.size(), s->stream);
+            // the call returns once the update is on the device: its requests
+            // are done here, before the round's searches run
+            upd_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         }
         std::vector<std::vector<uint32_t>> lvl(bfs.size());
         if (st == GPMA_OK && !bfs.empty()) {
@@ -487,11 +491,11 @@ gpma_status gpma_server_run_round(gpma_server *s, double now, gpma_round_info *i
     ri.seconds = seconds;
 
     // ---- complete --------------------------------------------------------------
-    auto finish = [&](Request *r) {
+    auto finish = [&](Request *r, double took) {
         r->state = st == GPMA_OK ? GPMA_REQ_DONE : GPMA_REQ_FAILED;
         r->status = st;
         r->start = now;
-        r->done = now + seconds;
+        r->done = now + took;
         r->round = round_no;
         s->last_round.push_back(r->id);
     };
@@ -507,7 +511,7 @@ gpma_status gpma_server_run_round(gpma_server *s, double now, gpma_round_info *i
         r->keys.shrink_to_fit();
         r->vals.clear();
         r->vals.shrink_to_fit();
-        finish(r);
+        finish(r, upd_seconds);
     }
     uint64_t lane_base = 0;
     for (const BfsEntry &e : bfs) {
@@ -521,7 +525,7 @@ gpma_status gpma_server_run_round(gpma_server *s, double now, gpma_round_info *i
                 r->reached[j] = reached[lane_base + r->lane + j];
             ri.bfs_requests++;
             ri.sources += r->nsrc;
-            finish(r);
+            finish(r, seconds);
         }
         lane_base += e.lanes;
         ri.bfs_graphs++;

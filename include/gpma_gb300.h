@@ -231,8 +231,9 @@ GPMA_API gpma_status gpma_batch_step_get_stats(const gpma_batch_step *st, gpma_s
  * arrive while a round runs join a later round. A graph's requests therefore
  * take effect in arrival order and every result equals what the same requests
  * give applied to that graph alone. Time is virtual: the caller passes the
- * current time to each round, and a round's requests complete at that time
- * plus the round's measured wall-clock duration.
+ * current time to each round; a round's updates complete at that time plus
+ * the measured wall-clock time of its update launch, its searches at that
+ * time plus the whole round's.
  *
  * Admission. A graph is admitted only if its estimated device bytes fit the
  * HBM budget; an update joins a round only if the graph's worst-case growth
