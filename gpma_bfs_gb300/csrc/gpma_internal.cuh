@@ -53,8 +53,8 @@ enum : uint32_t {
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;
 
 struct GridBarrier {
-    unsigned int count;
-    unsigned int gen;
+    unsigned int count;  // tickets taken (zero at the start of every launch)
+    unsigned int gen;    // generation of grid_barrier_gen
 };
 
 // Written by the update kernel, read back once per update.
@@ -460,12 +460,54 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) { return *(const volatile uint32_t *)p; }
 
-// Sense-free generation barrier across the CTAs of a cooperative launch.
-// Every wait is bounded: after WAIT_LIMIT_NS the CTA records
-// DERR_BARRIER_TIMEOUT and returns false; CTAs that see an error stop waiting.
+// Ticket barrier across the CTAs of a cooperative launch. Each CTA takes a
+// ticket from one counter (it must start each launch at zero) and waits
+// until the counter reaches the end of its ticket's round of gridDim.x;
+// there is no separate release write, so a barrier costs one atomic per CTA
+// and polling (measured 1.35 us at 304 CTAs against 2.8 us for a
+// count-then-generation barrier). Every wait is bounded: after WAIT_LIMIT_NS
+// the CTA records DERR_BARRIER_TIMEOUT and returns false; CTAs that see an
+// error stop waiting.
 __device__ __forceinline__ bool grid_barrier(GridBarrier *bar, uint32_t *err) {
     __syncthreads();
     __shared__ uint32_t s_ok;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned int ticket = atomicAdd(&bar->count, 1u);
+        const unsigned int target = (ticket / gridDim.x + 1) * gridDim.x;
+        uint64_t t0 = 0;
+        unsigned ns = 16;
+        for (;;) {
+            unsigned int c;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(&bar->count) : "memory");
+            if ((int)(c - target) >= 0)
+                break;
+            if (ld_volatile(err) != 0)
+                break;
+            if (t0 == 0)
+                t0 = globaltimer_ns();
+            __nanosleep(ns);
+            if (ns < 128)
+                ns <<= 1;
+            if (globaltimer_ns() - t0 > WAIT_LIMIT_NS) {
+                atomicCAS(err, 0u, DERR_BARRIER_TIMEOUT);
+                break;
+            }
+        }
+        __threadfence();
+        s_ok = ld_volatile(err) == 0;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Count-then-generation barrier over the same two words (the count returns
+// to zero, the last arriver advances the generation the others poll). Slower
+// than the ticket barrier in isolation, but measured faster inside the
+// multi-source BFS, whose 900-odd CTAs poll while others still work.
+__device__ __forceinline__ bool grid_barrier_gen(GridBarrier *bar, uint32_t *err) {
+    __syncthreads();
+    __shared__ uint32_t s_okg;
     if (threadIdx.x == 0) {
         volatile unsigned int *vgen = &bar->gen;
         unsigned int g0 = *vgen;
@@ -491,10 +533,10 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *bar, uint32_t *err) {
             }
         }
         __threadfence();
-        s_ok = ld_volatile(err) == 0;
+        s_okg = ld_volatile(err) == 0;
     }
     __syncthreads();
-    return s_ok != 0;
+    return s_okg != 0;
 }
 
 // One volatile read per CTA, broadcast through shared memory: a word that

@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
         if (Gr.levels)
             Gr.levels[(size_t)j * Gr.n + s] = 1;
     }
-    if (!grid_barrier(bar, err))
+    if (!grid_barrier_gen(bar, err))
         return;
     uint32_t level = 1;
     for (;; ++level) {
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
                     traversed += ms_visit(A, A.gr[rg], rg, rb + (p - rex), rf) * (unsigned long long)__popcll(rf);
             }
         }
-        if (!dense && !grid_barrier(bar, err))
+        if (!dense && !grid_barrier_gen(bar, err))
             return;
         // expand, phase 2: long-row chunks
         const uint32_t nch_all = dense ? 0u : min(cta_broadcast_read(chunk_cnt), A.chunk_cap);
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
             for (uint32_t s = ch.x + lane; s < ch.y; s += 32)
                 traversed += ms_visit(A, Gr, ch.z, s, fm) * (unsigned long long)__popcll(fm);
         }
-        if (!grid_barrier(bar, err))
+        if (!grid_barrier_gen(bar, err))
             return;
         // commit
         uint32_t changed = 0;
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
             fnext += __shfl_xor_sync(0xFFFFFFFFu, fnext, d);
         if (lane == 0 && fnext)
             atomicAdd(fslots(A, level + 1), fnext);
-        if (!grid_barrier(bar, err))
+        if (!grid_barrier_gen(bar, err))
             return;
         if (cta_broadcast_read(A.ctl + MS_CHANGE + level % 3) == 0)
             break;
