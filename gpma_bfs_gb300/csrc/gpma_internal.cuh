@@ -494,7 +494,9 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *bar, uint32_t *err) {
                 break;
             }
         }
-        __threadfence();
+        // no trailing fence: the arrivals are releases (fence, then the
+        // atomic) and the load that saw the last one is an acquire; the CTA
+        // barrier below passes that order on to the other threads
         s_ok = ld_volatile(err) == 0;
     }
     __syncthreads();
