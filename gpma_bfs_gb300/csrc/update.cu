@@ -723,7 +723,6 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
     {
         const uint32_t trivial = sort_trivial_mask(A.sort_hist + (size_t)(A.G == 1 ? 0 : A.G) * 2048, A.n);
         const uint32_t tiles = A.toff[A.G];
-        __shared__ uint32_t s_tile;
         for (int p = 0; p < 8; ++p) {
             if (trivial & (1u << p))
                 continue;
@@ -731,17 +730,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             const uint8_t *inv = sel ? A.bv[1] : A.bv[0];
             uint64_t *outk = sel ? A.bk[0] : A.bk[1];
             uint8_t *outv = sel ? A.bv[0] : A.bv[1];
-            for (;;) {
-                if (threadIdx.x == 0)
-                    s_tile = atomicAdd(&A.sort_tiles[p], 1u);
-                __syncthreads();
-                const uint32_t tile = s_tile;
-                __syncthreads();
-                if (tile >= tiles)
-                    break;
+            // CTA b takes tiles b, b + G, b + 2G, ... in order: every look-back
+            // waits on lower tiles only, and the lowest unfinished tile never
+            // waits on anything unfinished, so the pass always progresses
+            for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
                 sort_tile(p, tile, ink, inv, outk, outv, A.boff, A.toff, A.G, A.sort_hist, A.sort_status, st, smem,
                           tmp);
-            }
             sel ^= 1u;
             if (!grid_barrier(&st->bar, &st->err))
                 return;
