@@ -67,12 +67,14 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     sort_items = os.environ.get("GPMA_SORT_ITEMS", "8")
     lane_slots = os.environ.get("GPMA_BFS_LANE_SLOTS", "4")
+    lookback = os.environ.get("GPMA_SORT_LOOKBACK", "8")
     stamp = BUILD / "options.txt"
-    options = f"GPMA_SORT_ITEMS={sort_items}\nGPMA_BFS_LANE_SLOTS={lane_slots}\n"
+    options = f"GPMA_SORT_ITEMS={sort_items}\nGPMA_BFS_LANE_SLOTS={lane_slots}\nGPMA_SORT_LOOKBACK={lookback}\n"
     if not stamp.exists() or stamp.read_text() != options:
         stamp.write_text(options)
     NVCC_FLAGS.append(f"-DGPMA_SORT_ITEMS={sort_items}")
     NVCC_FLAGS.append(f"-DGPMA_BFS_LANE_SLOTS={lane_slots}")
+    NVCC_FLAGS.append(f"-DGPMA_SORT_LOOKBACK={lookback}")
     HEADERS.append(stamp)
     jobs = []
     objs = []

@@ -26,6 +26,11 @@ namespace gpma {
 #define GPMA_SORT_ITEMS 8
 #endif
 constexpr int SORT_ITEMS = GPMA_SORT_ITEMS;
+// Predecessor tiles a look-back step reads at once (build option).
+#ifndef GPMA_SORT_LOOKBACK
+#define GPMA_SORT_LOOKBACK 8
+#endif
+constexpr uint32_t SORT_LOOKBACK = GPMA_SORT_LOOKBACK;
 constexpr uint32_t SORT_TILE = BLOCK * SORT_ITEMS;
 static_assert(SORT_TILE * 9 + (BLOCK / 32 + 2) * 256 * 4 <= UPDATE_SMEM, "sort tile exceeds the update kernel's smem");
 constexpr uint32_t SORT_FLAG_AGG = 1u << 30;
@@ -152,13 +157,36 @@ __device__ void sort_tile(int pass, uint32_t tile, const uint64_t *__restrict__ 
         atomicExch(&status[(size_t)tile * 256 + d], SORT_FLAG_INC | local);
     } else {
         atomicExch(&status[(size_t)tile * 256 + d], SORT_FLAG_AGG | local);
+        // windows of LOOKBACK predecessors are read at once and summed
+        // nearest first, up to the first inclusive value or unpublished word
         int64_t t = (int64_t)tile - 1;
         uint64_t t0 = 0;
         unsigned ns = 32;
         while (t >= (int64_t)first_tile) {
-            uint32_t w = ld_volatile(&status[(size_t)t * 256 + d]);
-            uint32_t flag = w & ~SORT_VALUE_MASK;
-            if (flag == 0) {
+            uint32_t w[SORT_LOOKBACK];
+#pragma unroll
+            for (uint32_t i = 0; i < SORT_LOOKBACK; ++i)
+                w[i] = t - (int64_t)i >= (int64_t)first_tile ? ld_volatile(&status[(size_t)(t - i) * 256 + d])
+                                                              : SORT_FLAG_INC;  // never read: the first tile is inclusive
+            uint32_t take = 0;
+            bool inc = false, blocked = false;
+#pragma unroll
+            for (uint32_t i = 0; i < SORT_LOOKBACK; ++i) {
+                if (inc || blocked)
+                    continue;
+                const uint32_t flag = w[i] & ~SORT_VALUE_MASK;
+                if (flag == 0) {
+                    blocked = true;
+                    continue;
+                }
+                prefix += w[i] & SORT_VALUE_MASK;
+                ++take;
+                inc = flag == SORT_FLAG_INC;
+            }
+            if (inc)
+                break;
+            t -= take;
+            if (blocked) {
                 if (t0 == 0)
                     t0 = globaltimer_ns();
                 __nanosleep(ns);
@@ -168,12 +196,7 @@ __device__ void sort_tile(int pass, uint32_t tile, const uint64_t *__restrict__ 
                     atomicCAS(&st->err, 0u, DERR_LOOKBACK_TIMEOUT);
                     break;
                 }
-                continue;
             }
-            prefix += w & SORT_VALUE_MASK;
-            if (flag == SORT_FLAG_INC)
-                break;
-            --t;
         }
         atomicExch(&status[(size_t)tile * 256 + d], SORT_FLAG_INC | (prefix + local));
     }
