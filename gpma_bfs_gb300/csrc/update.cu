@@ -991,16 +991,20 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         {
             uint32_t ch = 0, ci = 0;
             for (uint32_t w = lo + threadIdx.x; w < hi; w += BLOCK) {
-                if (A.wflag[w])
+                // the window's and its left neighbour's fields in one round
+                const uint32_t f0 = A.wflag[w], fl = w > 0 ? A.wflag[w - 1] : 1u;
+                const uint32_t g = L.graph[w], gl = w > 0 ? L.graph[w - 1] : 0u;
+                const uint32_t nd = L.node[w], ndl = w > 0 ? L.node[w - 1] : 0u;
+                const uint32_t wa = L.a[w], wb = L.b[w];
+                if (f0)
                     continue;
-                const uint32_t g = L.graph[w];
-                if (level >= A.gd[g].height)
+                const GraphDesc &Dg = A.gd[g];
+                if (level >= Dg.height)
                     continue;  // root window: to the remaining buffer
-                const uint32_t W = A.gd[g].seg << level;
-                ci += L.b[w] - L.a[w];
-                const uint32_t par = L.node[w] & ~W;
-                const bool merged =
-                    w > 0 && !A.wflag[w - 1] && L.graph[w - 1] == g && (L.node[w - 1] & ~W) == par;
+                const uint32_t W = Dg.seg << level;
+                ci += wb - wa;
+                const uint32_t par = nd & ~W;
+                const bool merged = w > 0 && !fl && gl == g && (ndl & ~W) == par;
                 ch += merged ? 0u : 1u;
             }
             uint32_t th = block_sum(ch, tmp);
@@ -1025,37 +1029,46 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         }
         for (uint32_t w0 = lo; w0 < hi; w0 += BLOCK) {
             const uint32_t w = w0 + threadIdx.x;
-            const bool rej = w < hi && !A.wflag[w];
-            const uint32_t g = rej ? L.graph[w] : 0u;
-            const bool root = rej && level >= A.gd[g].height;
+            // every field this window and its neighbours may need, in one round
+            const bool in = w < hi;
+            const bool has_l = in && w > 0, has_r = in && w + 1 < nw;
+            const uint32_t f0 = in ? A.wflag[w] : 1u, fl = has_l ? A.wflag[w - 1] : 1u,
+                           fr = has_r ? A.wflag[w + 1] : 1u;
+            const uint32_t g = in ? L.graph[w] : 0u, gl = has_l ? L.graph[w - 1] : 0u,
+                           gr = has_r ? L.graph[w + 1] : 0u;
+            const uint32_t nd = in ? L.node[w] : 0u, ndl = has_l ? L.node[w - 1] : 0u,
+                           ndr = has_r ? L.node[w + 1] : 0u;
+            const uint32_t wa = in ? L.a[w] : 0u, wb = in ? L.b[w] : 0u;
+            const uint32_t wra = has_r ? L.a[w + 1] : 0u, wrb = has_r ? L.b[w + 1] : 0u;
+            const bool rej = in && !f0;
+            const GraphDesc &Dg = A.gd[g];
+            const bool root = rej && level >= Dg.height;
             const bool carry = rej && !root;
-            const uint32_t c = rej ? L.b[w] - L.a[w] : 0u;
+            const uint32_t c = rej ? wb - wa : 0u;
             uint32_t tot_i;
             const uint32_t nb = base_i + block_excl_scan(carry ? c : 0u, &tot_i, tmp);
             uint32_t head = 0, par = 0, W = 0;
             if (carry) {
-                W = A.gd[g].seg << level;
-                par = L.node[w] & ~W;
-                const bool merged =
-                    w > 0 && !A.wflag[w - 1] && L.graph[w - 1] == g && (L.node[w - 1] & ~W) == par;
+                W = Dg.seg << level;
+                par = nd & ~W;
+                const bool merged = has_l && !fl && gl == g && (ndl & ~W) == par;
                 head = merged ? 0u : 1u;
             }
             uint32_t tot_h;
             const uint32_t ex = block_excl_scan(head, &tot_h, tmp);
             if (head) {
                 const uint32_t e = base + ex;
-                const bool right =
-                    w + 1 < nw && !A.wflag[w + 1] && L.graph[w + 1] == g && (L.node[w + 1] & ~W) == par;
+                const bool right = has_r && !fr && gr == g && (ndr & ~W) == par;
                 nwn[e] = par;
                 nwg[e] = g;
                 nwa[e] = nb;
-                nwb[e] = nb + c + (right ? L.b[w + 1] - L.a[w + 1] : 0u);
+                nwb[e] = nb + c + (right ? wrb - wra : 0u);
             }
             if (root)
                 A.gs[g].remaining = c;
             // copy plan: carried windows to the next buffer, root windows to
             // the remaining-insertion buffer at the graph's first insertion
-            s_src[threadIdx.x] = rej ? L.a[w] : 0u;
+            s_src[threadIdx.x] = rej ? wa : 0u;
             s_cnt[threadIdx.x] = rej ? c : 0u;
             s_nb[threadIdx.x] = carry ? nb : (root ? A.gs[g].ins_base : 0u);
             s_dst[threadIdx.x] = root ? 1u : 0u;
