@@ -765,8 +765,20 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             log2stride = 31 - __clz(D.size / cached);
             const uint32_t hstep = log2stride - D.log2seg;  // stride >= seg
             uint64_t *f = reinterpret_cast<uint64_t *>(smem);
-            for (uint32_t j = threadIdx.x; j < cached; j += BLOCK)
-                f[j] = D.heads[(size_t)j << hstep];
+            // all of a thread's loads issued together (a loop with a runtime
+            // bound would issue them one round trip after another)
+            uint64_t hv[LOCATE_CACHE / BLOCK];
+#pragma unroll
+            for (uint32_t r = 0; r < LOCATE_CACHE / BLOCK; ++r) {
+                const uint32_t j = threadIdx.x + r * BLOCK;
+                hv[r] = j < cached ? D.heads[(size_t)j << hstep] : 0ull;
+            }
+#pragma unroll
+            for (uint32_t r = 0; r < LOCATE_CACHE / BLOCK; ++r) {
+                const uint32_t j = threadIdx.x + r * BLOCK;
+                if (j < cached)
+                    f[j] = hv[r];
+            }
             __syncthreads();
             fk = f;
         }
