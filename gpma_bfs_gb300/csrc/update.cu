@@ -150,6 +150,8 @@ __device__ __forceinline__ uint32_t leaf_find(const GraphDesc &D, uint32_t leaf,
 // every key's probe is issued before any comparison, so a thread keeps
 // LOC_ILP dependent chains in flight instead of one.
 constexpr int LOC_ILP = 4;
+// Consecutive items per thread in the grouping passes.
+constexpr uint32_t GROUP_ITEMS = 4;
 
 // Keys i0 + j * stride (j < LOC_ILP) below `end`; returns how many of them
 // are insertions (leaf set).
@@ -838,16 +840,27 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
     uint32_t base, m;
     cta_prefix(CNT(scan_id), base, m, tmp);
     const uint32_t out_lo = base;
-    for (uint32_t i0 = lo; i0 < hi; i0 += BLOCK) {
-        uint32_t i = i0 + threadIdx.x;
-        uint32_t f = (i < hi && A.leaf[i] != SIZE_NONE) ? 1u : 0u;
+    // GROUP_ITEMS consecutive items per thread and one scan per round
+    for (uint32_t r0 = lo; r0 < hi; r0 += GROUP_ITEMS * BLOCK) {
+        const uint32_t i0 = r0 + GROUP_ITEMS * threadIdx.x;
+        uint32_t lf[GROUP_ITEMS], cnt = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < GROUP_ITEMS; ++j) {
+            lf[j] = i0 + j < hi ? A.leaf[i0 + j] : SIZE_NONE;
+            cnt += lf[j] != SIZE_NONE;
+        }
         uint32_t tot;
-        uint32_t ex = block_excl_scan(f, &tot, tmp);
-        if (f) {
-            A.ikeys[0][base + ex] = bk[i];
-            A.ivals[0][base + ex] = bv[i];
-            A.ileaf[base + ex] = A.leaf[i];
-            A.igraph[base + ex] = graph_of(A, i);
+        uint32_t o = base + block_excl_scan(cnt, &tot, tmp);
+#pragma unroll
+        for (uint32_t j = 0; j < GROUP_ITEMS; ++j) {
+            if (lf[j] == SIZE_NONE)
+                continue;
+            const uint32_t i = i0 + j;
+            A.ikeys[0][o] = bk[i];
+            A.ivals[0][o] = bv[i];
+            A.ileaf[o] = lf[j];
+            A.igraph[o] = graph_of(A, i);
+            ++o;
         }
         base += tot;
     }
@@ -901,32 +914,51 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         nw = block_sum(all, tmp);
         base = block_sum(before, tmp);
     }
-    for (uint32_t j0 = out_lo; j0 < out_hi; j0 += BLOCK) {
-        uint32_t j = j0 + threadIdx.x;
-        bool in = j < out_hi;
-        uint32_t head = 0;
-        if (in) {
-            const uint32_t gj = A.igraph[j];
-            const bool new_graph = j == 0 || A.igraph[j - 1] != gj;
-            head = (new_graph || A.ileaf[j] != A.ileaf[j - 1]) ? 1u : 0u;
-            if (new_graph)
-                A.gs[gj].ins_base = j;
-            if (j + 1 == m || A.igraph[j + 1] != gj)
-                A.gs[gj].inserts = j + 1;  // end for now; made a count by the host
+    for (uint32_t r0 = out_lo; r0 < out_hi; r0 += GROUP_ITEMS * BLOCK) {
+        const uint32_t j0 = r0 + GROUP_ITEMS * threadIdx.x;
+        // items j0 - 1 .. j0 + GROUP_ITEMS: each item's run test needs its
+        // neighbours on both sides
+        uint32_t lf[GROUP_ITEMS + 2], gr[GROUP_ITEMS + 2];
+#pragma unroll
+        for (uint32_t q = 0; q < GROUP_ITEMS + 2; ++q) {
+            const uint32_t j = j0 + q - 1;  // wraps to UINT32_MAX for j0 == 0, q == 0
+            const bool ok = j0 + q >= 1 && j < m;
+            lf[q] = ok ? A.ileaf[j] : SIZE_NONE;
+            gr[q] = ok ? A.igraph[j] : SIZE_NONE;
+        }
+        uint32_t heads = 0;
+        uint32_t hd[GROUP_ITEMS];
+#pragma unroll
+        for (uint32_t q = 0; q < GROUP_ITEMS; ++q) {
+            const uint32_t j = j0 + q;
+            hd[q] = 0;
+            if (j < out_hi) {
+                const bool new_graph = j == 0 || gr[q] != gr[q + 1];
+                hd[q] = (new_graph || lf[q + 1] != lf[q]) ? 1u : 0u;
+                if (new_graph)
+                    A.gs[gr[q + 1]].ins_base = j;
+                if (j + 1 == m || gr[q + 2] != gr[q + 1])
+                    A.gs[gr[q + 1]].inserts = j + 1;  // end for now; made a count by the host
+            }
+            heads += hd[q];
         }
         uint32_t tot;
-        uint32_t ex = block_excl_scan(head, &tot, tmp);
-        if (in) {
-            // a run continued from the previous CTA's output extends window base - 1
-            uint32_t e = base + ex;
-            if (head) {
-                A.wnode[0][e] = A.ileaf[j];
-                A.wgraph[0][e] = A.igraph[j];
+        // a run continued from the previous CTA's output extends window base - 1
+        uint32_t e = base + block_excl_scan(heads, &tot, tmp);
+#pragma unroll
+        for (uint32_t q = 0; q < GROUP_ITEMS; ++q) {
+            const uint32_t j = j0 + q;
+            if (j >= out_hi)
+                continue;
+            if (hd[q]) {
+                A.wnode[0][e] = lf[q + 1];
+                A.wgraph[0][e] = gr[q + 1];
                 A.wa[0][e] = j;
+                ++e;
             }
-            const bool last = j + 1 == m || A.ileaf[j + 1] != A.ileaf[j] || A.igraph[j + 1] != A.igraph[j];
+            const bool last = j + 1 == m || lf[q + 2] != lf[q + 1] || gr[q + 2] != gr[q + 1];
             if (last)
-                A.wb[0][e + head - 1] = j + 1;
+                A.wb[0][e - 1] = j + 1;
         }
         base += tot;
     }
