@@ -972,7 +972,6 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
     // buffers selected by `cur`; each window's insertions are the contiguous
     // range [wa, wb) of the current insertion buffer.
     uint32_t cur = 0, level = 0;
-    __shared__ uint32_t s_nb[BLOCK], s_src[BLOCK], s_cnt[BLOCK], s_dst[BLOCK];
     for (; level <= A.max_height && nw > 0; ++level) {
         Windows L;
         L.node = cur ? A.wnode[1] : A.wnode[0];
@@ -1071,60 +1070,93 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             ++level;
             break;
         }
-        for (uint32_t w0 = lo; w0 < hi; w0 += BLOCK) {
-            const uint32_t w = w0 + threadIdx.x;
-            // every field this window and its neighbours may need, in one round
-            const bool in = w < hi;
-            const bool has_l = in && w > 0, has_r = in && w + 1 < nw;
-            const uint32_t f0 = in ? A.wflag[w] : 1u, fl = has_l ? A.wflag[w - 1] : 1u,
-                           fr = has_r ? A.wflag[w + 1] : 1u;
-            const uint32_t g = in ? L.graph[w] : 0u, gl = has_l ? L.graph[w - 1] : 0u,
-                           gr = has_r ? L.graph[w + 1] : 0u;
-            const uint32_t nd = in ? L.node[w] : 0u, ndl = has_l ? L.node[w - 1] : 0u,
-                           ndr = has_r ? L.node[w + 1] : 0u;
-            const uint32_t wa = in ? L.a[w] : 0u, wb = in ? L.b[w] : 0u;
-            const uint32_t wra = has_r ? L.a[w + 1] : 0u, wrb = has_r ? L.b[w + 1] : 0u;
-            const bool rej = in && !f0;
-            const GraphDesc &Dg = A.gd[g];
-            const bool root = rej && level >= Dg.height;
-            const bool carry = rej && !root;
-            const uint32_t c = rej ? wb - wa : 0u;
-            uint32_t tot_i;
-            const uint32_t nb = base_i + block_excl_scan(carry ? c : 0u, &tot_i, tmp);
-            uint32_t head = 0, par = 0, W = 0;
-            if (carry) {
-                W = Dg.seg << level;
-                par = nd & ~W;
-                const bool merged = has_l && !fl && gl == g && (ndl & ~W) == par;
-                head = merged ? 0u : 1u;
+        // GROUP_ITEMS consecutive windows per thread per round; the rejected
+        // windows' copy plan goes to a compact list in shared memory (free
+        // again once the level's windows are written), one warp per entry
+        uint32_t *l_src = reinterpret_cast<uint32_t *>(smem);
+        uint32_t *l_cnt = l_src + GROUP_ITEMS * BLOCK;
+        uint32_t *l_to = l_cnt + GROUP_ITEMS * BLOCK;
+        uint32_t *l_dst = l_to + GROUP_ITEMS * BLOCK;
+        for (uint32_t r0 = lo; r0 < hi; r0 += GROUP_ITEMS * BLOCK) {
+            const uint32_t w0 = r0 + GROUP_ITEMS * threadIdx.x;
+            // windows w0 - 1 .. w0 + GROUP_ITEMS: each needs both neighbours
+            uint32_t fl[GROUP_ITEMS + 2], gg[GROUP_ITEMS + 2], nd[GROUP_ITEMS + 2], wa[GROUP_ITEMS + 2],
+                wb[GROUP_ITEMS + 2];
+#pragma unroll
+            for (uint32_t q = 0; q < GROUP_ITEMS + 2; ++q) {
+                const uint32_t j = w0 + q - 1;
+                const bool ok = w0 + q >= 1 && j < nw;
+                fl[q] = ok ? A.wflag[j] : 1u;
+                gg[q] = ok ? L.graph[j] : 0u;
+                nd[q] = ok ? L.node[j] : 0u;
+                wa[q] = ok ? L.a[j] : 0u;
+                wb[q] = ok ? L.b[j] : 0u;
             }
-            uint32_t tot_h;
-            const uint32_t ex = block_excl_scan(head, &tot_h, tmp);
-            if (head) {
-                const uint32_t e = base + ex;
-                const bool right = has_r && !fr && gr == g && (ndr & ~W) == par;
-                nwn[e] = par;
-                nwg[e] = g;
-                nwa[e] = nb;
-                nwb[e] = nb + c + (right ? wrb - wra : 0u);
+            uint32_t csum = 0, hsum = 0, rsum = 0;
+#pragma unroll
+            for (uint32_t q = 0; q < GROUP_ITEMS; ++q) {
+                const uint32_t j = w0 + q;
+                const bool rej = j < hi && !fl[q + 1];
+                if (!rej)
+                    continue;
+                const GraphDesc &Dg = A.gd[gg[q + 1]];
+                ++rsum;
+                if (level >= Dg.height)
+                    continue;  // root window
+                csum += wb[q + 1] - wa[q + 1];
+                const uint32_t W = Dg.seg << level;
+                const bool merged = j > 0 && !fl[q] && gg[q] == gg[q + 1] && (nd[q] & ~W) == (nd[q + 1] & ~W);
+                hsum += merged ? 0u : 1u;
             }
-            if (root)
-                A.gs[g].remaining = c;
-            // copy plan: carried windows to the next buffer, root windows to
-            // the remaining-insertion buffer at the graph's first insertion
-            s_src[threadIdx.x] = rej ? wa : 0u;
-            s_cnt[threadIdx.x] = rej ? c : 0u;
-            s_nb[threadIdx.x] = carry ? nb : (root ? A.gs[g].ins_base : 0u);
-            s_dst[threadIdx.x] = root ? 1u : 0u;
+            uint32_t tot_i, tot_h, tot_r;
+            uint32_t nb = base_i + block_excl_scan(csum, &tot_i, tmp);
+            uint32_t e = base + block_excl_scan(hsum, &tot_h, tmp);
+            uint32_t li = block_excl_scan(rsum, &tot_r, tmp);
+#pragma unroll
+            for (uint32_t q = 0; q < GROUP_ITEMS; ++q) {
+                const uint32_t j = w0 + q;
+                const bool rej = j < hi && !fl[q + 1];
+                if (!rej)
+                    continue;
+                const uint32_t g = gg[q + 1];
+                const GraphDesc &Dg = A.gd[g];
+                const uint32_t c = wb[q + 1] - wa[q + 1];
+                const bool root = level >= Dg.height;
+                l_src[li] = wa[q + 1];
+                l_cnt[li] = c;
+                l_dst[li] = root ? 1u : 0u;
+                if (root) {
+                    // the root rebalance takes these: the graph's area of the
+                    // remaining-insertion buffer, at its first insertion
+                    A.gs[g].remaining = c;
+                    l_to[li] = A.gs[g].ins_base;
+                    ++li;
+                    continue;
+                }
+                l_to[li] = nb;
+                ++li;
+                const uint32_t W = Dg.seg << level;
+                const uint32_t par = nd[q + 1] & ~W;
+                const bool merged = j > 0 && !fl[q] && gg[q] == g && (nd[q] & ~W) == par;
+                if (!merged) {
+                    const bool right = j + 1 < nw && !fl[q + 2] && gg[q + 2] == g && (nd[q + 2] & ~W) == par;
+                    nwn[e] = par;
+                    nwg[e] = g;
+                    nwa[e] = nb;
+                    nwb[e] = nb + c + (right ? wb[q + 2] - wa[q + 2] : 0u);
+                    ++e;
+                }
+                nb += c;
+            }
             __syncthreads();
-            // copy the kept insertions, one warp per window of this tile
-            for (uint32_t t = threadIdx.x >> 5; t < BLOCK; t += BLOCK / 32) {
-                const uint32_t cc = s_cnt[t], from = s_src[t], to = s_nb[t];
-                uint64_t *dk = s_dst[t] ? A.rkeys : nk;
-                uint8_t *dv = s_dst[t] ? A.rvals : nv;
-                for (uint32_t e = threadIdx.x & 31; e < cc; e += 32) {
-                    dk[to + e] = pk[from + e];
-                    dv[to + e] = pv[from + e];
+            // copy the kept insertions, one warp per rejected window
+            for (uint32_t t = threadIdx.x >> 5; t < tot_r; t += BLOCK / 32) {
+                const uint32_t cc = l_cnt[t], from = l_src[t], to = l_to[t];
+                uint64_t *dk = l_dst[t] ? A.rkeys : nk;
+                uint8_t *dv = l_dst[t] ? A.rvals : nv;
+                for (uint32_t x = threadIdx.x & 31; x < cc; x += 32) {
+                    dk[to + x] = pk[from + x];
+                    dv[to + x] = pv[from + x];
                 }
             }
             __syncthreads();
