@@ -399,11 +399,21 @@ __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
     uint8_t *cv = pend_v + W;
     uint8_t *mv = cv + W;
     const uint32_t total_warps = gridDim.x * (BLOCK / 32);
-    for (uint32_t wbase = r0 + (blockIdx.x * (BLOCK / 32) + warp) * GPW; wbase < r1; wbase += total_warps * GPW) {
+    const uint32_t g_r0 = L.graph[r0];  // stands in for groups without a window
+    // the next round's window descriptor is read while this round works
+    uint32_t wbase = r0 + (blockIdx.x * (BLOCK / 32) + warp) * GPW;
+    uint32_t n_g = g_r0, n_node = 0, n_a = 0, n_b = 0;
+    if (wbase + grp < r1) {
+        n_g = L.graph[wbase + grp];
+        n_node = L.node[wbase + grp];
+        n_a = L.a[wbase + grp];
+        n_b = L.b[wbase + grp];
+    }
+    for (; wbase < r1; wbase += total_warps * GPW) {
         const uint32_t w = wbase + grp;
         const bool has = w < r1;
-        const GraphDesc &D = A.gd[has ? L.graph[w] : L.graph[r0]];
-        const uint32_t node = has ? L.node[w] : 0, a = has ? L.a[w] : 0, b = has ? L.b[w] : 0;
+        const GraphDesc &D = A.gd[n_g];
+        const uint32_t node = n_node, a = n_a, b = n_b;
         const uint32_t log2seg = D.log2seg, seg_mask = D.seg - 1;
         const uint32_t log2F = (31 - __clz(W)) - log2seg;
         const uint32_t lo = D.lower[level], hi = D.upper[level];
@@ -411,8 +421,28 @@ __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
         uint64_t k[K];
         uint8_t v[K];
         uint32_t c_l = 0;
+        // the window's first pending insertions, loaded beside its slots
+        uint64_t pk0 = 0;
+        uint8_t pv0 = 0;
         if (has) {
             load_slots<K>(D.keys, D.vals, t0, k, v);
+            if (gl < b - a) {
+                pk0 = pk[a + gl];
+                pv0 = pv[a + gl];
+            }
+        }
+        {
+            const uint32_t wn = w + total_warps * GPW;
+            n_g = g_r0;
+            n_node = n_a = n_b = 0;
+            if (wn < r1) {
+                n_g = L.graph[wn];
+                n_node = L.node[wn];
+                n_a = L.a[wn];
+                n_b = L.b[wn];
+            }
+        }
+        if (has) {
 #pragma unroll
             for (uint32_t j = 0; j < K; ++j)
                 c_l += (k[j] != KEY_NONE && v[j] != 0);
@@ -432,7 +462,11 @@ __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
                     ++o;
                 }
             }
-            for (uint32_t j = gl; j < p; j += G) {
+            if (gl < p) {
+                pend_k[gl] = pk0;
+                pend_v[gl] = pv0;
+            }
+            for (uint32_t j = gl + G; j < p; j += G) {
                 pend_k[j] = pk[a + j];
                 pend_v[j] = pv[a + j];
             }
