@@ -51,6 +51,20 @@ def test_null_arguments_rejected_without_gpu(built_lib):
     assert b"null" in built_lib.gpma_last_error() or b"NULL" in built_lib.gpma_last_error()
     with pytest.raises(ValueError):
         G.update_gpma(object(), np.zeros(3, np.uint64), np.zeros(2, np.uint8))
+    # recorded steps, the consistency check and the shard helpers validate
+    # their arguments before any CUDA call
+    L = G.lib()
+    out = ctypes.c_void_p()
+    assert L.gpma_step_create(None, ctypes.byref(out)) == 1
+    assert L.gpma_step_run(None, None, None, 0, 0, None, None, None) == 1
+    assert L.gpma_step_get_stats(None, None) == 1
+    assert L.gpma_step_destroy(None) == 0
+    assert L.gpma_batch_step_create(None, None, 0, ctypes.byref(out)) == 1
+    assert L.gpma_batch_step_run(None, None, None, None, None, None, None, None) == 1
+    assert L.gpma_batch_step_destroy(None) == 0
+    assert L.gpma_validate(None, None, None) == 1
+    assert L.gpma_partition_rows(None, None, 0, 10, 0, 1, None, None, None) == 1
+    assert L.gpma_shard_first_row(10, 3, 1) == 3 and L.gpma_shard_first_row(10, 0, 1) == 0
 
 
 def test_rmat_generator_deterministic(built_lib):
