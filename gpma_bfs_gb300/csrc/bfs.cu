@@ -280,7 +280,7 @@ constexpr uint32_t DENSE_GATE = 64;
 // Long-row chunks one CTA keeps in shared memory on a small level.
 constexpr uint32_t LOCAL_CHUNKS = 1024;
 
-__global__ void __launch_bounds__(BLOCK) bfs_kernel(BfsArgs A) {
+__global__ void __launch_bounds__(BLOCK, 5) bfs_kernel(BfsArgs A) {
     __shared__ uint2 s_chunks[LOCAL_CHUNKS];
     __shared__ uint32_t s_nch;
     GridBarrier *bar = reinterpret_cast<GridBarrier *>(A.ctl + CTL_BAR);
