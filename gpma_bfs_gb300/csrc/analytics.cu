@@ -285,10 +285,8 @@ gpma_status launch(const void *kernel, AnArgs &A, int sms, cudaStream_t s, uint3
     GPMA_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(sms * an_fit[dev]), dim3(BLOCK), params, 0, s));
     GPMA_CUDA(cudaMemcpyAsync(h_ctl, A.ctl, sizeof(uint32_t) * AN_WORDS, cudaMemcpyDeviceToHost, s));
     GPMA_CUDA(cudaStreamSynchronize(s));
-    if (h_ctl[AN_ERR]) {
-        set_error("device-side wait gave up in an analytics kernel (code %u)", h_ctl[AN_ERR]);
-        return GPMA_ERR_TIMEOUT;
-    }
+    if (h_ctl[AN_ERR])
+        return device_error("an analytics kernel", h_ctl[AN_ERR]);
     return GPMA_OK;
 }
 

@@ -214,8 +214,11 @@ __device__ __forceinline__ uint32_t frontier_pass(const BfsArgs &A, uint32_t *fr
         uint32_t b = 0, e = 0, len = 0;
         if (f & (1u << lane)) {
             const uint32_t u = (wi << 5) + lane;
+            const uint32_t r1 = A.ro[u + 1];
             b = A.ro[u];
-            e = min(A.ro[u + 1], A.size);
+            e = min(r1, A.size);
+            if (!in_bounds(A.ctl + CTL_ERR, b <= r1 && r1 <= A.size, BS_ROW))
+                b = e;  // an inconsistent row_offset: the row is skipped
             len = e > b ? e - b : 0;
         }
         slots += len;
@@ -514,10 +517,8 @@ gpma_status bfs_plan(gpma_graph *g, uint32_t src, BfsPlan *P) {
 }
 
 gpma_status bfs_finish(gpma_graph *g, uint64_t *reached) {
-    if (g->h_bfs_ctl[CTL_ERR]) {
-        set_error("device-side wait gave up in the BFS kernel (code %u)", g->h_bfs_ctl[CTL_ERR]);
-        return GPMA_ERR_TIMEOUT;
-    }
+    if (g->h_bfs_ctl[CTL_ERR])
+        return device_error("the BFS kernel", g->h_bfs_ctl[CTL_ERR]);
     if (reached)
         *reached = g->h_bfs_ctl[CTL_REACHED];
     return GPMA_OK;
@@ -640,10 +641,8 @@ gpma_status bfs_noalloc_run(gpma_graph *g, uint32_t src, uint32_t *levels, uint6
     uint32_t h_ctl[CTL_WORDS];
     GPMA_CUDA(cudaMemcpyAsync(h_ctl, ctl, sizeof(h_ctl), cudaMemcpyDeviceToHost, s));
     GPMA_CUDA(cudaStreamSynchronize(s));
-    if (h_ctl[CTL_ERR]) {
-        set_error("device-side wait gave up in the BFS kernel (code %u)", h_ctl[CTL_ERR]);
-        return GPMA_ERR_TIMEOUT;
-    }
+    if (h_ctl[CTL_ERR])
+        return device_error("the BFS kernel", h_ctl[CTL_ERR]);
     if (reached)
         *reached = h_ctl[CTL_REACHED];
     return GPMA_OK;

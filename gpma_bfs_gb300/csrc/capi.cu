@@ -19,6 +19,15 @@ void set_error(const char *fmt, ...) {
     va_end(ap);
 }
 
+gpma_status device_error(const char *where, uint32_t code) {
+    if ((code & 0xFFu) == DERR_BOUNDS) {
+        set_error("out-of-range index in %s (bounds-checked build, site %u)", where, code >> 8);
+        return GPMA_ERR_DEVICE;
+    }
+    set_error("device-side wait gave up in %s (code %u)", where, code);
+    return GPMA_ERR_TIMEOUT;
+}
+
 gpma_status cuda_fail(cudaError_t e, const char *what) {
     set_error("%s: %s", what, cudaGetErrorString(e));
     cudaGetLastError();

@@ -49,6 +49,24 @@ enum : uint32_t {
     DERR_INVALID_KEY = 4,
 };
 
+// Bounds-checked build (-DGPMA_BOUNDS_CHECK=1): every data-dependent index
+// range (a located leaf, a window, a pending-insertion range, a BFS row) is
+// checked against its buffer before the access. A failing check skips the
+// access and records DERR_BOUNDS | site << 8 in the launch's error word, and
+// the launch stops at its next grid barrier. The product build compiles the
+// checks away.
+#ifndef GPMA_BOUNDS_CHECK
+#define GPMA_BOUNDS_CHECK 0
+#endif
+enum BoundsSite : uint32_t {
+    BS_LEAF = 1,      // locate: the leaf's seg slots
+    BS_WINDOW = 2,    // level loop: a warp/CTA window's slots
+    BS_PENDING = 3,   // level loop: a window's pending insertions
+    BS_CHUNK = 4,     // level loop: a grid-wide window's chunk
+    BS_REBUILD = 5,   // bulk rebuild / compacted layout: a slot
+    BS_ROW = 6,       // BFS / multi-source BFS / analytics: a row's slot range
+};
+
 // Bounded waits give up after this long (ns of %globaltimer).
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;
 
@@ -227,6 +245,8 @@ namespace gpma {
 
 // ---- host error handling -------------------------------------------------
 void set_error(const char *fmt, ...);
+// Status and message for a kernel's non-zero error word (`where` names the kernel).
+gpma_status device_error(const char *where, uint32_t code);
 gpma_status cuda_fail(cudaError_t e, const char *what);
 #define GPMA_CUDA(expr)                                                                                                \
     do {                                                                                                               \
@@ -459,6 +479,18 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 }
 
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) { return *(const volatile uint32_t *)p; }
+
+// True when `ok`; in the bounds-checked build a false `ok` records the site
+// in *err (first error wins) and the caller skips the access.
+__device__ __forceinline__ bool in_bounds(uint32_t *err, bool ok, uint32_t site) {
+    if constexpr (GPMA_BOUNDS_CHECK != 0) {
+        if (!ok) {
+            atomicCAS(err, 0u, DERR_BOUNDS | (site << 8));
+            return false;
+        }
+    }
+    return true;
+}
 
 // Ticket barrier across the CTAs of a cooperative launch. Each CTA takes a
 // ticket from one counter (it must start each launch at zero) and waits

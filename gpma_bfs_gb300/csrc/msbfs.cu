@@ -201,8 +201,11 @@ __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
                 g = graph_of_node(A, u);
                 const MsGraph &Gr = A.gr[g];
                 const uint32_t lu = u - A.voff[g];
+                const uint32_t r1 = Gr.ro[lu + 1];
                 b = Gr.ro[lu];
-                e = min(Gr.ro[lu + 1], Gr.size);
+                e = min(r1, Gr.size);
+                if (!in_bounds(err, b <= r1 && r1 <= Gr.size, BS_ROW))
+                    b = e;  // an inconsistent row_offset: the row is skipped
                 len = e > b ? e - b : 0;
             }
             const uint32_t nch = len > MS_BIG_ROW ? (len + MS_CHUNK_SLOTS - 1) / MS_CHUNK_SLOTS : 0;
@@ -506,10 +509,8 @@ gpma_status batch_bfs_enqueue_readback(gpma_batch *b, const BatchBfsPlan &P, cud
 gpma_status batch_bfs_finish(gpma_batch *b, const uint32_t *nsrc, uint32_t k, uint64_t *reached) {
     b->prof.kernel_launches += 1;
     b->prof.bfs_kernels++;
-    if (b->h_ms_ctl[MS_ERR]) {
-        set_error("device-side wait gave up in the multi-source BFS kernel (code %u)", b->h_ms_ctl[MS_ERR]);
-        return GPMA_ERR_TIMEOUT;
-    }
+    if (b->h_ms_ctl[MS_ERR])
+        return device_error("the multi-source BFS kernel", b->h_ms_ctl[MS_ERR]);
     const unsigned long long *r = b->h_ms_reached;
     if (reached) {
         uint64_t o = 0;

@@ -214,6 +214,10 @@ __device__ __forceinline__ uint32_t locate_keys(const UpdateArgs &A, const uint6
         const GraphDesc &D = A.gd[g[j]];
         const uint8_t value = bv[idx[j]];
         uint32_t leaf = value == 0 ? SIZE_NONE : prefix[j];
+        if (!in_bounds(&A.st->err, (uint64_t)prefix[j] + D.seg <= D.size, BS_LEAF)) {
+            A.leaf[idx[j]] = SIZE_NONE;
+            continue;
+        }
         const uint32_t hit = leaf_find(D, prefix[j], key[j]);
         if (hit != SIZE_NONE) {
             D.vals[prefix[j] + hit] = value;  // delete / modify / revive in place
@@ -411,9 +415,10 @@ __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
     }
     for (; wbase < r1; wbase += total_warps * GPW) {
         const uint32_t w = wbase + grp;
-        const bool has = w < r1;
         const GraphDesc &D = A.gd[n_g];
         const uint32_t node = n_node, a = n_a, b = n_b;
+        const bool has =
+            w < r1 && in_bounds(&A.st->err, (uint64_t)node + W <= D.size && a <= b && b <= A.n, BS_WINDOW);
         const uint32_t log2seg = D.log2seg, seg_mask = D.seg - 1;
         const uint32_t log2F = (31 - __clz(W)) - log2seg;
         const uint32_t lo = D.lower[level], hi = D.upper[level];
@@ -531,6 +536,9 @@ __device__ void cta_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32_
     for (uint32_t w = r0 + blockIdx.x; w < r1; w += gridDim.x) {
         const GraphDesc &D = A.gd[L.graph[w]];
         const uint32_t node = L.node[w], a = L.a[w], b = L.b[w];
+        // the same condition in every thread: the whole CTA skips the window
+        if (!in_bounds(&A.st->err, (uint64_t)node + W <= D.size && a <= b && b <= A.n, BS_WINDOW))
+            continue;
         const uint32_t log2seg = D.log2seg, seg_mask = D.seg - 1;
         const uint32_t log2F = (31 - __clz(W)) - log2seg;
         const uint32_t lo = D.lower[level], hi = D.upper[level];
@@ -627,6 +635,10 @@ __device__ bool grid_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
     for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
         const uint32_t w = r0 + c / cpw, k = c % cpw;
         const GraphDesc &D = A.gd[L.graph[w]];
+        // a failed check stops the launch at the barrier after this pass,
+        // before B3/B4 touch the window
+        if (!in_bounds(&A.st->err, (uint64_t)L.node[w] + W <= D.size, BS_CHUNK))
+            continue;
         const uint32_t base = L.node[w] + k * CHUNK + threadIdx.x * K;
         uint32_t cl = 0;
 #pragma unroll
@@ -654,6 +666,8 @@ __device__ bool grid_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
         }
         uint32_t M = run + (L.b[w] - L.a[w]);
         bool accept = D.lower[level] <= M && M <= D.upper[level];
+        if (!in_bounds(&A.st->err, L.a[w] <= L.b[w] && L.b[w] <= A.n, BS_PENDING))
+            accept = false;
         if (threadIdx.x == 0) {
             A.wflag[w] = accept ? 1u : 0u;
             A.wlive[w] = run;
@@ -1347,7 +1361,7 @@ __global__ void __launch_bounds__(BLOCK) rebuild_kernel(uint64_t *keys, uint8_t 
                                                         uint32_t log2seg,
                                                         uint32_t log2F, const uint64_t *lk, const uint8_t *lv,
                                                         uint32_t L, const uint64_t *pk, const uint8_t *pv, uint32_t P,
-                                                        const uint32_t *split, uint64_t gap_key) {
+                                                        const uint32_t *split, uint64_t gap_key, uint32_t *err) {
     extern __shared__ __align__(16) unsigned char smem[];
     uint64_t *sk = reinterpret_cast<uint64_t *>(smem);  // staged: live part, then pending part
     uint64_t *mk = sk + CHUNK;                          // merged
@@ -1362,6 +1376,12 @@ __global__ void __launch_bounds__(BLOCK) rebuild_kernel(uint64_t *keys, uint8_t 
         const uint64_t f_lo = seg_first(t0 >> log2seg, M, log2F), f_hi = seg_first((t0 + len) >> log2seg, M, log2F);
         const uint32_t i_lo = (uint32_t)(f_lo < M ? f_lo : M), i_hi = (uint32_t)(f_hi < M ? f_hi : M);
         const uint32_t x0 = split[c], x1 = split[c + 1];
+        // the same condition in every thread: the whole CTA skips the chunk
+        if (!in_bounds(err,
+                       x0 <= x1 && x1 <= L && x0 <= i_lo && x1 <= i_hi && i_lo - x0 <= i_hi - x1 &&
+                           i_hi - x1 <= P && i_hi - i_lo <= CHUNK,
+                       BS_REBUILD))
+            continue;
         const uint32_t y0 = i_lo - x0, y1 = i_hi - x1;
         const uint32_t nl = x1 - x0, np = y1 - y0;  // nl + np = i_hi - i_lo <= len
         for (uint32_t k = threadIdx.x; k < nl; k += BLOCK) {
@@ -1528,6 +1548,10 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k
         GPMA_TRY(dev_alloc(&g->chunk_cnt, (uint64_t)out_chunks + 2));
     }
     uint32_t *split = g->chunk_cnt;
+    // the bounds-checked build's error word of the rebuild (after the splits)
+    uint32_t *rebuild_err = GPMA_BOUNDS_CHECK ? g->chunk_cnt + out_chunks + 1 : nullptr;
+    if (rebuild_err)
+        GPMA_CUDA(cudaMemsetAsync(rebuild_err, 0, sizeof(uint32_t), s));
     auto splits = [&]() {
         merge_split_kernel<<<grid_for((uint64_t)out_chunks + 1, g->sms, 8), BLOCK, 0, s>>>(
             g->skeys, live, pend_k, pend_n, geo.size, log2seg, log2F, split);
@@ -1538,7 +1562,7 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k
         splits();
         rebuild_kernel<<<rgrid, BLOCK, rsmem, s>>>(g->keys, g->values, g->heads, g->row_offset, g->row_num, geo.size,
                                                     log2seg, log2F, g->skeys, g->svals, live, pend_k, pend_v, pend_n,
-                                                    split, 0ull);
+                                                    split, 0ull, rebuild_err);
         g->stats.significant++;
         g->stats.accepted_windows++;
         g->stats.accepted_slots += geo.size;
@@ -1548,7 +1572,7 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k
             splits();
             rebuild_kernel<<<rgrid, BLOCK, rsmem, s>>>(g->keys, g->values, g->heads, g->row_offset, g->row_num,
                                                         geo.size, log2seg, log2F, g->skeys, g->svals, live, pend_k,
-                                                        pend_v, pend_n, split, KEY_NONE);
+                                                        pend_v, pend_n, split, KEY_NONE, rebuild_err);
             g->stats.accepted_windows++;
             g->stats.accepted_slots += geo.size;
         } else {
@@ -1564,6 +1588,12 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k
     prof_mark(g, 1, s);
     GPMA_CUDA(cudaStreamSynchronize(s));
     g->prof.rebuild_ms += prof_elapsed(g, 0, 1);
+    if (rebuild_err) {
+        uint32_t e = 0;
+        GPMA_CUDA(cudaMemcpy(&e, rebuild_err, sizeof(e), cudaMemcpyDeviceToHost));
+        if (e)
+            return device_error("the bulk rebuild", e);
+    }
     // the scratch must cover the whole array for later wide windows
     GPMA_TRY(ensure_scratch(g, geo.size));
     return GPMA_OK;
@@ -1933,10 +1963,8 @@ gpma_status update_finish(gpma_graph *const *graphs, uint32_t k, BatchBuffers &b
         set_error("update batch holds keys whose column is 0xFFFFFFFF (reserved for row guards and empty slots)");
         return GPMA_ERR_INVALID;
     }
-    if (h.err) {
-        set_error("device-side wait gave up in the update kernel (code %u)", h.err);
-        return h.err == DERR_BOUNDS ? GPMA_ERR_DEVICE : GPMA_ERR_TIMEOUT;
-    }
+    if (h.err)
+        return device_error("the update kernel", h.err);
     for (uint32_t i = 0; i < k; ++i) {
         gpma_graph *g = graphs[i];
         const GraphStatus &gs = h_gs[i];

@@ -25,14 +25,29 @@ def test_header_declares_entry_points():
         assert core in names
 
 
+def _exported(path):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(path)], capture_output=True, text=True, check=True).stdout
+    return {line.split()[-1] for line in out.splitlines() if " T " in line}
+
+
 def test_library_exports_every_declared_symbol(built_lib):
-    out = subprocess.run(["nm", "-D", "--defined-only", str(ROOT / "gpma_bfs_gb300" / "libgpma_gb300.so")],
-                         capture_output=True, text=True, check=True).stdout
-    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    exported = _exported(ROOT / "gpma_bfs_gb300" / "libgpma_gb300.so")
     missing = [n for n in declared_symbols() if n not in exported]
     assert not missing, f"declared but not exported: {missing}"
     for n in declared_symbols():
         assert getattr(built_lib, n) is not None
+
+
+def test_checked_build_exports_the_same_entry_points(built_lib):
+    """The bounds-checked variant is a drop-in for the product library."""
+    from gpma_bfs_gb300.build import build
+
+    checked = build(checked=True)
+    assert checked.name == "libgpma_gb300_checked.so"
+    assert _exported(checked) == _exported(ROOT / "gpma_bfs_gb300" / "libgpma_gb300.so")
+    assert "GPMA_BOUNDS_CHECK=1" in (checked.parent / "_build_checked" / "options.txt").read_text()
+    assert "GPMA_BOUNDS_CHECK=0" in (checked.parent / "_build" / "options.txt").read_text()
+    ctypes.CDLL(str(checked))
 
 
 def test_status_strings(built_lib):
