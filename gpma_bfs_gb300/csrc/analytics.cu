@@ -312,6 +312,7 @@ extern "C" {
 
 gpma_status gpma_pagerank(gpma_graph *g, float damping, uint32_t iterations, double tol, float *ranks,
                           uint32_t *iterations_run, void *stream) {
+    CallRange range("gpma_pagerank");
     if (!g || !ranks || !(damping >= 0.0f && damping <= 1.0f) || g->row_num == 0) {
         set_error("gpma_pagerank: bad arguments (damping in [0, 1], a graph with nodes, an output array)");
         return GPMA_ERR_INVALID;
@@ -359,6 +360,7 @@ gpma_status gpma_pagerank(gpma_graph *g, float damping, uint32_t iterations, dou
 }
 
 gpma_status gpma_components(gpma_graph *g, uint32_t *labels, uint64_t *components, uint32_t *rounds, void *stream) {
+    CallRange range("gpma_components");
     if (!g || !labels) {
         set_error("gpma_components: null argument");
         return GPMA_ERR_INVALID;

@@ -308,6 +308,7 @@ const char *gpma_status_string(gpma_status s) {
 }
 
 gpma_status gpma_create(uint32_t row_num, void *stream, gpma_graph **out) {
+    CallRange range("gpma_create");
     if (!out) {
         set_error("gpma_create: out is NULL");
         return GPMA_ERR_INVALID;
@@ -368,6 +369,7 @@ gpma_status gpma_destroy(gpma_graph *g) {
 }
 
 gpma_status gpma_update(gpma_graph *g, const uint64_t *keys, const uint8_t *values, uint64_t n, void *stream) {
+    CallRange range("gpma_update");
     if (!g || (n && (!keys || !values))) {
         set_error("gpma_update: null argument");
         return GPMA_ERR_INVALID;
@@ -388,6 +390,7 @@ gpma_status gpma_update(gpma_graph *g, const uint64_t *keys, const uint8_t *valu
 }
 
 gpma_status gpma_bfs(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached, void *stream) {
+    CallRange range("gpma_bfs");
     if (!g || !levels) {
         set_error("gpma_bfs: null argument");
         return GPMA_ERR_INVALID;
@@ -404,6 +407,7 @@ gpma_status gpma_bfs(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *re
 }
 
 gpma_status gpma_validate(gpma_graph *g, uint64_t *bad, void *stream) {
+    CallRange range("gpma_validate");
     if (!g || !bad) {
         set_error("gpma_validate: null argument");
         return GPMA_ERR_INVALID;
@@ -429,6 +433,7 @@ gpma_status gpma_bfs_noalloc(gpma_graph *g, uint32_t src, uint32_t *levels, uint
 
 gpma_status gpma_bfs_multi(gpma_graph *g, const uint32_t *srcs, uint32_t k, uint32_t *levels, uint64_t *reached,
                            void *stream) {
+    CallRange range("gpma_bfs_multi");
     if (!g || !srcs || !levels || k == 0 || k > 64) {
         set_error("gpma_bfs_multi: bad arguments (k must be 1..64)");
         return GPMA_ERR_INVALID;
@@ -505,6 +510,7 @@ gpma_status gpma_batch_destroy(gpma_batch *b) {
 
 gpma_status gpma_batch_update(gpma_batch *b, gpma_graph *const *graphs, const uint64_t *const *keys,
                               const uint8_t *const *values, const uint64_t *counts, uint32_t k, void *stream) {
+    CallRange range("gpma_batch_update");
     if (!b || (k && (!graphs || !keys || !values || !counts))) {
         set_error("gpma_batch_update: null argument");
         return GPMA_ERR_INVALID;
@@ -568,6 +574,7 @@ gpma_status gpma_batch_update(gpma_batch *b, gpma_graph *const *graphs, const ui
 
 gpma_status gpma_batch_update_packed(gpma_batch *b, gpma_graph *const *graphs, const uint64_t *keys,
                                      const uint8_t *values, const uint64_t *offsets, uint32_t k, void *stream) {
+    CallRange range("gpma_batch_update_packed");
     if (!b || (k && (!graphs || !offsets || !keys || !values))) {
         set_error("gpma_batch_update_packed: null argument");
         return GPMA_ERR_INVALID;
@@ -614,6 +621,7 @@ gpma_status gpma_batch_update_packed(gpma_batch *b, gpma_graph *const *graphs, c
 gpma_status gpma_batch_bfs_multi(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs,
                                  const uint32_t *nsrc, uint32_t k, uint32_t *const *levels, uint64_t *reached,
                                  void *stream) {
+    CallRange range("gpma_batch_bfs_multi");
     if (!b || (k && (!graphs || !srcs || !nsrc))) {
         set_error("gpma_batch_bfs_multi: null argument");
         return GPMA_ERR_INVALID;
@@ -744,6 +752,7 @@ bool valid_geometry(uint32_t size, uint32_t seg, uint32_t height) {
 extern "C" {
 
 gpma_status gpma_save(gpma_graph *g, const char *path, void *stream) {
+    CallRange range("gpma_save");
     if (!g || !path) {
         set_error("gpma_save: null argument");
         return GPMA_ERR_INVALID;
@@ -785,6 +794,7 @@ gpma_status gpma_save(gpma_graph *g, const char *path, void *stream) {
 }
 
 gpma_status gpma_load(const char *path, void *stream, gpma_graph **out) {
+    CallRange range("gpma_load");
     if (!path || !out) {
         set_error("gpma_load: null argument");
         return GPMA_ERR_INVALID;
@@ -921,6 +931,7 @@ gpma_status gpma_get_thresholds(const gpma_graph *g, uint32_t *lower, uint32_t *
 
 gpma_status gpma_export_layout(gpma_graph *g, uint64_t *keys, uint8_t *masked_values, uint32_t *row_offset,
                                void *stream) {
+    CallRange range("gpma_export_layout");
     if (!g) {
         set_error("gpma_export_layout: null argument");
         return GPMA_ERR_INVALID;
@@ -945,6 +956,7 @@ gpma_status gpma_export_layout(gpma_graph *g, uint64_t *keys, uint8_t *masked_va
 }
 
 gpma_status gpma_export_compact(gpma_graph *g, uint64_t *keys, uint64_t capacity, uint64_t *count, void *stream) {
+    CallRange range("gpma_export_compact");
     if (!g || !count) {
         set_error("gpma_export_compact: null argument");
         return GPMA_ERR_INVALID;

@@ -12,6 +12,7 @@
 #include "../../include/gpma_gb300.h"
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <algorithm>
@@ -254,6 +255,16 @@ gpma_status cuda_fail(cudaError_t e, const char *what);
         if (_e != cudaSuccess)                                                                                         \
             return ::gpma::cuda_fail(_e, #expr);                                                                       \
     } while (0)
+// A named NVTX range over one C-ABI call, so timeline tools and `ncu --nvtx`
+// filters see each update, BFS and round; without an attached tool a range
+// costs one indirect call.
+struct CallRange {
+    explicit CallRange(const char *name) { nvtxRangePushA(name); }
+    ~CallRange() { nvtxRangePop(); }
+    CallRange(const CallRange &) = delete;
+    CallRange &operator=(const CallRange &) = delete;
+};
+
 #define GPMA_TRY(expr)                                                                                                 \
     do {                                                                                                               \
         gpma_status _s = (expr);                                                                                       \

@@ -308,6 +308,7 @@ gpma_status gpma_server_submit_bfs(gpma_server *s, uint32_t graph_id, const uint
 }
 
 gpma_status gpma_server_run_round(gpma_server *s, double now, gpma_round_info *info) {
+    CallRange range("gpma_server_run_round");
     if (!s) {
         set_error("gpma_server_run_round: null argument");
         return GPMA_ERR_INVALID;

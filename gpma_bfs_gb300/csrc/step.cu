@@ -520,6 +520,7 @@ gpma_status gpma_step_destroy(gpma_step *st) {
 
 gpma_status gpma_step_run(gpma_step *st, const uint64_t *keys, const uint8_t *values, uint64_t n, uint32_t src,
                           uint32_t *levels, uint64_t *reached, void *stream) {
+    gpma::CallRange range("gpma_step_run");
     if (!st || (n && (!keys || !values))) {
         gpma::set_error("gpma_step_run: null argument");
         return GPMA_ERR_INVALID;
@@ -595,6 +596,7 @@ gpma_status gpma_batch_step_destroy(gpma_batch_step *st) {
 gpma_status gpma_batch_step_run(gpma_batch_step *st, const uint64_t *keys, const uint8_t *values,
                                 const uint64_t *offsets, const uint32_t *const *srcs, const uint32_t *nsrc,
                                 uint64_t *reached, void *stream) {
+    gpma::CallRange range("gpma_batch_step_run");
     if (!st || !offsets || !srcs || !nsrc) {
         gpma::set_error("gpma_batch_step_run: null argument");
         return GPMA_ERR_INVALID;
