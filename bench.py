@@ -258,10 +258,10 @@ def run_gpu(args):
     accepted_slots = (st1["accepted_slots"] - st0["accepted_slots"]) / args.steps
 
     # roofline of the dominant kernel (the persistent update kernel):
-    # algorithmic bytes per launch = 9 B x batch (read the sorted batch)
+    # algorithmic bytes per launch = 18 B x batch (read the batch, write it sorted)
     #                              + 18 B x slots of redispatched windows (read + write)
     upd_ms = prof["update_kernel_ms"] / max(1, prof["update_kernels"])
-    upd_bytes = 9.0 * batch + 18.0 * accepted_slots
+    upd_bytes = 18.0 * batch + 18.0 * accepted_slots
     peak, peak_src = peak_hbm()
     achieved = upd_bytes / (upd_ms * 1e-3) / 1e9
     traffic = profiled_traffic("update_kernel")
