@@ -30,7 +30,8 @@ from oracle.workload import digest, read_output, write_script  # noqa: E402
 DRIVER = ROOT / "oracle" / "_ref" / "ref_driver"
 
 
-def encode(name, n, ops, records, store_ops, input_digest=None):
+def records_to_arrays(n, ops, records, store_ops, input_digest=None) -> dict:
+    """The per-operation results of one reference run, as the arrays a fixture holds."""
     kinds, lens, srcs = [], [], []
     uk, uv = [], []
     for op in ops:
@@ -80,7 +81,11 @@ def encode(name, n, ops, records, store_ops, input_digest=None):
         out["dump_ro"] = np.concatenate([r["row_offset"] for r in dmp])
     if input_digest is not None:
         out["input_digest"] = np.uint64(input_digest)
-    np.savez_compressed(HERE / f"{name}.npz", **out)
+    return out
+
+
+def encode(name, n, ops, records, store_ops, input_digest=None):
+    np.savez_compressed(HERE / f"{name}.npz", **records_to_arrays(n, ops, records, store_ops, input_digest))
 
 
 def run_reference(n, ops):
