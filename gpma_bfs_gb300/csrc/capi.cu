@@ -746,6 +746,37 @@ bool valid_geometry(uint32_t size, uint32_t seg, uint32_t height) {
     return seg == want_seg && height == fls32(size / seg) - 1;
 }
 
+// The structure the device code walks without further checks: row_offset
+// starts at 0 and never decreases, row r's guard (r << 32 | 0xFFFFFFFF) sits
+// at slot row_offset[r + 1] < size, and the live slots hold keys in
+// ascending order. A file whose checksum matches but whose layout breaks one
+// of these (written by another program, or edited) is refused before
+// anything reaches the GPU: the BFS would otherwise walk row ranges outside
+// the array.
+const char *snapshot_layout_error(uint32_t row_num, uint32_t size, const uint64_t *keys, const unsigned char *vals,
+                                  const uint32_t *ro) {
+    if (ro[0] != 0)
+        return "row_offset[0] is not 0";
+    for (uint64_t r = 0; r < row_num; ++r) {
+        const uint32_t at = ro[r + 1];
+        if (at < ro[r] || at >= size)
+            return "row_offset is not a non-decreasing list of slots inside the array";
+        if (keys[at] != ((r << 32) | 0xFFFFFFFFull))
+            return "a row guard is not at its row_offset slot";
+    }
+    bool any = false;
+    uint64_t prev = 0;
+    for (uint32_t i = 0; i < size; ++i) {
+        if (keys[i] == KEY_NONE || vals[i] == 0)
+            continue;
+        if (any && keys[i] < prev)
+            return "live slots are not in ascending key order";
+        prev = keys[i];
+        any = true;
+    }
+    return nullptr;
+}
+
 }  // namespace
 }  // namespace gpma
 
@@ -836,6 +867,10 @@ gpma_status gpma_load(const char *path, void *stream, gpma_graph **out) {
     std::vector<uint32_t> ro(ro_n);
     from_le(payload.data(), size, keys.data());
     from_le(payload.data() + size * 9ull, ro_n, ro.data());
+    if (const char *why = snapshot_layout_error(row_num, size, keys.data(), payload.data() + size * 8ull, ro.data())) {
+        set_error("gpma_load: %s is not a valid layout: %s", path, why);
+        return GPMA_ERR_IO;
+    }
     gpma_graph *g = new (std::nothrow) gpma_graph();
     if (!g) {
         set_error("gpma_load: host allocation failed");

@@ -472,8 +472,11 @@ GPMA_API gpma_status gpma_partition_rows(const uint64_t *keys, const uint8_t *va
  * keys, values, row_offset) with a checksum; gpma_load creates a graph on the
  * current device with exactly that layout, so updates after a resume give
  * the same layouts as updates without one. A file that is truncated,
- * corrupt, of another version or with an impossible geometry is rejected
- * with GPMA_ERR_IO before any device memory is allocated. */
+ * corrupt, of another version or with an impossible geometry, or whose
+ * layout breaks what the device code relies on (row_offset from 0,
+ * non-decreasing and inside the array, each row's guard at its row_offset
+ * slot, live keys ascending), is rejected with GPMA_ERR_IO before any device
+ * memory is allocated. */
 GPMA_API gpma_status gpma_save(gpma_graph *g, const char *path, void *stream);
 GPMA_API gpma_status gpma_load(const char *path, void *stream, gpma_graph **out);
 
