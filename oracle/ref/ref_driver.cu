@@ -25,6 +25,7 @@
 #include "gpma.cuh"
 #include "gpma_bfs.cuh"
 
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -165,6 +166,28 @@ int main(int argc, char **argv) {
             std::vector<uint32_t> hi(g.upper_element.begin(), g.upper_element.end());
             wr(out, lo.data(), lo.size());
             wr(out, hi.data(), hi.size());
+        } else if (op == 4) {
+            // timed update: update_gpma alone, its wall time in nanoseconds
+            // (no layout digest), for timing the reference's CPU path
+            uint64_t n;
+            rd(in, &n, 1);
+            std::vector<uint64_t> k(n);
+            std::vector<uint8_t> v(n);
+            rd(in, k.data(), n);
+            rd(in, v.data(), n);
+            NATIVE_VEC_KEY<CPU> uk(k.begin(), k.end());
+            NATIVE_VEC_VALUE<CPU> uv(n);
+            for (uint64_t i = 0; i < n; ++i)
+                uv[i] = (VALUE_TYPE)v[i];
+            const auto t0 = std::chrono::steady_clock::now();
+            update_gpma(g, uk, uv);
+            const uint64_t ns = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
+                                    std::chrono::steady_clock::now() - t0)
+                                    .count();
+            uint32_t tag = 4;
+            wr(out, &tag, 1);
+            wr(out, &n, 1);
+            wr(out, &ns, 1);
         } else if (op == 2) {
             uint32_t src;
             rd(in, &src, 1);

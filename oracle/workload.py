@@ -1,7 +1,8 @@
 """Workload scripts for the reference driver and the shared digest.
 
 Test infrastructure only. ``write_script`` encodes a sequence of operations
-("update", keys, values) / ("bfs", src) / ("dump",) in the binary format read
+("update", keys, values) / ("bfs", src) / ("dump",) / ("timed_update", keys,
+values: the update alone, timed, no layout digest) in the binary format read
 by oracle/ref/ref_driver.cu; ``read_output`` decodes its results; ``digest``
 is the order-sensitive 64-bit digest both sides use.
 """
@@ -35,6 +36,12 @@ def write_script(path, row_num: int, ops) -> None:
                 k = np.ascontiguousarray(op[1], np.uint64)
                 v = np.ascontiguousarray(op[2], np.uint8)
                 f.write(struct.pack("<IQ", 1, len(k)))
+                f.write(k.tobytes())
+                f.write(v.tobytes())
+            elif op[0] == "timed_update":
+                k = np.ascontiguousarray(op[1], np.uint64)
+                v = np.ascontiguousarray(op[2], np.uint8)
+                f.write(struct.pack("<IQ", 4, len(k)))
                 f.write(k.tobytes())
                 f.write(v.tobytes())
             elif op[0] == "bfs":
@@ -82,6 +89,9 @@ def read_output(path, row_num: int) -> list[dict]:
             size, row_num = take("<II")
             out.append({"op": "dump", "keys": arr(np.uint64, size), "values": arr(np.uint8, size),
                         "row_offset": arr(np.uint32, row_num + 1)})
+        elif tag == 4:
+            n, ns = take("<QQ")
+            out.append({"op": "timed_update", "keys": n, "seconds": ns * 1e-9})
         else:
             raise ValueError(f"bad tag {tag}")
     return out

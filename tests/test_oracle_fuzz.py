@@ -65,3 +65,24 @@ def test_single_row_hub_matches_reference(built_lib):
         ops.append(("dump",))
     ops.append(("bfs", 7))
     _compare(n, ops)
+
+
+@needs_ref
+def test_timed_update_op_applies_the_same_update(built_lib):
+    """The driver's timed update (used to time the reference's CPU path) changes
+    the structure exactly as the recorded update does."""
+    n, ops = cases.random_case(200)
+    timed = [("timed_update", op[1], op[2]) if op[0] == "update" else op for op in ops]
+    recs = make_golden.run_reference(n, timed)
+    assert sum(r["op"] == "timed_update" for r in recs) == sum(op[0] == "update" for op in ops)
+    assert all(r["seconds"] >= 0 for r in recs if r["op"] == "timed_update")
+    o = OracleGPMA(n, threads=2)
+    dumps = iter(r for r in recs if r["op"] == "dump")
+    for op in ops:
+        if op[0] == "update":
+            o.update(op[1], op[2])
+        elif op[0] == "dump":
+            r = next(dumps)
+            keys, masked, ro = o.export_layout()
+            assert np.array_equal(keys, r["keys"]) and np.array_equal(masked, r["values"])
+            assert np.array_equal(ro, r["row_offset"])
