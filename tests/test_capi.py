@@ -25,6 +25,23 @@ def test_header_declares_entry_points():
         assert core in names
 
 
+def test_header_is_plain_c99_and_links(tmp_path, built_lib):
+    """An FFI or C caller includes the header with a C compiler: no C++ in it,
+    no warnings under -pedantic, and every call resolves against the library."""
+    calls = "\n".join(f"    (void)&{n};" for n in declared_symbols())
+    src = tmp_path / "c_caller.c"
+    src.write_text('#include "gpma_gb300.h"\n#include <string.h>\nint main(void) {\n'
+                   f"{calls}\n"
+                   "    return gpma_create(4, 0, 0) == GPMA_ERR_INVALID && strlen(gpma_last_error()) > 0 ? 0 : 1;\n}\n")
+    exe = tmp_path / "c_caller"
+    libdir = ROOT / "gpma_bfs_gb300"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", f"-I{ROOT / 'include'}",
+                        str(src), f"-L{libdir}", "-lgpma_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([str(exe)]).returncode == 0
+
+
 def _exported(path):
     out = subprocess.run(["nm", "-D", "--defined-only", str(path)], capture_output=True, text=True, check=True).stdout
     return {line.split()[-1] for line in out.splitlines() if " T " in line}
