@@ -395,7 +395,9 @@ GPMA_API gpma_status gpma_bfs_level_profile(const gpma_graph *g, double *ms, uin
 /* ---- tuning -----------------------------------------------------------------
  * No reference counterpart. Launch shapes and switch points of the kernels;
  * they change speed, never results (the PMA geometry itself is fixed by the
- * reference's sizing rules). Process-wide; takes effect at the next call. */
+ * reference's sizing rules). Process-wide; takes effect at the next call.
+ * The settings are plain words read at each launch: change them while no
+ * other host thread is inside a library call. */
 typedef struct gpma_tuning {
     uint32_t bfs_dense_div;        /* single-source BFS: a level whose frontier's rows span >= size / bfs_dense_div
                                       slots sweeps the whole slot array instead of walking rows (0: never) */
