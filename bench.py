@@ -831,10 +831,21 @@ def cpu_baseline(n, keys, half, slide, steps):
         o.update(k, v)
         t += time.perf_counter() - t0
         batch = len(k)
+    # the next slides on one core (the reference's own CPU baseline program is single-threaded)
+    o.set_threads(1)
+    one_steps = min(steps, 3)
+    t1 = 0.0
+    for i in range(steps, steps + one_steps):
+        k, v = slide(i)
+        t0 = time.perf_counter()
+        o.update(k, v)
+        t1 += time.perf_counter() - t0
     o.close()
     return {"value": steps * batch / t, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{steps} slide updates of {batch:,} keys after an untimed load of {half:,} edges "
-                      f"(same graph), OpenMP on {cores} threads"}
+                      f"(same graph), OpenMP on {cores} threads",
+            "single_core": {"value": one_steps * batch / t1, "unit": UNIT, "cores": 1,
+                            "sample": f"the next {one_steps} slide updates on one thread"}}
 
 
 def run_reference(args):

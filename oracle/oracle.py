@@ -89,6 +89,10 @@ class OracleGPMA:
     def _s(self) -> _Gpma:
         return self._g.contents
 
+    def set_threads(self, threads: int) -> None:
+        """OpenMP threads of the following calls (results do not depend on it)."""
+        self._s.threads = max(1, int(threads))
+
     def update(self, keys: np.ndarray, values: np.ndarray) -> None:
         k = np.ascontiguousarray(keys, np.uint64)
         v = np.ascontiguousarray(values, np.uint8)
