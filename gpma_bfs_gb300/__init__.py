@@ -138,6 +138,7 @@ def lib() -> ctypes.CDLL:
         "gpma_server_destroy": (st, [P]),
         "gpma_server_add_graph": (st, [P, u32, u64, ctypes.POINTER(u32)]),
         "gpma_server_graph": (st, [P, u32, ctypes.POINTER(P)]),
+        "gpma_server_cancel": (st, [P, u64]),
         "gpma_server_submit_update": (st, [P, u32, P, P, u64, ctypes.c_double, ctypes.POINTER(u64)]),
         "gpma_server_submit_bfs": (st, [P, u32, P, u32, ctypes.c_double, P, ctypes.POINTER(u64)]),
         "gpma_server_run_round": (st, [P, ctypes.c_double, ctypes.POINTER(_RoundInfo)]),
@@ -869,6 +870,11 @@ class Server:
         ri = _RoundInfo()
         _check(lib().gpma_server_run_round(self._h, float(now), ctypes.byref(ri)), "gpma_server_run_round")
         return {name: getattr(ri, name) for name, _ in _RoundInfo._fields_}
+
+    def cancel(self, rid: int) -> None:
+        """Withdraws a request no round has taken yet (state 3 afterwards)."""
+        _check(lib().gpma_server_cancel(self._h, int(rid)), "gpma_server_cancel")
+        self._keep.pop(int(rid), None)
 
     def poll(self, rid: int, release: bool = False) -> dict:
         info = _RequestInfo()

@@ -581,6 +581,35 @@ gpma_status gpma_server_poll(gpma_server *s, uint64_t request_id, int release, g
     return GPMA_OK;
 }
 
+gpma_status gpma_server_cancel(gpma_server *s, uint64_t request_id) {
+    if (!s) {
+        set_error("gpma_server_cancel: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    auto it = s->reqs.find(request_id);
+    if (it == s->reqs.end()) {
+        set_error("gpma_server_cancel: unknown request %llu", (unsigned long long)request_id);
+        return GPMA_ERR_INVALID;
+    }
+    Request *r = it->second.get();
+    if (r->state != GPMA_REQ_QUEUED) {
+        set_error("gpma_server_cancel: request %llu has already run", (unsigned long long)request_id);
+        return GPMA_ERR_INVALID;
+    }
+    // a queued request sits in its graph's queue until a round takes it
+    std::deque<uint64_t> &q = s->graphs[r->graph].queue;
+    q.erase(std::find(q.begin(), q.end(), request_id));
+    s->queued--;
+    s->queued_keys -= r->n;
+    r->state = GPMA_REQ_CANCELLED;
+    r->levels_out = nullptr;
+    r->keys.clear();
+    r->keys.shrink_to_fit();
+    r->vals.clear();
+    r->vals.shrink_to_fit();
+    return GPMA_OK;
+}
+
 gpma_status gpma_server_last_round(const gpma_server *s, uint64_t *ids, uint32_t capacity, uint32_t *count) {
     if (!s || !count || (capacity && !ids)) {
         set_error("gpma_server_last_round: null argument");

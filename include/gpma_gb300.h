@@ -259,7 +259,8 @@ typedef struct gpma_server_config {
 typedef enum gpma_request_state {
     GPMA_REQ_QUEUED = 0,
     GPMA_REQ_DONE = 1,
-    GPMA_REQ_FAILED = 2
+    GPMA_REQ_FAILED = 2,
+    GPMA_REQ_CANCELLED = 3  /* withdrawn by gpma_server_cancel before a round took it */
 } gpma_request_state;
 
 typedef struct gpma_request_info {
@@ -317,6 +318,14 @@ GPMA_API gpma_status gpma_server_submit_bfs(gpma_server *s, uint32_t graph_id, c
 GPMA_API gpma_status gpma_server_run_round(gpma_server *s, double now, gpma_round_info *info);
 /* A request's state and result; release != 0 forgets a finished request. */
 GPMA_API gpma_status gpma_server_poll(gpma_server *s, uint64_t request_id, int release, gpma_request_info *out);
+/* Withdraws a request that no round has taken yet (its client went away, or
+ * it waits behind work it no longer needs): it leaves its graph's queue, its
+ * keys no longer count against max_queued_keys, its level array is never
+ * written, and polls report GPMA_REQ_CANCELLED. The graph's other requests
+ * keep their order; a search queued behind a cancelled update sees the graph
+ * without that update. GPMA_ERR_INVALID for an unknown request or one that
+ * has already run. No reference counterpart. */
+GPMA_API gpma_status gpma_server_cancel(gpma_server *s, uint64_t request_id);
 /* Ids of the requests the last round ran, in execution order (updates, then
  * searches graph by graph, lanes ascending). */
 GPMA_API gpma_status gpma_server_last_round(const gpma_server *s, uint64_t *ids, uint32_t capacity, uint32_t *count);

@@ -200,3 +200,59 @@ def test_replay_waits_when_the_queue_is_full(G):
         big.submit_update(gid, *_upd(11), arrival=0.0)  # never admissible
     srv.close()
     big.close()
+
+
+def test_cancel_withdraws_queued_requests_only(G):
+    """A client that goes away: its queued request leaves the queue (keys no
+    longer count), the graph's other requests keep their order, and a request
+    that already ran cannot be cancelled."""
+    s = G.Server(plan_only=True, max_queued_keys=25)
+    g0, g1 = s.add_graph(100, 1000), s.add_graph(100, 1000)
+    u1 = s.submit_update(g0, *_upd(10), arrival=0.0)
+    u2 = s.submit_update(g0, *_upd(10), arrival=0.1)
+    b1 = s.submit_bfs(g0, [1], arrival=0.2, levels=True)
+    b2 = s.submit_bfs(g1, [2], arrival=0.0)
+    with pytest.raises(G.GPMAError) as e:
+        s.submit_update(g1, *_upd(10), arrival=0.3)  # 30 keys would wait: over max_queued_keys
+    assert e.value.status == G.ERR_BUSY
+    s.cancel(u2)
+    assert s.queued()[:2] == (3, 10)
+    u3 = s.submit_update(g1, *_upd(10), arrival=0.3)  # fits now
+    s.cancel(b2)
+    assert s.poll(u2)["state"] == 3 and s.poll(b2)["state"] == 3 and s.levels(b2) is None
+    s.run_round(1.0)
+    # u1 then the search behind it (u2 is gone); g1's head is now its update
+    assert s.last_round() == [u1, u3, b1]
+    assert s.poll(b1)["state"] == 1
+    with pytest.raises(G.GPMAError):
+        s.cancel(u1)  # already ran
+    with pytest.raises(G.GPMAError):
+        s.cancel(12345)  # unknown
+    assert s.poll(u2, release=True)["state"] == 3
+    with pytest.raises(G.GPMAError):
+        s.poll(u2)  # released
+    assert s.queued()[0] == 0 and s.run_round(2.0)["updates"] == 0
+    s.close()
+
+
+def test_cancelled_update_frees_the_graph_for_its_searches(G):
+    """An update that must wait (the round's key limit is taken by an earlier
+    graph) holds back the searches queued behind it; cancelled, it no longer
+    does, and they run in the same round."""
+    def scenario(cancel):
+        s = G.Server(plan_only=True, max_round_keys=20)
+        g0, g1 = s.add_graph(100, 1000), s.add_graph(100, 1000)
+        first = s.submit_update(g1, *_upd(15), arrival=0.0)
+        late = s.submit_update(g0, *_upd(10), arrival=0.1)
+        b = s.submit_bfs(g0, [5], arrival=0.1)
+        if cancel:
+            s.cancel(late)
+        s.run_round(1.0)
+        ran = s.last_round()
+        s.close()
+        return ran, first, late, b
+
+    ran, first, late, b = scenario(cancel=False)
+    assert ran == [first]  # g0's update waits for the next round, its search with it
+    ran, first, late, b = scenario(cancel=True)
+    assert ran == [first, b]
