@@ -598,7 +598,12 @@ gpma_status gpma_server_cancel(gpma_server *s, uint64_t request_id) {
     }
     // a queued request sits in its graph's queue until a round takes it
     std::deque<uint64_t> &q = s->graphs[r->graph].queue;
-    q.erase(std::find(q.begin(), q.end(), request_id));
+    const auto qi = std::find(q.begin(), q.end(), request_id);
+    if (qi == q.end()) {
+        set_error("gpma_server_cancel: request %llu is not in its graph's queue", (unsigned long long)request_id);
+        return GPMA_ERR_INVALID;
+    }
+    q.erase(qi);
     s->queued--;
     s->queued_keys -= r->n;
     r->state = GPMA_REQ_CANCELLED;
