@@ -86,3 +86,19 @@ def test_timed_update_op_applies_the_same_update(built_lib):
             keys, masked, ro = o.export_layout()
             assert np.array_equal(keys, r["keys"]) and np.array_equal(masked, r["values"])
             assert np.array_equal(ro, r["row_offset"])
+
+
+@needs_ref
+@pytest.mark.parametrize("spec", [dict(kind="chung_lu", n=20000, m=300000, exponent=2.3, max_degree=3000, seed=41),
+                                  dict(kind="rmat", scale=14, edge_factor=16, seed=42)],
+                         ids=["chung_lu_20k", "rmat14"])
+def test_larger_slides_match_reference(spec, built_lib):
+    """The social configuration's shape at a size the reference runs in
+    seconds (power-law hubs: long rows, deep windows), and R-MAT scale 14:
+    half-load (bulk of the first batch), 100 slides, BFS from a hub before
+    and after, a whole-layout dump at the end."""
+    from gpma_bfs_gb300.workloads import make_graph
+
+    n, src, dst = make_graph(spec)
+    ops = cases.sliding_ops(n, src, dst, 100, bfs_src=0, dumps=(100,))
+    _compare(n, ops)
