@@ -18,9 +18,14 @@ value  - updates/s over K steps with batches resident in HBM, device time
 e2e    - the same through the C ABI from pinned host buffers: the batch
          upload and the read-back of the update status are inside the span.
 --impl reference - the reference algorithm on the host cores (the C
-         restatement in oracle/, OpenMP on all cores), same workload/metric.
+         restatement in oracle/, OpenMP on all cores), same workload/metric;
+         it loads only oracle/ libraries (graph generator included).
 Several GPUs run independent replicas (the path does not shard); value sums
 the ranks' updates over the slowest rank's time.
+
+The printed line carries the headline figures of every configuration as
+top-level scalars (bfs, batched, served, large_graph); the full sub-reports
+go to --report (default bench_report.json next to this file).
 """
 from __future__ import annotations
 
@@ -44,6 +49,8 @@ GRAPH = "social"
 DATA = ("synthetic: seeded Chung-Lu power-law graph with pokec's shape (1,632,803 nodes, 30,622,564 edges, "
         "exponent 2.3, max expected degree 9,000, seed 2), shuffled")
 L2_FLUSH_BYTES = 256 << 20
+# the social configuration's generator parameters (gpma_bfs_gb300.workloads.GRAPHS["social"])
+SOCIAL = dict(n=1632803, m=30622564, exponent=2.3, max_degree=9000, seed=2)
 
 
 def workload_config(n, m, step):
@@ -168,14 +175,44 @@ def replica_value(units_per_rank: float, time_s: float, world: int) -> float:
     return units_per_rank * world / time_s
 
 
-def live_out_degree_sum(g, levels):
-    """Edges traversed by a BFS: live out-edges of the reached nodes."""
+def bfs_counts(g, levels):
+    """(edges traversed, algorithmic bytes) of a BFS: the live out-edges of the
+    reached nodes (GTEPS numerator), and the HBM model 9 B x slots of every
+    reached row + 8 B x reached nodes (their row_offset pair) + 4 B x nodes
+    (level array) + 2 x nodes/8 B x levels (frontier bitmaps)."""
     keys, vals, ro = g.export_layout()
     valid = ((keys & np.uint64(0xFFFFFFFF)) != np.uint64(0xFFFFFFFF)) & (vals != 0)
     csum = np.concatenate([[0], np.cumsum(valid, dtype=np.int64)])
     ro = ro.astype(np.int64)
     per_row = csum[ro[1:]] - csum[ro[:-1]]
-    return int(per_row[levels != 0].sum())
+    reached = levels != 0
+    n = len(levels)
+    slots = int((ro[1:] - ro[:-1])[reached].sum())
+    model = 9.0 * slots + 8.0 * int(reached.sum()) + 4.0 * n + 2.0 * (n / 8.0) * int(levels.max())
+    return int(per_row[reached].sum()), model
+
+
+class _DeviceArray:
+    """A zero-copy view of library-owned device memory for torch.as_tensor."""
+
+    def __init__(self, ptr: int, n: int, typestr: str):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 3}
+
+
+def live_out_degrees(G, g):
+    """Live out-degree of every row, on the device (torch), read straight from
+    the graph's arrays: for graphs too large to export."""
+    import torch
+
+    kp, vp, _ = g.device_arrays()
+    size = g.get_size()
+    keys = torch.as_tensor(_DeviceArray(kp, size, "<i8"), device="cuda")
+    vals = torch.as_tensor(_DeviceArray(vp, size, "|u1"), device="cuda")
+    src = keys >> 32
+    ok = (vals != 0) & ((keys & 0xFFFFFFFF) != 0xFFFFFFFF) & (keys >= 0) & (src < g.row_num)
+    deg = torch.bincount(src[ok], minlength=g.row_num)
+    del keys, vals, src, ok
+    return deg
 
 
 def run_gpu(args):
@@ -210,9 +247,10 @@ def run_gpu(args):
             _, reached = G.gpma_bfs(g, n, m, 0, out, stream)
             times.append(g.profile()["bfs_ms"])
         levels = out.cpu().numpy().view(np.uint32)
-        edges = live_out_degree_sum(g, levels)
+        edges, model = bfs_counts(g, levels)
         ms = statistics.median(times)
-        return {"reached": int(reached), "edges_traversed": edges, "ms": ms, "gteps": edges / (ms * 1e-3) / 1e9}
+        return {"reached": int(reached), "edges_traversed": edges, "ms": ms, "gteps": edges / (ms * 1e-3) / 1e9,
+                "levels": int(levels.max()), "model_bytes": model}
 
     tuning = {}
     if not args.no_autotune:
@@ -294,48 +332,96 @@ def run_gpu(args):
     g.close()
     del dk, dv, hk, hv
     steps_report = run_steps(args, G, n, keys, half, slide, stream, flush)
+    del keys
     batched = None
     if args.batched_graphs > 0:
         batched = run_batched(args, stream)
     served = None
     if args.served_seconds > 0:
         served = run_served(args, stream)
+    large = None
+    if args.large_graph and rank == 0:
+        large = run_sweep(args, sizes=(100_000, 1_000_000, 10_000_000), ratios=((1, 1),), reps=2, bfs_sources=4)
 
     if rank == 0:
+        bfs_roof = {"bound": "hbm", "kernel": "bfs_kernel", "unit": "GB/s", "peak": peak,
+                    "bytes_per_launch": bfs_after["model_bytes"], "launch_ms": bfs_after["ms"],
+                    "achieved": bfs_after["model_bytes"] / (bfs_after["ms"] * 1e-3) / 1e9,
+                    "traffic": profiled_traffic("bfs_kernel")}
+        bfs_roof["frac"] = bfs_roof["achieved"] / peak
+        roofline = {"bound": "hbm", "kernel": "update_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_launch": upd_bytes,
+                    "launch_ms": upd_ms, "peak_source": peak_src, "step_bytes": step_bytes,
+                    "step_frac": step_bytes / (1e-3 * time_s * 1e3 / args.steps) / 1e9 / peak}
+        phases = {"update_kernel": prof["update_kernel_ms"] / args.steps,
+                  "in_kernel_sort": prof["sort_ms"] / args.steps,
+                  "in_kernel_locate": prof["locate_ms"] / args.steps,
+                  "in_kernel_group": prof["group_ms"] / args.steps,
+                  "in_kernel_levels": prof["levels_ms"] / args.steps,
+                  "root_rebuild": prof["rebuild_ms"] / args.steps}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * time_s / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": DATA,
             "config": workload_config(n, m, step),
-            "roofline": {"bound": "hbm", "kernel": "update_kernel", "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "algorithmic_bytes_per_launch": upd_bytes, "launch_ms": upd_ms, "peak_source": peak_src,
-                         "step_bytes": step_bytes, "step_frac": step_bytes / (1e-3 * time_s * 1e3 / args.steps)
-                         / 1e9 / peak},
+            "roofline": roofline,
             "e2e": {"value": updates / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 9 * batch,
                     "d2h_bytes_per_step": 64},
             "gpu_launches": prof["kernel_launches"],
             "clocks": clk.summary(),
-            "autotune": tuning or None,
-            "analytics": analytics,
-            "bfs": {"before": bfs_before, "after": bfs_after, "unit": "GTEPS",
-                    "gteps": bfs_after["gteps"]},
-            "phases_ms_per_step": {"update_kernel": prof["update_kernel_ms"] / args.steps,
-                                   "in_kernel_sort": prof["sort_ms"] / args.steps,
-                                   "in_kernel_locate": prof["locate_ms"] / args.steps,
-                                   "in_kernel_group": prof["group_ms"] / args.steps,
-                                   "in_kernel_levels": prof["levels_ms"] / args.steps,
-                                   "root_rebuild": prof["rebuild_ms"] / args.steps},
-            "levels_per_step": (st1["levels_visited"] - st0["levels_visited"]) / args.steps,
-            "setup_s": {"generate": gen_s},
+            "phases_ms_per_step": phases,
+            "bfs": {"unit": "GTEPS", "gteps": bfs_after["gteps"], "gteps_before": bfs_before["gteps"],
+                    "ms": bfs_after["ms"], "reached": bfs_after["reached"], "levels": bfs_after["levels"],
+                    "roofline": bfs_roof},
         }
         if cpu:
             line["cpu_baseline"] = cpu
-        line["update_bfs_steps"] = steps_report
+        line["update_bfs_step_ms"] = {"eager": steps_report["eager_ms"], "graph": steps_report["graph_ms"],
+                                      "identical": steps_report["identical_levels"]}
         if batched:
-            line["batched"] = batched
+            bu, bb = batched["update"], batched["bfs"]
+            line["batched"] = {
+                "graphs": batched["graphs"], "updates_per_step": batched["updates_per_step"],
+                "updates_per_s": bu["batched_updates_per_s"], "plain_updates_per_s": bu["plain_updates_per_s"],
+                "speedup_vs_plain": bu["speedup"], "roofline_frac": bu["roofline"]["frac"],
+                "update_kernel_ms": bu["phases_ms_per_step"]["update_kernel_ms"],
+                "bfs_gteps": bb["batched_gteps"], "plain_bfs_gteps": bb["plain_gteps"], "bfs_speedup": bb["speedup"],
+                "identical_layouts": bu["identical_layouts"],
+                "step_ms": {"eager": batched["update_bfs_steps"]["eager_ms"],
+                            "graph": batched["update_bfs_steps"]["graph_ms"],
+                            "identical": batched["update_bfs_steps"]["identical"]}}
         if served:
-            line["served"] = served
+            light, sat = served["phases"][0], served["phases"][-1]
+
+            def lat(ph, who):
+                return {f"{k}_{q[:3]}_ms": (ph[who][f"{k}_latency"] or {}).get(q) for k in ("update", "bfs")
+                        for q in ("p50_ms", "p99_ms")}
+
+            line["served"] = {
+                "graphs": served["graphs"], "requests": served["requests"], "failed": served["failed"],
+                "identical_results": served["identical_results"],
+                "light_load": {"rate_per_s": light["rate_per_s"], "served": lat(light, "served"),
+                               "plain": lat(light, "plain")},
+                "saturation": {"rate_per_s": sat["rate_per_s"], "speedup_sustained": sat["speedup_sustained"],
+                               "requests_per_s": sat["served"]["requests_per_s"],
+                               "plain_requests_per_s": sat["plain"]["requests_per_s"],
+                               "served": lat(sat, "served"), "plain": lat(sat, "plain")}}
+        if large:
+            line["large_graph"] = {
+                "workload": large["config"]["workload"],
+                "updates_per_s": {str(r["batch"]): r["edge_updates_per_s"] for r in large["updates"]},
+                "kernel_hbm_frac": {str(r["batch"]): r["hbm_frac"] for r in large["updates"]},
+                "bfs_gteps": large["bfs"]["gteps"], "multi_source_gteps": large["bfs"]["multi_gteps"],
+                "load_edges_per_s": large["load"]["edges_per_s"]}
+        report = dict(line)
+        report.update({"roofline": roofline, "autotune": tuning or None, "analytics": analytics,
+                       "bfs_detail": {"before": bfs_before, "after": bfs_after},
+                       "levels_per_step": (st1["levels_visited"] - st0["levels_visited"]) / args.steps,
+                       "setup_s": {"generate": gen_s}, "update_bfs_steps": steps_report,
+                       "batched_detail": batched, "served_detail": served, "large_graph_detail": large})
+        if args.report:
+            Path(args.report).write_text(json.dumps(report, indent=1))
+            line["report"] = str(args.report)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -696,7 +782,11 @@ def run_served(args, stream):
     }
 
 
-def run_sweep(args):
+SWEEP_SIZES = (1_000, 10_000, 100_000, 1_000_000, 10_000_000)
+SWEEP_RATIOS = ((1, 0), (1, 1), (0, 1))
+
+
+def run_sweep(args, sizes=SWEEP_SIZES, ratios=SWEEP_RATIOS, reps=None, bfs_sources=16):
     """Large single graph + batch sweep: R-MAT scale `sweep_scale` (edge factor
     `sweep_edge_factor`, a/b/c = .57/.19/.19, seed 3, deduplicated, shuffled)
     loaded except for a reserve of fresh edges; then, per insert:delete ratio
@@ -704,12 +794,12 @@ def run_sweep(args):
     inserts and uniformly drawn existing edges to delete, each timed alone
     (device-resident batch, L2 flushed, CUDA events); then BFS from 16 random
     non-isolated sources (one search each, and all 16 as lanes of one
-    multi-source search)."""
+    multi-source search). The default bench run takes a subset: batches of
+    100k, 1M and 10M keys at 1:1, two each, BFS from 4 sources."""
     import torch
 
     import gpma_bfs_gb300 as G
 
-    torch.cuda.set_device(0)
     stream = torch.cuda.current_stream()
     t0 = time.time()
     src, dst = G.gen_rmat(args.sweep_scale, args.sweep_edge_factor, seed=3)
@@ -718,10 +808,9 @@ def run_sweep(args):
     del src, dst
     m = len(keys)
     gen_s = time.time() - t0
-    reps = args.sweep_reps
+    reps = reps or args.sweep_reps
     # batch sizes the graph can feed (fresh inserts and distinct deletes)
-    sizes = [s for s in (1_000, 10_000, 100_000, 1_000_000, 10_000_000) if 2 * reps * s <= m // 4]
-    ratios = [(1, 0), (1, 1), (0, 1)]
+    sizes = [s for s in sizes if 2 * reps * s <= m // 4]
     reserve = sum(reps * s * i // (i + d) for s in sizes for i, d in ratios) + 1
     loaded = keys[: m - reserve]
     fresh = keys[m - reserve:]
@@ -773,36 +862,32 @@ def run_sweep(args):
             bytes_ = 18.0 * size + 18.0 * statistics.median(slots)
             rows.append({"ratio": f"{ins}:{dels}", "batch": size, "ms": ms, "edge_updates_per_s": size / (ms * 1e-3),
                          "kernel_ms": kms, "hbm_frac": bytes_ / (kms * 1e-3) / 1e9 / peak if kms else None})
-    # BFS from 16 random non-isolated sources (live out-degree per row, once)
-    lk, lvals, ro = g.export_layout()
-    valid = ((lk & np.uint64(0xFFFFFFFF)) != np.uint64(0xFFFFFFFF)) & (lvals != 0)
-    del lk, lvals
-    csum = np.concatenate([[0], np.cumsum(valid, dtype=np.int64)])
-    del valid
-    ro = ro.astype(np.int64)
-    per_row = csum[ro[1:]] - csum[ro[:-1]]
-    del csum
-    cand = np.nonzero(per_row > 0)[0]
-    sources = rng.choice(cand, 16, replace=False).astype(np.uint32)
+    # BFS from random non-isolated sources (live out-degree per row, once, on the device)
+    deg = live_out_degrees(G, g)
+    cand = torch.nonzero(deg > 0).flatten().cpu().numpy()
+    sources = rng.choice(cand, bfs_sources, replace=False).astype(np.uint32)
     out = torch.empty(n, dtype=torch.int32, device="cuda")
     single = []
     for s in sources:
         g.reset_profile()
         G.gpma_bfs(g, n, live, int(s), out, stream)
-        lv = out.cpu().numpy().view(np.uint32)
-        single.append((g.profile()["bfs_ms"], int(per_row[lv != 0].sum()), int((lv != 0).sum())))
+        hit = out != 0
+        single.append((g.profile()["bfs_ms"], int(deg[hit].sum()), int(hit.sum())))
     g.reset_profile()
-    lvm = torch.empty(16 * n, dtype=torch.int32, device="cuda")
-    G.gpma_bfs_multi(g, sources, lvm.view(16, n), stream=stream)
+    lvm = torch.empty(len(sources) * n, dtype=torch.int32, device="cuda")
+    G.gpma_bfs_multi(g, sources, lvm.view(len(sources), n), stream=stream)
     pm = g.profile()
+    del deg, lvm
     bfs_ms = statistics.median(x[0] for x in single)
     edges = statistics.median(x[1] for x in single)
     g.close()
     return {
         "metric": "edge updates/s and BFS GTEPS, large single graph", "impl": "gpma",
         "config": {"workload": f"R-MAT scale {args.sweep_scale}, edge factor {args.sweep_edge_factor}, "
-                               f"{m:,} edges after dedup, {len(loaded):,} loaded, batch sweep 1k-10M at 1:0 / 1:1 / "
-                               f"0:1, BFS from 16 random non-isolated sources",
+                               f"{m:,} edges after dedup, {len(loaded):,} loaded, batches of "
+                               + "/".join(f"{z:,}" for z in sizes) + " keys at "
+                               + " / ".join(f"{i}:{d}" for i, d in ratios)
+                               + f", {reps} each, BFS from {len(sources)} random non-isolated sources",
                    "l2": "flushed before every timed update"},
         "geometry": geo, "density_after_load": (len(loaded) + n + 2) / geo["size"],
         "load": {"edges": len(loaded), "seconds": load_s, "edges_per_s": len(loaded) / load_s},
@@ -810,7 +895,7 @@ def run_sweep(args):
         "bfs": {"single_source_median_ms": bfs_ms, "median_edges": edges,
                 "gteps": edges / (bfs_ms * 1e-3) / 1e9,
                 "reached": [x[2] for x in single],
-                "multi16_ms": pm["bfs_ms"], "multi16_gteps": pm["bfs_edges"] / (pm["bfs_ms"] * 1e-3) / 1e9},
+                "multi_ms": pm["bfs_ms"], "multi_gteps": pm["bfs_edges"] / (pm["bfs_ms"] * 1e-3) / 1e9},
         "setup_s": {"generate": gen_s},
     }
 
@@ -849,16 +934,19 @@ def cpu_baseline(n, keys, half, slide, steps):
 
 
 def run_reference(args):
+    """The reference algorithm (the oracle's restatement of GPMA<CPU>) on all
+    host cores. Loads only oracle/ libraries: the graph comes from the same
+    generator source built into oracle/_build/libgraphgen.so."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return
-    import gpma_bfs_gb300 as G
-    from gpma_bfs_gb300.workloads import make_graph
-    from oracle.oracle import OracleGPMA, build
+    from oracle.oracle import OracleGPMA, build, gen_chung_lu
 
     build()
-    n, src, dst = make_graph(GRAPH)
-    keys = G.edges_to_keys(src, dst)
+    n = SOCIAL["n"]
+    src, dst = gen_chung_lu(**SOCIAL)
+    keys = (src.astype(np.uint64) << np.uint64(32)) + dst.astype(np.uint64)
+    del src, dst
     half, step, slide = schedule(keys)
     cores = os.cpu_count() or 1
     o = OracleGPMA(n, threads=cores)
@@ -908,10 +996,18 @@ def main():
     ap.add_argument("--sweep-scale", type=int, default=24)
     ap.add_argument("--sweep-edge-factor", type=int, default=32)
     ap.add_argument("--sweep-reps", type=int, default=3)
+    ap.add_argument("--no-large-graph", dest="large_graph", action="store_false",
+                    help="skip the large-graph subset (R-MAT scale 24: 100k/1M/10M batches at 1:1, BFS) of the "
+                         "default run")
+    ap.add_argument("--report", default=str(ROOT / "bench_report.json"),
+                    help="file for the full sub-reports ('' for none)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.sweep:
+        import torch
+
+        torch.cuda.set_device(0)
         print(json.dumps(run_sweep(args)), flush=True)
     elif args.impl == "reference":
         run_reference(args)

@@ -74,6 +74,11 @@ class _Tuning(ctypes.Structure):
                [("reserved", ctypes.c_uint32 * 3)]
 
 
+class _TestHooks(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint32) for n in ("update_stall", "bfs_stall", "wait_limit_us", "noalloc_chunk_cap",
+                                               "noalloc_overflows")] + [("reserved", ctypes.c_uint32 * 3)]
+
+
 class _StepStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in ("runs", "graph_launches", "builds", "param_updates", "host_runs")] + \
         [("last_ms", ctypes.c_double), ("total_ms", ctypes.c_double)]
@@ -149,6 +154,8 @@ def lib() -> ctypes.CDLL:
         "gpma_get_tuning": (st, [ctypes.POINTER(_Tuning)]),
         "gpma_bfs_level_profile": (st, [P, P, P, P, u32, ctypes.POINTER(u32)]),
         "gpma_set_tuning": (st, [ctypes.POINTER(_Tuning)]),
+        "gpma_get_test_hooks": (st, [ctypes.POINTER(_TestHooks)]),
+        "gpma_set_test_hooks": (st, [ctypes.POINTER(_TestHooks)]),
         "gpma_set_profiling": (st, [P, ctypes.c_int]),
         "gpma_get_profile": (st, [P, ctypes.POINTER(_Profile)]),
         "gpma_reset_profile": (st, [P]),
@@ -552,6 +559,31 @@ def set_tuning(**values) -> dict:
     t = _Tuning(*[int(values.get(n, old[n])) for n in TUNING_FIELDS])
     _check(lib().gpma_set_tuning(ctypes.byref(t)), "gpma_set_tuning")
     return old
+
+
+TEST_HOOK_FIELDS = ("update_stall", "bfs_stall", "wait_limit_us", "noalloc_chunk_cap")
+
+
+def get_test_hooks() -> dict:
+    """Error-path test hooks in effect, plus noalloc_overflows: how often the
+    last gpma_bfs_noalloc call found its long-row chunk list full."""
+    h = _TestHooks()
+    _check(lib().gpma_get_test_hooks(ctypes.byref(h)), "gpma_get_test_hooks")
+    return {n: getattr(h, n) for n in TEST_HOOK_FIELDS + ("noalloc_overflows",)}
+
+
+def set_test_hooks(**values) -> dict:
+    """Changes some test-hook fields (update_stall / bfs_stall: the next
+    launches' first grid barrier waits for an arrival that never comes and
+    gives up after wait_limit_us; noalloc_chunk_cap: entries of the
+    no-allocation BFS's chunk list); returns the previous settings."""
+    old = get_test_hooks()
+    unknown = set(values) - set(TEST_HOOK_FIELDS)
+    if unknown:
+        raise ValueError(f"unknown test hooks {sorted(unknown)}")
+    h = _TestHooks(*[int(values.get(n, old[n])) for n in TEST_HOOK_FIELDS])
+    _check(lib().gpma_set_test_hooks(ctypes.byref(h)), "gpma_set_test_hooks")
+    return {n: old[n] for n in TEST_HOOK_FIELDS}
 
 
 # ---- synthetic graphs and the reference's text format -------------------------

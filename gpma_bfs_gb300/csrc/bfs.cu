@@ -40,6 +40,7 @@ enum : uint32_t {
     CTL_ERR = 6,
     CTL_LEVELS = 7,
     CTL_REACHED = 8,
+    CTL_OVERFLOW = 9, // times a warp found the chunk list full and walked its long rows in place
     CTL_BAR = 10,     // GridBarrier (2 words)
     CTL_SLOTS = 12,   // 3 rotating counters: slots of the current frontier's rows (measured levels)
     CTL_WORDS = 16,
@@ -90,6 +91,9 @@ struct BfsArgs {
     uint32_t *ctl;
     uint32_t dense_div;  // a level whose frontier rows span >= size / dense_div slots sweeps every slot (0: never)
     unsigned long long *stamps;  // per-level profile (CTL_PROFILE_LEVELS stamps + info words) or null
+    // test hooks: extra arrivals the first grid barrier waits for, and its limit
+    uint32_t stall;
+    uint64_t stall_limit_ns;
 };
 
 // N edge slots of one lane (SIZE_NONE: absent): every key, value and
@@ -241,6 +245,8 @@ __device__ __forceinline__ uint32_t frontier_pass(const BfsArgs &A, uint32_t *fr
                     for (uint32_t c = base + lane; c < min(base + ch_total, list_cap); c += 32)
                         list[c] = make_uint2(0, 0);
                     overflow = true;
+                    if (lane == 0)
+                        atomicAdd(A.ctl + CTL_OVERFLOW, 1u);
                 }
             }
         }
@@ -299,6 +305,7 @@ __global__ void __launch_bounds__(BLOCK, 5) bfs_kernel(BfsArgs A) {
         if (A.stamps && blockIdx.x == 0 && threadIdx.x == 0 && i < CTL_PROFILE_LEVELS)
             A.stamps[i] = globaltimer_ns();
         const uint32_t frontier = cta_broadcast_read(A.ctl + CTL_CNT + i % 3);
+        const uint32_t stall = i == 0 ? A.stall : 0u;  // test hook: the first barrier never completes
         if (frontier == 0)
             break;
         const uint32_t prev_frontier = last_frontier;
@@ -326,7 +333,7 @@ __global__ void __launch_bounds__(BLOCK, 5) bfs_kernel(BfsArgs A) {
                 slots += __shfl_xor_sync(0xFFFFFFFFu, slots, d);
             if (lane == 0 && slots)
                 atomicAdd(A.ctl + CTL_SLOTS + i % 3, slots);
-            if (!grid_barrier(bar, err))
+            if (!grid_barrier(bar, err, stall, A.stall_limit_ns))
                 return;
             dense = (uint64_t)cta_broadcast_read(A.ctl + CTL_SLOTS + i % 3) * A.dense_div >= A.size;
         }
@@ -350,12 +357,12 @@ __global__ void __launch_bounds__(BLOCK, 5) bfs_kernel(BfsArgs A) {
                 const uint2 v = make_uint2(A.vals[0] | (A.vals[1] << 8) | (A.vals[2] << 16) | ((uint32_t)A.vals[3] << 24), 0u);
                 fresh += dense_visit8(A, k, v, front_cur, next_level, front_next);
             }
-            if (!grid_barrier(bar, err))
+            if (!grid_barrier(bar, err, stall, A.stall_limit_ns))
                 return;
             for (uint32_t w = gtid; w < words; w += nthreads)
                 front_cur[w] = 0;
             added += level_count(A, i, fresh, lane);
-            if (!grid_barrier(bar, err))
+            if (!grid_barrier(bar, err, stall, A.stall_limit_ns))
                 return;
             continue;
         }
@@ -386,13 +393,13 @@ __global__ void __launch_bounds__(BLOCK, 5) bfs_kernel(BfsArgs A) {
                 }
             }
             added += level_count(A, i, fresh, lane);
-            if (!grid_barrier(bar, err))
+            if (!grid_barrier(bar, err, stall, A.stall_limit_ns))
                 return;
             continue;
         } else {
             fresh += frontier_pass<true, true, true>(A, front_cur, front_next, A.chunks, A.chunk_cap, chunk_cnt,
                                                      next_level, words, gwarp, nwarps, lane, slots);
-            if (!grid_barrier(bar, err))
+            if (!grid_barrier(bar, err, stall, A.stall_limit_ns))
                 return;
         }
         // Phase 2: long-row chunks, one warp per chunk (one step).
@@ -408,7 +415,7 @@ __global__ void __launch_bounds__(BLOCK, 5) bfs_kernel(BfsArgs A) {
             }
         }
         added += level_count(A, i, fresh, lane);
-        if (!grid_barrier(bar, err))
+        if (!grid_barrier(bar, err, stall, A.stall_limit_ns))
             return;
     }
     if (lane == 0 && added)
@@ -510,6 +517,8 @@ gpma_status bfs_plan(gpma_graph *g, uint32_t src, BfsPlan *P) {
     A.ctl = g->bfs_ctl;
     A.dense_div = g_tuning.bfs_dense_div;
     A.stamps = g->profiling ? reinterpret_cast<unsigned long long *>(g->bfs_ctl + CTL_WORDS) : nullptr;
+    A.stall = g_test_hooks.bfs_stall;
+    A.stall_limit_ns = g_test_hooks.bfs_stall ? g_test_hooks.wait_limit_ns : WAIT_LIMIT_NS;
     P->main.set((const void *)bfs_kernel, g->sms * blocks_per_sm(g->bfs_grid, g_tuning.bfs_blocks_per_sm), 0, &A,
                 sizeof(A));
     P->ctl_bytes = sizeof(uint32_t) * (CTL_WORDS + (g->profiling ? CTL_PROFILE_WORDS : 0));
@@ -622,6 +631,7 @@ gpma_status bfs_noalloc_run(gpma_graph *g, uint32_t src, uint32_t *levels, uint6
     GPMA_CUDA(cudaMemsetAsync(ctl, 0, sizeof(uint32_t) * CTL_WORDS, s));
     bfs_init_kernel<<<1, 1, 0, s>>>(levels, visited, front0, ctl, src);
     BfsArgs A;
+    memset(&A, 0, sizeof(A));
     A.keys = g->keys;
     A.vals = g->values;
     A.ro = g->row_offset;
@@ -632,15 +642,19 @@ gpma_status bfs_noalloc_run(gpma_graph *g, uint32_t src, uint32_t *levels, uint6
     A.front0 = front0;
     A.front1 = front1;
     A.chunks = chunks;
-    A.chunk_cap = NOALLOC_CHUNK_CAP;
+    A.chunk_cap = g_test_hooks.noalloc_chunk_cap ? std::min(g_test_hooks.noalloc_chunk_cap, NOALLOC_CHUNK_CAP)
+                                                 : NOALLOC_CHUNK_CAP;
     A.ctl = ctl;
     A.dense_div = g_tuning.bfs_dense_div;
     A.stamps = nullptr;
+    A.stall = g_test_hooks.bfs_stall;
+    A.stall_limit_ns = g_test_hooks.bfs_stall ? g_test_hooks.wait_limit_ns : WAIT_LIMIT_NS;
     void *params[] = {&A};
     GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)bfs_kernel, dim3(grid), dim3(BLOCK), params, 0, s));
     uint32_t h_ctl[CTL_WORDS];
     GPMA_CUDA(cudaMemcpyAsync(h_ctl, ctl, sizeof(h_ctl), cudaMemcpyDeviceToHost, s));
     GPMA_CUDA(cudaStreamSynchronize(s));
+    g_test_hooks.noalloc_overflows = h_ctl[CTL_OVERFLOW];
     if (h_ctl[CTL_ERR])
         return device_error("the BFS kernel", h_ctl[CTL_ERR]);
     if (reached)

@@ -938,6 +938,41 @@ gpma_status gpma_set_tuning(const gpma_tuning *t) {
     return GPMA_OK;
 }
 
+gpma_status gpma_get_test_hooks(gpma_test_hooks *out) {
+    if (!out) {
+        set_error("gpma_get_test_hooks: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    *out = gpma_test_hooks{};
+    out->update_stall = g_test_hooks.update_stall;
+    out->bfs_stall = g_test_hooks.bfs_stall;
+    out->wait_limit_us = g_test_hooks.wait_limit_ns == WAIT_LIMIT_NS ? 0u
+                                                                     : (uint32_t)(g_test_hooks.wait_limit_ns / 1000);
+    out->noalloc_chunk_cap = g_test_hooks.noalloc_chunk_cap;
+    out->noalloc_overflows = g_test_hooks.noalloc_overflows;
+    return GPMA_OK;
+}
+
+gpma_status gpma_set_test_hooks(const gpma_test_hooks *h) {
+    if (!h) {
+        set_error("gpma_set_test_hooks: null argument");
+        return GPMA_ERR_INVALID;
+    }
+    if (h->update_stall > 1 || h->bfs_stall > 1) {
+        set_error("gpma_set_test_hooks: stall flags are 0 or 1");
+        return GPMA_ERR_INVALID;
+    }
+    if (h->noalloc_chunk_cap > 65536) {
+        set_error("gpma_set_test_hooks: noalloc_chunk_cap above 65536");
+        return GPMA_ERR_INVALID;
+    }
+    g_test_hooks.update_stall = h->update_stall;
+    g_test_hooks.bfs_stall = h->bfs_stall;
+    g_test_hooks.wait_limit_ns = h->wait_limit_us ? 1000ull * h->wait_limit_us : WAIT_LIMIT_NS;
+    g_test_hooks.noalloc_chunk_cap = h->noalloc_chunk_cap;
+    return GPMA_OK;
+}
+
 gpma_status gpma_get_geometry(const gpma_graph *g, gpma_geometry *out) {
     if (!g || !out) {
         set_error("gpma_get_geometry: null argument");

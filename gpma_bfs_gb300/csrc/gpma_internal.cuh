@@ -71,6 +71,18 @@ enum BoundsSite : uint32_t {
 // Bounded waits give up after this long (ns of %globaltimer).
 constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;
 
+// Test hooks (process-wide, gpma_set_test_hooks): make one bounded wait run
+// out on purpose so its error path runs on a GPU without hanging it, and
+// shrink the no-allocation BFS's chunk list so its full-list branch runs.
+struct TestHooks {
+    uint32_t update_stall = 0;         // 1: the update kernel's first grid barrier waits for one arrival too many
+    uint32_t bfs_stall = 0;            // 1: the BFS kernel's first grid barrier does the same
+    uint64_t wait_limit_ns = WAIT_LIMIT_NS;  // limit of those two waits
+    uint32_t noalloc_chunk_cap = 0;    // gpma_bfs_noalloc chunk-list entries (0: all it has)
+    uint32_t noalloc_overflows = 0;    // full-list events of the last gpma_bfs_noalloc call (written by it)
+};
+extern TestHooks g_test_hooks;
+
 struct GridBarrier {
     unsigned int count;  // tickets taken (zero at the start of every launch)
     unsigned int gen;    // generation of grid_barrier_gen
@@ -511,13 +523,16 @@ __device__ __forceinline__ bool in_bounds(uint32_t *err, bool ok, uint32_t site)
 // count-then-generation barrier). Every wait is bounded: after WAIT_LIMIT_NS
 // the CTA records DERR_BARRIER_TIMEOUT and returns false; CTAs that see an
 // error stop waiting.
-__device__ __forceinline__ bool grid_barrier(GridBarrier *bar, uint32_t *err) {
+// `extra` (test hooks only, 0 otherwise) adds arrivals that never come, so the
+// wait runs out after `limit_ns`.
+__device__ __forceinline__ bool grid_barrier(GridBarrier *bar, uint32_t *err, uint32_t extra = 0,
+                                             uint64_t limit_ns = WAIT_LIMIT_NS) {
     __syncthreads();
     __shared__ uint32_t s_ok;
     if (threadIdx.x == 0) {
         __threadfence();
         const unsigned int ticket = atomicAdd(&bar->count, 1u);
-        const unsigned int target = (ticket / gridDim.x + 1) * gridDim.x;
+        const unsigned int target = (ticket / gridDim.x + 1) * gridDim.x + extra;
         uint64_t t0 = 0;
         unsigned ns = 16;
         for (;;) {
@@ -532,7 +547,7 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier *bar, uint32_t *err) {
             __nanosleep(ns);
             if (ns < 128)
                 ns <<= 1;
-            if (globaltimer_ns() - t0 > WAIT_LIMIT_NS) {
+            if (globaltimer_ns() - t0 > limit_ns) {
                 atomicCAS(err, 0u, DERR_BARRIER_TIMEOUT);
                 break;
             }

@@ -103,6 +103,9 @@ struct UpdateArgs {
     uint32_t next_slot_words;
     uint32_t hist_words;
     uint32_t status_words;
+    // test hooks: extra arrivals the first grid barrier waits for, and its limit
+    uint32_t stall;
+    uint64_t stall_limit_ns;
 };
 
 // Current window list of a level.
@@ -765,7 +768,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
     // S: stable radix sort of each graph's batch (gpma.cuh:977); digit passes
     // are separated by grid barriers, digits constant over all batches skipped.
     sort_histogram(A.bk[0], A.boff, A.G, A.sort_hist, st, A.check_keys, reinterpret_cast<uint32_t *>(smem));
-    if (!grid_barrier(&st->bar, &st->err))
+    if (!grid_barrier(&st->bar, &st->err, A.stall, A.stall_limit_ns))
         return;
     if (ld_volatile(&st->invalid_keys) != 0)
         return;  // reserved-column keys: reject the batch before any change
@@ -1671,6 +1674,7 @@ gpma_status count_bad_heads(gpma_graph *g, cudaStream_t s, uint64_t *bad) {
 }
 
 Tuning g_tuning;
+TestHooks g_test_hooks;
 
 int update_grid_size(int sms, uint64_t n) {
     int dev = 0;
@@ -1921,6 +1925,8 @@ gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t
     A.next_slot_words = (uint32_t)(buf.stat_slot / sizeof(uint32_t));
     A.hist_words = hist_rows * 2048;
     A.status_words = (uint32_t)status_words;
+    A.stall = g_test_hooks.update_stall;
+    A.stall_limit_ns = g_test_hooks.update_stall ? g_test_hooks.wait_limit_ns : WAIT_LIMIT_NS;
     L->set(update_kernel_ptr(update_variant(n)), grid, UPDATE_SMEM, &A, sizeof(A));
     return GPMA_OK;
 }

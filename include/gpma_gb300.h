@@ -107,8 +107,10 @@ GPMA_API gpma_status gpma_bfs_multi(gpma_graph *g, const uint32_t *srcs, uint32_
  * while serving). No counterpart in the reference. Same result as gpma_bfs,
  * but it allocates nothing: its working set (visited bitmap, two frontier
  * bitmaps, big-row chunk list, control words) is one fixed device array inside
- * the library, about 1.3 MB, held by every GPU that loads the library until
- * the process exits.
+ * the library, about 1.3 MB. A device commits it when the library's kernels are
+ * first used there (CUDA loads modules lazily by default) and holds it until
+ * the process exits. Rows that find the chunk list (65,536 entries) full are
+ * walked in place: slower, same result.
  * Limits: row_num <= 2,097,152 (GPMA_ERR_CAPACITY beyond); levels must be
  * device memory of row_num entries (GPMA_ERR_INVALID otherwise); reached is an
  * optional host pointer. The first call on a device looks up the array's
@@ -420,6 +422,32 @@ typedef struct gpma_tuning {
 } gpma_tuning;
 GPMA_API gpma_status gpma_get_tuning(gpma_tuning *out);
 GPMA_API gpma_status gpma_set_tuning(const gpma_tuning *t);
+
+/* ---- test hooks ---------------------------------------------------------------
+ * No reference counterpart. For tests of error paths that a correct run never
+ * takes. Every device-side wait of the library (grid barriers, the sort's
+ * look-back) gives up after a time limit and the call returns
+ * GPMA_ERR_TIMEOUT; a stall hook makes the first grid barrier of the next
+ * update (or BFS) launch wait for one arrival that never comes, with the
+ * limit wait_limit_us, so that path runs without hanging the GPU. The
+ * structure is unchanged by a stalled update (the barrier comes before any
+ * write to the array) and the next call clears the launch state the stalled
+ * one left. noalloc_chunk_cap shrinks the long-row chunk list of
+ * gpma_bfs_noalloc (results do not change: rows that find the list full are
+ * walked in place); noalloc_overflows reports how often the last
+ * gpma_bfs_noalloc call found it full (read-only). Process-wide; set them
+ * while no other host thread is inside a library call, and set all fields
+ * back to zero afterwards. */
+typedef struct gpma_test_hooks {
+    uint32_t update_stall;      /* 1: stall the next update launches' first grid barrier */
+    uint32_t bfs_stall;         /* 1: stall the next BFS launches' first grid barrier */
+    uint32_t wait_limit_us;     /* limit of a stalled wait (0: the library's 2 s) */
+    uint32_t noalloc_chunk_cap; /* gpma_bfs_noalloc chunk-list entries, 1..65536 (0: 65536) */
+    uint32_t noalloc_overflows; /* out: full-list events of the last gpma_bfs_noalloc call */
+    uint32_t reserved[3];
+} gpma_test_hooks;
+GPMA_API gpma_status gpma_get_test_hooks(gpma_test_hooks *out);
+GPMA_API gpma_status gpma_set_test_hooks(const gpma_test_hooks *h);
 
 /* ---- diagnostics ---------------------------------------------------------- */
 GPMA_API const char *gpma_status_string(gpma_status s);

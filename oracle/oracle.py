@@ -14,6 +14,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "libgpma_oracle.so"
+GRAPHGEN = HERE / "_build" / "libgraphgen.so"
 
 
 class _Stats(ctypes.Structure):
@@ -31,10 +32,29 @@ class _Gpma(ctypes.Structure):
 
 
 def build() -> Path:
-    src = [HERE / "gpma_oracle.c", HERE / "gpma_oracle.h", HERE / "Makefile"]
-    if not LIB.exists() or any(p.stat().st_mtime > LIB.stat().st_mtime for p in src):
+    src = [HERE / "gpma_oracle.c", HERE / "gpma_oracle.h", HERE / "Makefile",
+           HERE.parent / "gpma_bfs_gb300" / "csrc" / "graphgen.c"]
+    if not LIB.exists() or not GRAPHGEN.exists() or any(
+            p.stat().st_mtime > min(LIB.stat().st_mtime, GRAPHGEN.stat().st_mtime) for p in src if p.exists()):
         subprocess.run(["make", "-C", str(HERE), "oracle"], check=True, capture_output=True)
     return LIB
+
+
+def gen_chung_lu(n: int, m: int, exponent: float = 2.3, max_degree: int = 9000, seed: int = 2):
+    """The seeded Chung-Lu edge list of the benchmarks (same generator source
+    as the library, built on its own into oracle/_build/libgraphgen.so), so a
+    CPU baseline produces its input without loading the product library."""
+    build()
+    L = ctypes.CDLL(str(GRAPHGEN))
+    L.gpma_gen_chung_lu.restype = ctypes.c_int
+    L.gpma_gen_chung_lu.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_double, ctypes.c_uint32,
+                                    ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p]
+    src = np.empty(m, np.uint32)
+    dst = np.empty(m, np.uint32)
+    rc = L.gpma_gen_chung_lu(n, m, exponent, max_degree, seed, src.ctypes.data, dst.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"gpma_gen_chung_lu failed ({rc})")
+    return src, dst
 
 
 _lib = None

@@ -6,8 +6,9 @@ own GPMA<CPU> + update_gpma + CPU BFS (built from the reference sources by
 
     python tests/golden/make_golden.py [case ...]
 
-Needs the reference checkout (REF, default /root/reference); the fixtures it
-writes are committed, so the tests never need the reference.
+Needs oracle/_ref/ref_driver, built from a reference checkout with
+`make -C oracle ref REF=<checkout>`; the fixtures it writes are committed,
+so the tests never need the reference.
 """
 from __future__ import annotations
 

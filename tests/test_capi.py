@@ -164,3 +164,22 @@ def test_oracle_thresholds_follow_reference_formula():
     # initial structure: 4 slots, segment 2, height 1
     assert o.geometry() == {"size": 4, "segment_length": 2, "tree_height": 1, "row_num": 0}
     assert list(lo) == [1, 2] and list(hi) == [1, 2]
+
+
+def test_test_hooks_round_trip_and_reject_bad_values(built_lib):
+    """The error-path test hooks are plain host settings: checked on the host,
+    read back as set, and left at zero."""
+    import gpma_bfs_gb300 as G
+
+    assert G.get_test_hooks() == dict(update_stall=0, bfs_stall=0, wait_limit_us=0, noalloc_chunk_cap=0,
+                                      noalloc_overflows=0)
+    for bad in (dict(update_stall=2), dict(bfs_stall=3), dict(noalloc_chunk_cap=65537)):
+        with pytest.raises(G.GPMAError):
+            G.set_test_hooks(**bad)
+    old = G.set_test_hooks(update_stall=1, wait_limit_us=50_000, noalloc_chunk_cap=16)
+    try:
+        now = G.get_test_hooks()
+        assert (now["update_stall"], now["wait_limit_us"], now["noalloc_chunk_cap"]) == (1, 50_000, 16)
+    finally:
+        G.set_test_hooks(**old)
+    assert G.get_test_hooks()["update_stall"] == 0

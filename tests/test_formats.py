@@ -67,3 +67,14 @@ def test_snapshot_load_rejects_before_touching_the_gpu(built_lib, tmp_path, muta
     with pytest.raises(G.GPMAError) as e:
         G.load(p)
     assert e.value.status == 6  # GPMA_ERR_IO
+
+
+def test_oracle_side_generator_equals_the_library_generator(built_lib):
+    """The CPU baselines build the benchmark graphs from the same generator
+    source compiled on its own (oracle/_build/libgraphgen.so): same edges."""
+    import gpma_bfs_gb300 as G
+    from oracle.oracle import gen_chung_lu
+
+    a = gen_chung_lu(20000, 300000, 2.3, 3000, 41)
+    b = G.gen_chung_lu(20000, 300000, 2.3, 3000, 41)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])

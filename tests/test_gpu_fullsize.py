@@ -1,7 +1,16 @@
 """The social-network sliding window at full size (1,632,803 nodes,
 30,622,564 edges: the first half loaded in one bulk batch, then slides of
-153,112 inserts + 153,112 deletes), checked through properties that hold at
-any size, because the oracle does not finish at this size within a test:
+153,112 inserts + 153,112 deletes).
+
+test_social_sliding_window_matches_oracle runs the whole schedule -- bulk
+load, BFS from node 0, all 100 slides, BFS from node 0 -- through the CUDA
+path and the oracle side by side and compares, after the load and after
+every slide, the full key layout, the values (masked where the key is
+empty), row_offset, geometry and density thresholds, and both BFS level
+arrays and reach counts: bit-exact.
+
+test_social_sliding_window_full_size checks properties that hold at any
+size on the same configuration:
 
 * the live edge set equals the window's edges exactly;
 * layout invariants: live slots strictly ascending, row r's guard at
@@ -121,3 +130,52 @@ def test_social_sliding_window_full_size(built_lib):
     assert np.array_equal(_edges_of(g.compact_keys()), window)
     assert g.validate() == 0
     g.close()
+
+
+def test_social_sliding_window_matches_oracle(built_lib):
+    """Every step of the full social schedule, GPU against the oracle, bit for
+    bit (gpma_bfs_demo.cu:85-112: load, BFS, 100 slides, BFS)."""
+    import os
+
+    import gpma_bfs_gb300 as G
+    from gpma_bfs_gb300.workloads import make_graph, sliding_window
+    from oracle.oracle import OracleGPMA
+
+    n, src, dst = make_graph("social")
+    sw = sliding_window(src, dst, num_slide=100)
+    del src, dst
+    assert (n, sw.half, sw.step, sw.num_slide) == (1_632_803, 15_311_282, 153_112, 100)
+    g = G.GPMA(n)
+    o = OracleGPMA(n, threads=os.cpu_count() or 1)
+
+    def compare(ctx):
+        assert g.geometry() == o.geometry(), ctx + ": geometry"
+        glo, ghi = g.thresholds()
+        olo, ohi = o.thresholds()
+        assert np.array_equal(glo, olo) and np.array_equal(ghi, ohi), ctx + ": density thresholds"
+        gk, gv, gr = g.export_layout()
+        ok, ov, orow = o.export_layout()
+        assert np.array_equal(gk, ok), ctx + ": key layout"
+        assert np.array_equal(gv, ov), ctx + ": values"
+        assert np.array_equal(gr, orow), ctx + ": row_offset"
+
+    def bfs(ctx):
+        gl, gr = G.gpma_bfs(g, n, 0, 0)
+        ol, orr = o.bfs(0)
+        assert gr == orr and np.array_equal(gl, ol), ctx + ": BFS from node 0"
+        return gr
+
+    G.update_gpma(g, sw.load_keys, sw.load_values)
+    o.update(sw.load_keys, sw.load_values)
+    assert g.stats()["significant"] == 1  # >= 5M insertions: the bulk rebuild
+    compare("after the bulk load")
+    before = bfs("before the slides")
+    for i in range(sw.num_slide):
+        G.update_gpma(g, sw.slide_keys[i], sw.slide_values[i])
+        o.update(sw.slide_keys[i], sw.slide_values[i])
+        compare(f"slide {i}")
+    after = bfs("after the slides")
+    assert before > n // 2 and after > n // 2  # the giant component is reached
+    assert g.validate() == 0
+    g.close()
+    o.close()

@@ -108,6 +108,37 @@ def test_sliding_window_rmat14_step_by_step():
     gpu.close()
 
 
+def test_sliding_window_chung_lu_20k_every_slide():
+    """The social configuration's power-law shape (hub rows of thousands of
+    edges, deep windows) at 20,000 nodes and 300,000 edges: half-load, BFS
+    from node 0, 100 slides, BFS again; the full layout is compared after
+    every operation (the same graph the oracle is checked on against the
+    reference binary)."""
+    from gpma_bfs_gb300.workloads import make_graph, sliding_window
+
+    n, src, dst = make_graph(dict(kind="chung_lu", n=20000, m=300000, exponent=2.3, max_degree=3000, seed=41))
+    sw = sliding_window(src, dst, 100)
+    gpu, orc = GpuAdapter(n), OracleGPMA(n, threads=8)
+    gpu.update(sw.load_keys, sw.load_values)
+    orc.update(sw.load_keys, sw.load_values)
+    _compare_full(gpu, orc, "load")
+    assert gpu.thresholds()[0].tolist() == orc.thresholds()[0].tolist()
+    gl, gr = gpu.bfs(0)
+    ol, orr = orc.bfs(0)
+    assert gr == orr and np.array_equal(gl, ol), "bfs before the slides"
+    for i in range(sw.num_slide):
+        gpu.update(sw.slide_keys[i], sw.slide_values[i])
+        orc.update(sw.slide_keys[i], sw.slide_values[i])
+        _compare_full(gpu, orc, f"slide {i}")
+        glo, ghi = gpu.thresholds()
+        olo, ohi = orc.thresholds()
+        assert np.array_equal(glo, olo) and np.array_equal(ghi, ohi), f"slide {i}: thresholds"
+    gl, gr = gpu.bfs(0)
+    ol, orr = orc.bfs(0)
+    assert gr == orr and np.array_equal(gl, ol), "bfs after the slides"
+    gpu.close()
+
+
 def test_device_pointers_and_torch_tensors():
     import torch
 
