@@ -156,6 +156,7 @@ struct BatchBuffers {
     uint32_t *wlive = nullptr;
     uint64_t *rkeys = nullptr;  // insertions left for the root rebalance
     uint8_t *rvals = nullptr;
+    uint64_t *top = nullptr;    // one graph: its top-of-tree heads, gathered per launch for the locate cache
     // sort state
     uint32_t *sort_tiles = nullptr;    // 8 tile counters
     uint32_t *sort_status = nullptr;   // look-back words, 8 x tiles x 256

@@ -79,9 +79,15 @@ __device__ __forceinline__ void sort_histogram(const uint64_t *__restrict__ keys
 // Bit p set when digit p is the same for every key of every graph (that
 // pass is skipped); `total` is the all-graph histogram.
 __device__ __forceinline__ uint32_t sort_trivial_mask(const uint32_t *total, uint32_t n) {
-    uint32_t mask = 0;
+    // all eight loads in flight before the first CTA vote
+    uint32_t c[8];
+#pragma unroll
     for (int p = 0; p < 8; ++p)
-        if (__syncthreads_or(total[p * 256 + threadIdx.x] == n))
+        c[p] = total[p * 256 + threadIdx.x];
+    uint32_t mask = 0;
+#pragma unroll
+    for (int p = 0; p < 8; ++p)
+        if (__syncthreads_or(c[p] == n))
             mask |= 1u << p;
     return mask;
 }
