@@ -203,7 +203,8 @@ struct gpma_graph {
     uint32_t scratch_cap = 0;
     uint64_t *skeys = nullptr;        // scratch for wide windows and resizes
     uint8_t *svals = nullptr;
-    uint32_t *chunk_cnt = nullptr;    // scratch_cap / CHUNK + 2 entries (root rebuild)
+    uint32_t *chunk_cnt = nullptr;    // root rebuild: compaction statuses, then merge splits
+    uint64_t chunk_words = 0;         // its u32 words
     uint64_t *heads = nullptr;        // first key of every segment (size / seg entries), kept by every writer
     uint32_t heads_cap = 0;
     gpma::BatchBuffers buf;           // single-graph update buffers

@@ -1300,81 +1300,6 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
 
 // ---- whole-array kernels for the root resize and the bulk rebuild ----------
 
-// Per-chunk live counts of slots [0, size).
-__global__ void __launch_bounds__(BLOCK) chunk_live_kernel(const uint64_t *keys, const uint8_t *vals, uint32_t size,
-                                                           uint32_t *chunk_cnt) {
-    __shared__ uint32_t tmp[BLOCK / 32 + 1];
-    uint32_t chunks = (size + CHUNK - 1) / CHUNK;
-    for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {
-        uint32_t cl = 0;
-        for (uint32_t t = c * CHUNK + threadIdx.x; t < min(size, (c + 1) * CHUNK); t += BLOCK)
-            cl += (keys[t] != KEY_NONE && vals[t] != 0);
-        uint32_t s = block_sum(cl, tmp);
-        if (threadIdx.x == 0)
-            chunk_cnt[c] = s;
-    }
-}
-
-// Exclusive scan of chunk counts in one CTA; writes the total to *total.
-__global__ void __launch_bounds__(BLOCK) chunk_scan_kernel(uint32_t *chunk_cnt, uint32_t chunks, uint32_t *total) {
-    __shared__ uint32_t tmp[BLOCK / 32 + 1];
-    uint32_t run = 0;
-    for (uint32_t k0 = 0; k0 < chunks; k0 += BLOCK) {
-        uint32_t k = k0 + threadIdx.x;
-        uint32_t v = k < chunks ? chunk_cnt[k] : 0;
-        uint32_t tot;
-        uint32_t ex = block_excl_scan(v, &tot, tmp);
-        if (k < chunks)
-            chunk_cnt[k] = run + ex;
-        run += tot;
-    }
-    if (threadIdx.x == 0)
-        *total = run;
-}
-
-// Stable compaction of live slots into dst. Warp w of a chunk takes its 256
-// slots as 8 steps of 32 consecutive slots (coalesced loads); a ballot per
-// step gives each live slot its rank, so the writes are coalesced too.
-__global__ void __launch_bounds__(BLOCK) chunk_compact_kernel(const uint64_t *keys, const uint8_t *vals, uint32_t size,
-                                                              const uint32_t *chunk_off, uint64_t *dk, uint8_t *dv) {
-    __shared__ uint32_t s_warp[BLOCK / 32];
-    constexpr uint32_t STEPS = CHUNK / BLOCK;  // 8 steps of 32 slots per warp
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t chunks = (size + CHUNK - 1) / CHUNK;
-    for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) {
-        const uint32_t base = c * CHUNK + warp * (32 * STEPS);
-        uint64_t k[STEPS];
-        uint8_t v[STEPS];
-        uint32_t mask[STEPS];
-        uint32_t total = 0;
-#pragma unroll
-        for (uint32_t j = 0; j < STEPS; ++j) {
-            const uint32_t t = base + 32 * j + lane;
-            k[j] = t < size ? keys[t] : KEY_NONE;
-            v[j] = t < size ? vals[t] : 0;
-            mask[j] = __ballot_sync(0xFFFFFFFFu, k[j] != KEY_NONE && v[j] != 0);
-            total += __popc(mask[j]);
-        }
-        if (lane == 0)
-            s_warp[warp] = total;
-        __syncthreads();
-        uint32_t o = chunk_off[c];
-        for (uint32_t w = 0; w < warp; ++w)
-            o += s_warp[w];
-        __syncthreads();
-        const uint32_t lt = lanemask_lt();
-#pragma unroll
-        for (uint32_t j = 0; j < STEPS; ++j) {
-            if ((mask[j] >> lane) & 1u) {
-                const uint32_t pos = o + __popc(mask[j] & lt);
-                dk[pos] = k[j];
-                dv[pos] = v[j];
-            }
-            o += __popc(mask[j]);
-        }
-    }
-}
-
 // Live elements among the first d of the stable merge of live[0..L) and
 // pend[0..P) (ties: live first).
 __device__ __forceinline__ uint32_t merge_split(const uint64_t *lk, uint32_t L, const uint64_t *pk, uint32_t P,
@@ -1497,6 +1422,433 @@ __global__ void __launch_bounds__(BLOCK) rebuild_kernel(uint64_t *keys, uint8_t 
     }
 }
 
+// ---- bulk copies: global memory -> this CTA's own shared memory -----------
+// cp.async.bulk (TMA, no tensor map, no multicast) completing on an mbarrier
+// of the CTA. Copies start and end on 16-byte boundaries.
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits for phase `parity` of the barrier; false (and DERR_BARRIER_TIMEOUT in
+// *err) after WAIT_LIMIT_NS.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t *err) {
+    if (mbar_try_wait(bar, parity))
+        return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (;;) {
+        if (mbar_try_wait(bar, parity))
+            return true;
+        if (globaltimer_ns() - t0 > WAIT_LIMIT_NS) {
+            atomicCAS(err, 0u, DERR_BARRIER_TIMEOUT);
+            return false;
+        }
+    }
+}
+
+// One-pass stable compaction of the live slots of [0, size) into dk/dv
+// (resize_gpma, gpma.cuh:909-915): CHUNK-slot chunks, a decoupled look-back
+// over the chunks' live counts for each chunk's output offset. status[c]
+// (zeroed before the launch) holds chunk c's live count once it has loaded
+// its slots (CST_AGG) and its inclusive prefix once its look-back is done
+// (CST_INC); status[chunks] receives the total. CTAs take chunks b, b + grid,
+// ... in order in a cooperative launch (all resident), so a look-back waits
+// only on chunks already being processed; every wait gives up after
+// WAIT_LIMIT_NS (DERR_LOOKBACK_TIMEOUT in *err). Each chunk's slots arrive by
+// bulk copies into one of two stage buffers while the CTA compacts the
+// previous chunk, so the look-back's latency overlaps the next chunk's loads
+// (arrays under CHUNK slots are read directly). Replaces a count pass, a
+// single-CTA scan and a second read of the array.
+constexpr unsigned long long CST_AGG = 1ull << 62, CST_INC = 2ull << 62, CST_VAL = (1ull << 62) - 1;
+constexpr uint32_t CST_WINDOW = 4;  // predecessors a look-back step reads at once
+constexpr uint32_t CP_STAGE_BYTES = CHUNK * 9;
+constexpr size_t CP_SMEM = 2ull * CP_STAGE_BYTES + 2 * sizeof(uint64_t);
+
+// Thread 0: decoupled look-back for chunk c with T live slots; returns the
+// chunk's exclusive prefix and publishes its inclusive one.
+__device__ __forceinline__ unsigned long long compact_lookback(uint32_t c, uint32_t T, unsigned long long *status,
+                                                               uint32_t *err) {
+    unsigned long long prefix = 0;
+    if (c == 0) {
+        atomicExch(&status[0], CST_INC | T);
+        return 0;
+    }
+    atomicExch(&status[c], CST_AGG | T);
+    int64_t t = (int64_t)c - 1;
+    uint64_t t0 = 0;
+    unsigned ns = 32;
+    while (t >= 0) {
+        unsigned long long w[CST_WINDOW];
+#pragma unroll
+        for (uint32_t i = 0; i < CST_WINDOW; ++i)
+            w[i] = t - (int64_t)i >= 0 ? (unsigned long long)*(volatile unsigned long long *)&status[t - i]
+                                       : (unsigned long long)CST_INC;
+        uint32_t take = 0;
+        bool inc = false, blocked = false;
+#pragma unroll
+        for (uint32_t i = 0; i < CST_WINDOW; ++i) {
+            if (inc || blocked)
+                continue;
+            const unsigned long long flag = w[i] & ~CST_VAL;
+            if (flag == 0) {
+                blocked = true;
+                continue;
+            }
+            prefix += w[i] & CST_VAL;
+            ++take;
+            inc = flag == CST_INC;
+        }
+        if (inc)
+            break;
+        t -= take;
+        if (blocked) {
+            if (t0 == 0)
+                t0 = globaltimer_ns();
+            __nanosleep(ns);
+            if (ns < 256)
+                ns <<= 1;
+            if (globaltimer_ns() - t0 > WAIT_LIMIT_NS || ld_volatile(err) != 0) {
+                atomicCAS(err, 0u, DERR_LOOKBACK_TIMEOUT);
+                break;
+            }
+        }
+    }
+    atomicExch(&status[c], CST_INC | (prefix + T));
+    return prefix;
+}
+
+__global__ void __launch_bounds__(BLOCK, 4) compact_kernel(const uint64_t *keys, const uint8_t *vals, uint32_t size,
+                                                           uint64_t *dk, uint8_t *dv, unsigned long long *status,
+                                                           uint32_t *err) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + 2 * CP_STAGE_BYTES);
+    __shared__ uint32_t s_warp[BLOCK / 32];
+    __shared__ unsigned long long s_base;
+    constexpr uint32_t STEPS = CHUNK / BLOCK;  // 8 steps of 32 consecutive slots per warp
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t chunks = (size + CHUNK - 1) / CHUNK;
+    const bool staged = size >= CHUNK;  // whole chunks only: size is a power of two
+    if (threadIdx.x == 0 && staged) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    auto issue = [&](uint32_t c, uint32_t st) {
+        unsigned char *stage = smem + st * CP_STAGE_BYTES;
+        mbar_arrive_expect_tx(&bar[st], CP_STAGE_BYTES);
+        bulk_copy_g2s(stage, keys + (size_t)c * CHUNK, CHUNK * 8, &bar[st]);
+        bulk_copy_g2s(stage + CHUNK * 8, vals + (size_t)c * CHUNK, CHUNK, &bar[st]);
+    };
+    uint32_t phases = 0;   // bit st: parity of stage st's next phase
+    uint32_t pending = 0;  // thread 0: bit st set while stage st has copies outstanding
+    if (staged && threadIdx.x == 0 && blockIdx.x < chunks) {
+        issue(blockIdx.x, 0);
+        pending |= 1u;
+    }
+    bool stop = false;
+    uint32_t i = 0;
+    for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x, ++i) {
+        const uint32_t st = i & 1u;
+        uint64_t k[STEPS];
+        uint8_t v[STEPS];
+        if (staged) {
+            if (threadIdx.x == 0 && c + gridDim.x < chunks) {
+                issue(c + gridDim.x, st ^ 1u);
+                pending |= 2u >> st;  // bit st ^ 1
+            }
+            const bool landed = mbar_wait(&bar[st], (phases >> st) & 1u, err);
+            if (__syncthreads_or(!landed)) {
+                stop = true;
+                break;
+            }
+            phases ^= 1u << st;
+            pending &= ~(1u << st);
+            const uint64_t *sk = reinterpret_cast<const uint64_t *>(smem + st * CP_STAGE_BYTES);
+            const uint8_t *sv = smem + st * CP_STAGE_BYTES + CHUNK * 8;
+#pragma unroll
+            for (uint32_t j = 0; j < STEPS; ++j) {
+                const uint32_t t = warp * (32 * STEPS) + 32 * j + lane;
+                k[j] = sk[t];
+                v[j] = sv[t];
+            }
+        } else {
+            const uint32_t base = c * CHUNK + warp * (32 * STEPS);
+#pragma unroll
+            for (uint32_t j = 0; j < STEPS; ++j) {
+                const uint32_t t = base + 32 * j + lane;
+                k[j] = t < size ? keys[t] : KEY_NONE;
+                v[j] = t < size ? vals[t] : 0;
+            }
+        }
+        uint32_t mask[STEPS];
+        uint32_t total = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < STEPS; ++j) {
+            mask[j] = __ballot_sync(0xFFFFFFFFu, k[j] != KEY_NONE && v[j] != 0);
+            total += __popc(mask[j]);
+        }
+        if (lane == 0)
+            s_warp[warp] = total;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t T = 0;
+            for (uint32_t w = 0; w < BLOCK / 32; ++w) {
+                const uint32_t x = s_warp[w];
+                s_warp[w] = T;  // exclusive offsets of the warps
+                T += x;
+            }
+            const unsigned long long prefix = compact_lookback(c, T, status, err);
+            s_base = prefix;
+            if (c + 1 == chunks)
+                status[chunks] = prefix + T;
+        }
+        __syncthreads();
+        uint64_t o = s_base + s_warp[warp];
+        const uint32_t lt = lanemask_lt();
+#pragma unroll
+        for (uint32_t j = 0; j < STEPS; ++j) {
+            if ((mask[j] >> lane) & 1u) {
+                const uint64_t pos = o + __popc(mask[j] & lt);
+                dk[pos] = k[j];
+                dv[pos] = v[j];
+            }
+            o += __popc(mask[j]);
+        }
+        __syncthreads();  // s_warp, s_base and this stage are reused
+    }
+    // a stop can leave copies in flight: wait for them (bounded) before the
+    // CTA's shared memory is released
+    if (stop && threadIdx.x == 0) {
+        for (uint32_t st = 0; st < 2; ++st)
+            if ((pending >> st) & 1u)
+                mbar_wait(&bar[st], (phases >> st) & 1u, err);
+    }
+}
+
+// Redispatch of the whole array [0, size) (size a multiple of CHUNK, segments
+// of >= 8 slots) from live[0..L) and pend[0..P), as rebuild_kernel, with the
+// sources of each CHUNK-slot output chunk staged by bulk copies: chunk c's
+// live range [split[c], split[c + 1]) and its pending range, each widened to
+// 16-byte bounds (the arrays' allocations are multiples of 16 bytes, so the
+// widened ranges stay inside them), land in one of two stage buffers while
+// the CTA merges and writes the previous chunk; the chunk is written in slot
+// pairs with 16-byte key stores.
+constexpr uint32_t RB_KEY_BYTES = CHUNK * 8 + 64;   // a stage's live + pending keys, each widened
+constexpr uint32_t RB_VAL_BYTES = CHUNK + 128;      // a stage's live + pending values, each widened
+constexpr uint32_t RB_STAGE_BYTES = RB_KEY_BYTES + RB_VAL_BYTES;
+struct RbDesc {
+    uint32_t i_lo, nl, np;    // first merged element of the chunk, live and pending counts
+    uint32_t lk_off, pk_off;  // byte offsets of the first live / pending key in the stage
+    uint32_t lv_off, pv_off;  // byte offsets of the first live / pending value in the stage
+    uint32_t ok;              // 0: the chunk failed its bounds check and is skipped
+};
+constexpr size_t RB_SMEM = 2ull * RB_STAGE_BYTES + CHUNK * 9ull + 2 * sizeof(RbDesc) + 2 * sizeof(uint64_t) + 16;
+constexpr uint32_t RB_MIN_SLOTS = 1u << 16;  // smaller arrays take rebuild_kernel
+
+// Thread 0: chunk c's ranges, its descriptor and its copies into `stage`.
+__device__ __forceinline__ void rb_issue(uint32_t c, unsigned char *stage, RbDesc *d, uint64_t *bar,
+                                         const uint64_t *lk, const uint8_t *lv, uint32_t L, const uint64_t *pk,
+                                         const uint8_t *pv, uint32_t P, const uint32_t *split, uint32_t log2seg,
+                                         uint32_t log2F, uint32_t *err) {
+    const uint64_t M = (uint64_t)L + P;
+    const uint32_t t0 = c * CHUNK;
+    const uint64_t f_lo = seg_first(t0 >> log2seg, M, log2F), f_hi = seg_first((t0 + CHUNK) >> log2seg, M, log2F);
+    const uint32_t i_lo = (uint32_t)(f_lo < M ? f_lo : M), i_hi = (uint32_t)(f_hi < M ? f_hi : M);
+    const uint32_t x0 = split[c], x1 = split[c + 1];
+    const bool ok = in_bounds(err,
+                              x0 <= x1 && x1 <= L && x0 <= i_lo && x1 <= i_hi && i_lo - x0 <= i_hi - x1 &&
+                                  i_hi - x1 <= P && i_hi - i_lo <= CHUNK,
+                              BS_REBUILD);
+    uint32_t bytes = 0;
+    RbDesc r{};
+    r.ok = ok ? 1u : 0u;
+    if (ok) {
+        const uint32_t y0 = i_lo - x0, y1 = i_hi - x1;
+        r.i_lo = i_lo;
+        r.nl = x1 - x0;
+        r.np = y1 - y0;
+        // [lo, hi) byte ranges widened to 16-byte bounds
+        auto widen = [](const void *a, const void *b, uintptr_t &lo, uint32_t &len) {
+            lo = reinterpret_cast<uintptr_t>(a) & ~uintptr_t(15);
+            const uintptr_t hi = (reinterpret_cast<uintptr_t>(b) + 15) & ~uintptr_t(15);
+            len = (uint32_t)(hi - lo);
+        };
+        uintptr_t lo;
+        uint32_t len;
+        uint32_t kpos = 0, vpos = RB_KEY_BYTES;
+        if (r.nl) {
+            widen(lk + x0, lk + x1, lo, len);
+            r.lk_off = kpos + (uint32_t)(reinterpret_cast<uintptr_t>(lk + x0) - lo);
+            bulk_copy_g2s(stage + kpos, reinterpret_cast<const void *>(lo), len, bar);
+            kpos += len;
+            bytes += len;
+            widen(lv + x0, lv + x1, lo, len);
+            r.lv_off = vpos + (uint32_t)(reinterpret_cast<uintptr_t>(lv + x0) - lo);
+            bulk_copy_g2s(stage + vpos, reinterpret_cast<const void *>(lo), len, bar);
+            vpos += len;
+            bytes += len;
+        }
+        if (r.np) {
+            widen(pk + y0, pk + y1, lo, len);
+            r.pk_off = kpos + (uint32_t)(reinterpret_cast<uintptr_t>(pk + y0) - lo);
+            bulk_copy_g2s(stage + kpos, reinterpret_cast<const void *>(lo), len, bar);
+            bytes += len;
+            widen(pv + y0, pv + y1, lo, len);
+            r.pv_off = vpos + (uint32_t)(reinterpret_cast<uintptr_t>(pv + y0) - lo);
+            bulk_copy_g2s(stage + vpos, reinterpret_cast<const void *>(lo), len, bar);
+            bytes += len;
+        }
+    }
+    *d = r;
+    mbar_arrive_expect_tx(bar, bytes);  // the phase completes once the copies' bytes have landed
+}
+
+__global__ void __launch_bounds__(BLOCK, 4) rebuild_bulk_kernel(uint64_t *keys, uint8_t *vals, uint64_t *heads,
+                                                                uint32_t *row_offset, uint32_t row_num, uint32_t size,
+                                                                uint32_t log2seg, uint32_t log2F, const uint64_t *lk,
+                                                                const uint8_t *lv, uint32_t L, const uint64_t *pk,
+                                                                const uint8_t *pv, uint32_t P, const uint32_t *split,
+                                                                uint64_t gap_key, uint32_t *err) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    // stage st starts at smem + st * RB_STAGE_BYTES (computed, not indexed
+    // from an array, so nothing of the loop lives in local memory)
+    uint64_t *mk = reinterpret_cast<uint64_t *>(smem + 2 * RB_STAGE_BYTES);
+    uint8_t *mv = reinterpret_cast<uint8_t *>(mk + CHUNK);
+    RbDesc *desc = reinterpret_cast<RbDesc *>(mv + CHUNK);
+    uint64_t *bar = reinterpret_cast<uint64_t *>((reinterpret_cast<uintptr_t>(desc + 2) + 15) & ~uintptr_t(15));
+    const uint64_t M = (uint64_t)L + P;
+    const uint32_t seg = 1u << log2seg;
+    const uint32_t chunks = size / CHUNK;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    uint32_t pending = 0;  // thread 0: bit st set while stage st has copies outstanding
+    if (threadIdx.x == 0 && blockIdx.x < chunks) {
+        rb_issue(blockIdx.x, smem, &desc[0], &bar[0], lk, lv, L, pk, pv, P, split, log2seg, log2F, err);
+        pending = 1u;
+    }
+    uint32_t phases = 0;  // bit st: parity of stage st's next phase
+    uint32_t i = 0;
+    bool stop = false;
+    for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x, ++i) {
+        const uint32_t s = i & 1u;
+        unsigned char *stage = smem + s * RB_STAGE_BYTES;
+        // the next chunk's copies go to the other stage, read last iteration
+        if (threadIdx.x == 0 && c + gridDim.x < chunks) {
+            rb_issue(c + gridDim.x, smem + (s ^ 1u) * RB_STAGE_BYTES, &desc[s ^ 1u], &bar[s ^ 1u], lk, lv, L, pk, pv,
+                     P, split, log2seg, log2F, err);
+            pending |= 2u >> s;  // bit s ^ 1
+        }
+        const bool landed = mbar_wait(&bar[s], (phases >> s) & 1u, err);
+        if (__syncthreads_or(!landed)) {
+            stop = true;
+            break;
+        }
+        phases ^= 1u << s;
+        pending &= ~(1u << s);
+        const RbDesc d = desc[s];
+        if (!d.ok) {
+            // bounds-checked build: the chunk is skipped (the error is recorded)
+            __syncthreads();
+            continue;
+        }
+        const uint64_t *sl = reinterpret_cast<const uint64_t *>(stage + d.lk_off);
+        const uint64_t *sp = reinterpret_cast<const uint64_t *>(stage + d.pk_off);
+        const uint8_t *slv = stage + d.lv_off;
+        const uint8_t *spv = stage + d.pv_off;
+        const uint32_t nl = d.nl, np = d.np, cnt = nl + np;
+        const uint32_t ipt = (cnt + BLOCK - 1) / BLOCK;
+        const uint32_t e0 = threadIdx.x * ipt;
+        if (e0 < cnt) {
+            uint32_t lo = e0 > np ? e0 - np : 0, hi = min(e0, nl);
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (sp[e0 - mid - 1] < sl[mid])
+                    hi = mid;
+                else
+                    lo = mid + 1;
+            }
+            uint32_t x = lo, y = e0 - lo;
+            const uint32_t end = min(cnt, e0 + ipt);
+            for (uint32_t e = e0; e < end; ++e) {
+                const bool take_live = x < nl && (y >= np || sl[x] <= sp[y]);
+                if (take_live) {
+                    mk[e] = sl[x];
+                    mv[e] = slv[x];
+                    ++x;
+                } else {
+                    mk[e] = sp[y];
+                    mv[e] = spv[y];
+                    ++y;
+                }
+            }
+        }
+        __syncthreads();
+        // slot pairs: round r, thread t writes slots 2 (r * BLOCK + t) and the
+        // next one, so a warp's 16-byte key stores are contiguous (512 B) and
+        // its 2-byte value stores too; a pair never straddles a segment
+#pragma unroll
+        for (uint32_t r = 0; r < CHUNK / (2 * BLOCK); ++r) {
+            const uint32_t t = 2 * (r * BLOCK + threadIdx.x);
+            const uint32_t slot = c * CHUNK + t;
+            const uint32_t sg = slot >> log2seg, ln0 = slot & (seg - 1);
+            const uint64_t f0 = seg_first(sg, M, log2F), f1 = seg_first(sg + 1, M, log2F);
+            const uint32_t have = (uint32_t)(f1 - f0);
+            uint64_t k0 = gap_key, k1 = gap_key;
+            uint32_t v0 = 0, v1 = 0;
+            if (ln0 < have) {
+                const uint32_t e = (uint32_t)(f0 + ln0 - d.i_lo);
+                k0 = mk[e];
+                v0 = mv[e];
+            }
+            if (ln0 + 1 < have) {
+                const uint32_t e = (uint32_t)(f0 + ln0 + 1 - d.i_lo);
+                k1 = mk[e];
+                v1 = mv[e];
+            }
+            *reinterpret_cast<ulonglong2 *>(keys + slot) = make_ulonglong2(k0, k1);
+            *reinterpret_cast<uint16_t *>(vals + slot) = (uint16_t)(v0 | (v1 << 8));
+            if (ln0 == 0)
+                heads[sg] = k0;
+            if (is_guard(k0) && (uint32_t)(k0 >> 32) < row_num)
+                row_offset[(k0 >> 32) + 1] = slot;
+            if (is_guard(k1) && (uint32_t)(k1 >> 32) < row_num)
+                row_offset[(k1 >> 32) + 1] = slot + 1;
+        }
+        __syncthreads();  // mk/mv and this stage are reused
+    }
+    // a stop can leave copies in flight: wait for them (bounded) before the
+    // CTA's shared memory is released
+    if (stop && threadIdx.x == 0) {
+        for (uint32_t st = 0; st < 2; ++st)
+            if ((pending >> st) & 1u)
+                mbar_wait(&bar[st], (phases >> st) & 1u, err);
+    }
+}
+
 // keys[0..L) = live, keys[L..size) = KEY_NONE (values 0): the layout
 // resize_gpma leaves when the root rebalance that follows it is rejected.
 __global__ void compacted_layout_kernel(uint64_t *keys, uint8_t *vals, uint64_t *heads, uint32_t log2seg,
@@ -1535,19 +1887,37 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k
     const uint32_t size = g->geo.size;
     const uint32_t chunks = (size + CHUNK - 1) / CHUNK;
     prof_mark(g, 0, s);
-    g->prof.kernel_launches += 4;
-    // 1. stable compaction of the live slots (resize_gpma, gpma.cuh:909-915)
-    chunk_live_kernel<<<grid_for((uint64_t)chunks * BLOCK, g->sms, 8), BLOCK, 0, s>>>(g->keys, g->values, size,
-                                                                                       g->chunk_cnt);
-    uint32_t *d_total = g->chunk_cnt + chunks;
-    chunk_scan_kernel<<<1, BLOCK, 0, s>>>(g->chunk_cnt, chunks, d_total);
-    chunk_compact_kernel<<<grid_for((uint64_t)chunks * BLOCK, g->sms, 8), BLOCK, 0, s>>>(g->keys, g->values, size,
-                                                                                          g->chunk_cnt, g->skeys,
-                                                                                          g->svals);
-    GPMA_CUDA(cudaGetLastError());
-    uint32_t live = 0;
-    GPMA_CUDA(cudaMemcpyAsync(&live, d_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    g->prof.kernel_launches += 2;
+    // 1. stable compaction of the live slots (resize_gpma, gpma.cuh:909-915),
+    // one pass with a decoupled look-back; the chunk statuses, the total and
+    // the error word live in the graph's chunk buffer (u64 words)
+    unsigned long long *cst = reinterpret_cast<unsigned long long *>(g->chunk_cnt);
+    uint32_t *cerr = reinterpret_cast<uint32_t *>(cst + chunks + 1);
+    GPMA_CUDA(cudaMemsetAsync(cst, 0, sizeof(unsigned long long) * (chunks + 2), s));
+    {
+        int dev = 0;
+        GPMA_CUDA(cudaGetDevice(&dev));
+        static int fit[64] = {};
+        int &f = fit[dev >= 0 && dev < 64 ? dev : 0];
+        if (f == 0) {
+            GPMA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, compact_kernel, BLOCK, CP_SMEM));
+            f = std::max(1, std::min(f, MAX_BLOCKS_PER_SM));
+        }
+        const uint64_t *ck = g->keys;
+        const uint8_t *cv = g->values;
+        uint32_t csize = size;
+        uint64_t *dk = g->skeys;
+        uint8_t *dv = g->svals;
+        void *args[] = {&ck, &cv, &csize, &dk, &dv, &cst, &cerr};
+        const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(chunks, (uint64_t)g->sms * f));
+        GPMA_CUDA(cudaLaunchCooperativeKernel((const void *)compact_kernel, dim3(grid), dim3(BLOCK), args, CP_SMEM, s));
+    }
+    unsigned long long h_cst[2] = {0, 0};  // total, error word
+    GPMA_CUDA(cudaMemcpyAsync(h_cst, cst + chunks, sizeof(h_cst), cudaMemcpyDeviceToHost, s));
     GPMA_CUDA(cudaStreamSynchronize(s));
+    if ((uint32_t)h_cst[1])
+        return device_error("the compaction of the root rebuild", (uint32_t)h_cst[1]);
+    const uint32_t live = (uint32_t)h_cst[0];
     // 2. new geometry (gpma.cuh:917-930)
     uint64_t merge = (uint64_t)live + pend_n;
     uint64_t tree_size = 4;
@@ -1595,15 +1965,42 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k
     // merge splits at every chunk boundary of the new array: the chunk counts
     // of the compaction are spent, so their buffer holds them (grown if the
     // array grew)
-    if (out_chunks + 2 > g->scratch_cap / CHUNK + 2) {
+    if ((uint64_t)out_chunks + 2 > g->chunk_words) {
         dev_free(g->chunk_cnt);
-        GPMA_TRY(dev_alloc(&g->chunk_cnt, (uint64_t)out_chunks + 2));
+        g->chunk_words = 0;
+        GPMA_TRY(dev_alloc(&g->chunk_cnt, 2ull * (out_chunks + 2) + 4));
+        g->chunk_words = 2ull * (out_chunks + 2) + 4;
     }
     uint32_t *split = g->chunk_cnt;
-    // the bounds-checked build's error word of the rebuild (after the splits)
-    uint32_t *rebuild_err = GPMA_BOUNDS_CHECK ? g->chunk_cnt + out_chunks + 1 : nullptr;
-    if (rebuild_err)
-        GPMA_CUDA(cudaMemsetAsync(rebuild_err, 0, sizeof(uint32_t), s));
+    // the error word of the rebuild (after the splits): bounded waits, and
+    // the bounds-checked build's checks
+    uint32_t *rebuild_err = g->chunk_cnt + out_chunks + 1;
+    GPMA_CUDA(cudaMemsetAsync(rebuild_err, 0, sizeof(uint32_t), s));
+    // arrays of RB_MIN_SLOTS slots or more stage each chunk's sources by bulk
+    // copies (double-buffered); smaller ones take rebuild_kernel
+    auto rebuild = [&](uint64_t gap) -> gpma_status {
+        if (geo.size >= RB_MIN_SLOTS) {
+            static bool attr_set[64] = {};
+            int dev = 0;
+            GPMA_CUDA(cudaGetDevice(&dev));
+            if (!attr_set[dev >= 0 && dev < 64 ? dev : 0]) {
+                GPMA_CUDA(cudaFuncSetAttribute(rebuild_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)RB_SMEM));
+                attr_set[dev >= 0 && dev < 64 ? dev : 0] = true;
+            }
+            const int grid = (int)std::min<uint64_t>((uint64_t)out_chunks, (uint64_t)g->sms * 4);
+            rebuild_bulk_kernel<<<grid, BLOCK, RB_SMEM, s>>>(g->keys, g->values, g->heads, g->row_offset, g->row_num,
+                                                             geo.size, log2seg, log2F, g->skeys, g->svals, live,
+                                                             pend_k, pend_v, pend_n, split, gap, rebuild_err);
+        } else {
+            rebuild_kernel<<<rgrid, BLOCK, rsmem, s>>>(g->keys, g->values, g->heads, g->row_offset, g->row_num,
+                                                        geo.size, log2seg, log2F, g->skeys, g->svals, live, pend_k,
+                                                        pend_v, pend_n, split, gap, rebuild_err);
+        }
+        GPMA_CUDA(cudaGetLastError());
+        g->prof.kernel_launches += 1;
+        return GPMA_OK;
+    };
     auto splits = [&]() {
         merge_split_kernel<<<grid_for((uint64_t)out_chunks + 1, g->sms, 8), BLOCK, 0, s>>>(
             g->skeys, live, pend_k, pend_n, geo.size, log2seg, log2F, split);
@@ -1612,9 +2009,7 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k
     if (significant) {
         // significant_insert: everything redispatched, gaps are key 0 / value 0
         splits();
-        rebuild_kernel<<<rgrid, BLOCK, rsmem, s>>>(g->keys, g->values, g->heads, g->row_offset, g->row_num, geo.size,
-                                                    log2seg, log2F, g->skeys, g->svals, live, pend_k, pend_v, pend_n,
-                                                    split, 0ull, rebuild_err);
+        GPMA_TRY(rebuild(0ull));
         g->stats.significant++;
         g->stats.accepted_windows++;
         g->stats.accepted_slots += geo.size;
@@ -1622,9 +2017,7 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k
         const uint32_t h = geo.height;
         if (geo.lower[h] <= merge && merge <= geo.upper[h]) {
             splits();
-            rebuild_kernel<<<rgrid, BLOCK, rsmem, s>>>(g->keys, g->values, g->heads, g->row_offset, g->row_num,
-                                                        geo.size, log2seg, log2F, g->skeys, g->svals, live, pend_k,
-                                                        pend_v, pend_n, split, KEY_NONE, rebuild_err);
+            GPMA_TRY(rebuild(KEY_NONE));
             g->stats.accepted_windows++;
             g->stats.accepted_slots += geo.size;
         } else {
@@ -1640,7 +2033,7 @@ gpma_status root_rebuild(gpma_graph *g, bool significant, const uint64_t *pend_k
     prof_mark(g, 1, s);
     GPMA_CUDA(cudaStreamSynchronize(s));
     g->prof.rebuild_ms += prof_elapsed(g, 0, 1);
-    if (rebuild_err) {
+    {
         uint32_t e = 0;
         GPMA_CUDA(cudaMemcpy(&e, rebuild_err, sizeof(e), cudaMemcpyDeviceToHost));
         if (e)
@@ -1750,9 +2143,13 @@ gpma_status ensure_scratch(gpma_graph *g, uint32_t slots) {
     dev_free(g->svals);
     dev_free(g->chunk_cnt);
     g->scratch_cap = 0;
-    GPMA_TRY(dev_alloc(&g->skeys, slots));
-    GPMA_TRY(dev_alloc(&g->svals, slots));
-    GPMA_TRY(dev_alloc(&g->chunk_cnt, slots / CHUNK + 2));
+    // at least 64 slots: both arrays are whole 16-byte units (bulk copies of
+    // ranges widened to 16-byte bounds stay inside them)
+    GPMA_TRY(dev_alloc(&g->skeys, std::max<uint32_t>(slots, 64)));
+    GPMA_TRY(dev_alloc(&g->svals, std::max<uint32_t>(slots, 64)));
+    // u64 compaction statuses (chunks + 2), or u32 merge splits
+    g->chunk_words = 2ull * (slots / CHUNK + 2) + 4;
+    GPMA_TRY(dev_alloc(&g->chunk_cnt, g->chunk_words));
     g->scratch_cap = slots;
     return GPMA_OK;
 }
@@ -1808,7 +2205,9 @@ gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
     if (!b.top)
         GPMA_TRY(dev_alloc(&b.top, LOCATE_CACHE));
     if (n > b.cap || !b.bkeys[0]) {
-        uint64_t cap = std::max<uint64_t>(n, 1024);
+        // a multiple of 16 entries: every buffer is a whole number of 16-byte
+        // units, so a bulk copy of a range widened to 16-byte bounds stays inside
+        uint64_t cap = (std::max<uint64_t>(n, 1024) + 15) & ~uint64_t(15);
         for (int i = 0; i < 2; ++i) {
             dev_free(b.bkeys[i]);
             dev_free(b.bvals[i]);
