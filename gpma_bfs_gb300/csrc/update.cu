@@ -1479,60 +1479,64 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32
 // (arrays under CHUNK slots are read directly). Replaces a count pass, a
 // single-CTA scan and a second read of the array.
 constexpr unsigned long long CST_AGG = 1ull << 62, CST_INC = 2ull << 62, CST_VAL = (1ull << 62) - 1;
-constexpr uint32_t CST_WINDOW = 4;  // predecessors a look-back step reads at once
 constexpr uint32_t CP_STAGE_BYTES = CHUNK * 9;
 constexpr size_t CP_SMEM = 2ull * CP_STAGE_BYTES + 2 * sizeof(uint64_t);
 
-// Thread 0: decoupled look-back for chunk c with T live slots; returns the
-// chunk's exclusive prefix and publishes its inclusive one.
+// Warp 0: decoupled look-back for chunk c with T live slots; returns the
+// chunk's exclusive prefix (in every lane) and publishes its inclusive one.
+// Each step reads 32 predecessors at once (lane l reads chunk t - l): the
+// chunks of one wave of CTAs publish their counts together, and a look-back
+// that read them a few at a time would walk a whole wave one L2 round trip
+// per few chunks.
 __device__ __forceinline__ unsigned long long compact_lookback(uint32_t c, uint32_t T, unsigned long long *status,
-                                                               uint32_t *err) {
-    unsigned long long prefix = 0;
+                                                               uint32_t *err, uint32_t lane) {
     if (c == 0) {
-        atomicExch(&status[0], CST_INC | T);
+        if (lane == 0)
+            atomicExch(&status[0], CST_INC | T);
         return 0;
     }
-    atomicExch(&status[c], CST_AGG | T);
+    if (lane == 0)
+        atomicExch(&status[c], CST_AGG | T);
+    unsigned long long prefix = 0;
     int64_t t = (int64_t)c - 1;
     uint64_t t0 = 0;
     unsigned ns = 32;
     while (t >= 0) {
-        unsigned long long w[CST_WINDOW];
+        const int64_t idx = t - (int64_t)lane;
+        // chunks before the first count as inclusive zeros
+        const unsigned long long w =
+            idx >= 0 ? (unsigned long long)*(volatile unsigned long long *)&status[idx] : (unsigned long long)CST_INC;
+        const unsigned long long flag = w & ~CST_VAL;
+        const uint32_t blocked = __ballot_sync(0xFFFFFFFFu, flag == 0);
+        const uint32_t inc = __ballot_sync(0xFFFFFFFFu, flag == CST_INC);
+        const uint32_t fb = blocked ? (uint32_t)__ffs(blocked) - 1 : 32u;
+        const uint32_t fi = inc ? (uint32_t)__ffs(inc) - 1 : 32u;
+        const uint32_t take = fi < fb ? fi + 1 : fb;  // lanes summed this step
+        unsigned long long v = lane < take ? (w & CST_VAL) : 0ull;
 #pragma unroll
-        for (uint32_t i = 0; i < CST_WINDOW; ++i)
-            w[i] = t - (int64_t)i >= 0 ? (unsigned long long)*(volatile unsigned long long *)&status[t - i]
-                                       : (unsigned long long)CST_INC;
-        uint32_t take = 0;
-        bool inc = false, blocked = false;
-#pragma unroll
-        for (uint32_t i = 0; i < CST_WINDOW; ++i) {
-            if (inc || blocked)
-                continue;
-            const unsigned long long flag = w[i] & ~CST_VAL;
-            if (flag == 0) {
-                blocked = true;
-                continue;
-            }
-            prefix += w[i] & CST_VAL;
-            ++take;
-            inc = flag == CST_INC;
-        }
-        if (inc)
+        for (int d = 16; d >= 1; d >>= 1)
+            v += __shfl_xor_sync(0xFFFFFFFFu, v, d);
+        prefix += v;
+        if (fi < fb)
             break;
         t -= take;
-        if (blocked) {
+        if (take == 0) {
+            // the nearest predecessor has not published yet
             if (t0 == 0)
                 t0 = globaltimer_ns();
             __nanosleep(ns);
             if (ns < 256)
                 ns <<= 1;
-            if (globaltimer_ns() - t0 > WAIT_LIMIT_NS || ld_volatile(err) != 0) {
-                atomicCAS(err, 0u, DERR_LOOKBACK_TIMEOUT);
+            const bool give_up = globaltimer_ns() - t0 > WAIT_LIMIT_NS || ld_volatile(err) != 0;
+            if (__any_sync(0xFFFFFFFFu, give_up)) {
+                if (lane == 0)
+                    atomicCAS(err, 0u, DERR_LOOKBACK_TIMEOUT);
                 break;
             }
         }
     }
-    atomicExch(&status[c], CST_INC | (prefix + T));
+    if (lane == 0)
+        atomicExch(&status[c], CST_INC | (prefix + T));
     return prefix;
 }
 
@@ -1610,17 +1614,20 @@ __global__ void __launch_bounds__(BLOCK, 4) compact_kernel(const uint64_t *keys,
         if (lane == 0)
             s_warp[warp] = total;
         __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t T = 0;
-            for (uint32_t w = 0; w < BLOCK / 32; ++w) {
-                const uint32_t x = s_warp[w];
-                s_warp[w] = T;  // exclusive offsets of the warps
-                T += x;
+        if (warp == 0) {
+            // exclusive offsets of the warps, then the chunk's look-back
+            const uint32_t x = lane < BLOCK / 32 ? s_warp[lane] : 0u;
+            const uint32_t inc_x = warp_incl_scan(x);
+            const uint32_t T = __shfl_sync(0xFFFFFFFFu, inc_x, 31);
+            __syncwarp();
+            if (lane < BLOCK / 32)
+                s_warp[lane] = inc_x - x;
+            const unsigned long long prefix = compact_lookback(c, T, status, err, lane);
+            if (lane == 0) {
+                s_base = prefix;
+                if (c + 1 == chunks)
+                    status[chunks] = prefix + T;
             }
-            const unsigned long long prefix = compact_lookback(c, T, status, err);
-            s_base = prefix;
-            if (c + 1 == chunks)
-                status[chunks] = prefix + T;
         }
         __syncthreads();
         uint64_t o = s_base + s_warp[warp];
