@@ -900,6 +900,69 @@ def run_sweep(args, sizes=SWEEP_SIZES, ratios=SWEEP_RATIOS, reps=None, bfs_sourc
     }
 
 
+def run_profile_case(args):
+    """Small cases for ncu captures (one JSON line each, not a bench line):
+    `bulk`: R-MAT scale --profile-scale (edge factor 32) loaded in 64M-key
+    batches, then one batch of 10M fresh inserts (the >= 5M bulk rebuild);
+    `batched`: the batched configuration's 256 graphs loaded, then four
+    packed sliding-window steps."""
+    import torch
+
+    import gpma_bfs_gb300 as G
+    from gpma_bfs_gb300.workloads import SlidingStream, batched_graphs
+
+    torch.cuda.set_device(0)
+    out = {"case": args.profile_case}
+    if args.profile_case == "bulk":
+        src, dst = G.gen_rmat(args.profile_scale, 32, seed=3)
+        keys = G.edges_to_keys(src, dst)
+        del src, dst
+        fresh, loaded = keys[len(keys) - 10_000_000:], keys[: len(keys) - 10_000_000]
+        g = G.GPMA(1 << args.profile_scale)
+        for i in range(0, len(loaded), 1 << 26):
+            part = torch.from_numpy(loaded[i:i + (1 << 26)].view(np.int64)).cuda()
+            G.update_gpma(g, part, torch.ones(len(part), dtype=torch.uint8, device="cuda"))
+        dk = torch.from_numpy(fresh.view(np.int64)).cuda()
+        dv = torch.ones(len(fresh), dtype=torch.uint8, device="cuda")
+        g.set_profiling(True)
+        g.reset_profile()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        G.update_gpma(g, dk, dv)
+        b.record()
+        torch.cuda.synchronize()
+        p = g.profile()
+        out.update(loaded=len(loaded), geometry=g.geometry(), batch_ms=a.elapsed_time(b),
+                   update_kernel_ms=p["update_kernel_ms"], rebuild_ms=p["rebuild_ms"])
+        g.close()
+    else:
+        specs = batched_graphs(256, seed=4)
+        graphs = [G.GPMA(nn) for nn, _ in specs]
+        streams = [SlidingStream(kk) for _, kk in specs]
+        b = G.Batch()
+        loads = [s.load() for s in streams]
+        off = np.concatenate([[0], np.cumsum([len(x[0]) for x in loads])]).astype(np.uint64)
+        b.update_packed(graphs, np.concatenate([x[0] for x in loads]), np.concatenate([x[1] for x in loads]), off)
+        rng = np.random.default_rng(44)
+        b.set_profiling(True)
+        steps = []
+        for _ in range(4):
+            sizes = np.exp(rng.uniform(np.log(100), np.log(200_000), len(specs))).astype(np.int64)
+            parts = [s.step(int(z)) for s, z in zip(streams, sizes)]
+            o = np.concatenate([[0], np.cumsum([len(q[0]) for q in parts])]).astype(np.uint64)
+            dk = torch.from_numpy(np.concatenate([q[0] for q in parts]).view(np.int64)).cuda()
+            dv = torch.from_numpy(np.concatenate([q[1] for q in parts])).cuda()
+            b.reset_profile()
+            b.update_packed(graphs, dk, dv, o)
+            steps.append({"keys": int(o[-1]), **{k: v for k, v in b.profile().items() if k.endswith("_ms")}})
+        out["steps"] = steps
+        b.close()
+        for x in graphs:
+            x.close()
+    print(json.dumps(out), flush=True)
+
+
 def cpu_baseline(n, keys, half, slide, steps):
     """The oracle restatement on all host cores: load untimed, `steps` slides timed."""
     from oracle.oracle import OracleGPMA, build
@@ -999,12 +1062,17 @@ def main():
     ap.add_argument("--no-large-graph", dest="large_graph", action="store_false",
                     help="skip the large-graph subset (R-MAT scale 24: 100k/1M/10M batches at 1:1, BFS) of the "
                          "default run")
+    ap.add_argument("--profile-case", choices=["bulk", "batched"],
+                    help="only a small case for ncu captures (its own JSON line, not a bench line)")
+    ap.add_argument("--profile-scale", type=int, default=21, help="R-MAT scale of the bulk profile case")
     ap.add_argument("--report", default=str(ROOT / "bench_report.json"),
                     help="file for the full sub-reports ('' for none)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
-    if args.sweep:
+    if args.profile_case:
+        run_profile_case(args)
+    elif args.sweep:
         import torch
 
         torch.cuda.set_device(0)

@@ -146,6 +146,8 @@ struct BatchBuffers {
     uint32_t *leaf = nullptr;
     uint64_t *ikeys[2] = {nullptr, nullptr};  // pending insertions, compacted per level (ping-pong)
     uint8_t *ivals[2] = {nullptr, nullptr};
+    uint64_t *rkeys = nullptr;  // insertions left for the root rebalance
+    uint8_t *rvals = nullptr;
     uint32_t *ileaf = nullptr;
     uint32_t *igraph = nullptr;
     uint32_t *wnode[2] = {nullptr, nullptr};
@@ -154,8 +156,6 @@ struct BatchBuffers {
     uint32_t *wb[2] = {nullptr, nullptr};
     uint32_t *wflag = nullptr;
     uint32_t *wlive = nullptr;
-    uint64_t *rkeys = nullptr;  // insertions left for the root rebalance
-    uint8_t *rvals = nullptr;
     uint64_t *top = nullptr;    // one graph: its top-of-tree heads, gathered per launch for the locate cache
     // sort state
     uint32_t *sort_tiles = nullptr;    // 8 tile counters

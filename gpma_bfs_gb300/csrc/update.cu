@@ -86,14 +86,14 @@ struct UpdateArgs {
     uint8_t *ivals[2];
     uint32_t *ileaf;
     uint32_t *igraph;
+    uint64_t *rkeys;
+    uint8_t *rvals;
     uint32_t *wnode[2];
     uint32_t *wgraph[2];
     uint32_t *wa[2];
     uint32_t *wb[2];
     uint32_t *wflag;
     uint32_t *wlive;
-    uint64_t *rkeys;
-    uint8_t *rvals;
     uint32_t *chunk_cnt;
     uint32_t *cta_cnt;
     DeviceStatus *st;
@@ -1172,11 +1172,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         }
         // GROUP_ITEMS consecutive windows per thread per round; the rejected
         // windows' copy plan goes to a compact list in shared memory (free
-        // again once the level's windows are written), one warp per entry
+        // again once the level's windows are written): source, destination
+        // (the next level's buffer, or the remaining buffer for a root
+        // window) and the exclusive prefix of the counts, so the whole CTA
+        // copies the concatenated ranges (a window of a million insertions is
+        // not left to one warp)
         uint32_t *l_src = reinterpret_cast<uint32_t *>(smem);
-        uint32_t *l_cnt = l_src + GROUP_ITEMS * BLOCK;
-        uint32_t *l_to = l_cnt + GROUP_ITEMS * BLOCK;
-        uint32_t *l_dst = l_to + GROUP_ITEMS * BLOCK;
+        uint32_t *l_pre = l_src + GROUP_ITEMS * BLOCK + 1;
+        uint32_t *l_to = l_pre + GROUP_ITEMS * BLOCK + 1;  // destination offset | root << 31
         for (uint32_t r0 = lo; r0 < hi; r0 += GROUP_ITEMS * BLOCK) {
             const uint32_t w0 = r0 + GROUP_ITEMS * threadIdx.x;
             // windows w0 - 1 .. w0 + GROUP_ITEMS: each needs both neighbours
@@ -1192,7 +1195,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
                 wa[q] = ok ? L.a[j] : 0u;
                 wb[q] = ok ? L.b[j] : 0u;
             }
-            uint32_t csum = 0, hsum = 0, rsum = 0;
+            uint32_t csum = 0, hsum = 0, rsum = 0, asum = 0;
 #pragma unroll
             for (uint32_t q = 0; q < GROUP_ITEMS; ++q) {
                 const uint32_t j = w0 + q;
@@ -1201,6 +1204,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
                     continue;
                 const GraphDesc &Dg = A.gd[gg[q + 1]];
                 ++rsum;
+                asum += wb[q + 1] - wa[q + 1];
                 if (level >= Dg.height)
                     continue;  // root window
                 csum += wb[q + 1] - wa[q + 1];
@@ -1208,10 +1212,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
                 const bool merged = j > 0 && !fl[q] && gg[q] == gg[q + 1] && (nd[q] & ~W) == (nd[q + 1] & ~W);
                 hsum += merged ? 0u : 1u;
             }
-            uint32_t tot_i, tot_h, tot_r;
+            uint32_t tot_i, tot_h, tot_r, tot_a;
             uint32_t nb = base_i + block_excl_scan(csum, &tot_i, tmp);
             uint32_t e = base + block_excl_scan(hsum, &tot_h, tmp);
             uint32_t li = block_excl_scan(rsum, &tot_r, tmp);
+            uint32_t pre = block_excl_scan(asum, &tot_a, tmp);
 #pragma unroll
             for (uint32_t q = 0; q < GROUP_ITEMS; ++q) {
                 const uint32_t j = w0 + q;
@@ -1221,15 +1226,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
                 const uint32_t g = gg[q + 1];
                 const GraphDesc &Dg = A.gd[g];
                 const uint32_t c = wb[q + 1] - wa[q + 1];
-                const bool root = level >= Dg.height;
                 l_src[li] = wa[q + 1];
-                l_cnt[li] = c;
-                l_dst[li] = root ? 1u : 0u;
-                if (root) {
+                l_pre[li] = pre;
+                pre += c;
+                if (level >= Dg.height) {
                     // the root rebalance takes these: the graph's area of the
                     // remaining-insertion buffer, at its first insertion
                     A.gs[g].remaining = c;
-                    l_to[li] = A.gs[g].ins_base;
+                    l_to[li] = A.gs[g].ins_base | 0x80000000u;
                     ++li;
                     continue;
                 }
@@ -1249,15 +1253,24 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
                 nb += c;
             }
             __syncthreads();
-            // copy the kept insertions, one warp per rejected window
-            for (uint32_t t = threadIdx.x >> 5; t < tot_r; t += BLOCK / 32) {
-                const uint32_t cc = l_cnt[t], from = l_src[t], to = l_to[t];
-                uint64_t *dk = l_dst[t] ? A.rkeys : nk;
-                uint8_t *dv = l_dst[t] ? A.rvals : nv;
-                for (uint32_t x = threadIdx.x & 31; x < cc; x += 32) {
-                    dk[to + x] = pk[from + x];
-                    dv[to + x] = pv[from + x];
+            // copy the kept insertions: position p of the round's
+            // concatenation (p < tot_a) is element p - l_pre[t] of entry t,
+            // the last entry with l_pre <= p
+            for (uint32_t p = threadIdx.x; p < tot_a; p += BLOCK) {
+                uint32_t lo2 = 0, hi2 = tot_r;  // answer in [0, tot_r)
+                while (hi2 - lo2 > 1) {
+                    const uint32_t mid = (lo2 + hi2) >> 1;
+                    if (l_pre[mid] <= p)
+                        lo2 = mid;
+                    else
+                        hi2 = mid;
                 }
+                const uint32_t k = p - l_pre[lo2], to = l_to[lo2];
+                const uint32_t from = l_src[lo2] + k;
+                uint64_t *dk = (to >> 31) ? A.rkeys : nk;
+                uint8_t *dv = (to >> 31) ? A.rvals : nv;
+                dk[(to & 0x7FFFFFFFu) + k] = pk[from];
+                dv[(to & 0x7FFFFFFFu) + k] = pv[from];
             }
             __syncthreads();
             base += tot_h;
@@ -2173,12 +2186,12 @@ void free_buffers(BatchBuffers &b) {
         dev_free(b.wb[i]);
     }
     dev_free(b.leaf);
+    dev_free(b.rkeys);
+    dev_free(b.rvals);
     dev_free(b.ileaf);
     dev_free(b.igraph);
     dev_free(b.wflag);
     dev_free(b.wlive);
-    dev_free(b.rkeys);
-    dev_free(b.rvals);
     dev_free(b.sort_tiles);
     dev_free(b.top);
     dev_free(b.sort_status);
@@ -2226,12 +2239,12 @@ gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
             dev_free(b.wb[i]);
         }
         dev_free(b.leaf);
+        dev_free(b.rkeys);
+        dev_free(b.rvals);
         dev_free(b.ileaf);
         dev_free(b.igraph);
         dev_free(b.wflag);
         dev_free(b.wlive);
-        dev_free(b.rkeys);
-        dev_free(b.rvals);
         b.cap = 0;
         for (int i = 0; i < 2; ++i) {
             GPMA_TRY(dev_alloc(&b.bkeys[i], cap));
@@ -2244,12 +2257,12 @@ gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
             GPMA_TRY(dev_alloc(&b.wb[i], cap));
         }
         GPMA_TRY(dev_alloc(&b.leaf, cap));
+        GPMA_TRY(dev_alloc(&b.rkeys, cap));
+        GPMA_TRY(dev_alloc(&b.rvals, cap));
         GPMA_TRY(dev_alloc(&b.ileaf, cap));
         GPMA_TRY(dev_alloc(&b.igraph, cap));
         GPMA_TRY(dev_alloc(&b.wflag, cap));
         GPMA_TRY(dev_alloc(&b.wlive, cap));
-        GPMA_TRY(dev_alloc(&b.rkeys, cap));
-        GPMA_TRY(dev_alloc(&b.rvals, cap));
         b.cap = cap;
     }
     if (graphs > b.gcap || !b.d_tab) {
@@ -2288,6 +2301,11 @@ gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t
                         bool check_keys, size_t *tab_bytes, KernelLaunch *L) {
     static_assert(sizeof(UpdateArgs) <= KernelLaunch::ARG_BYTES, "update arguments exceed the launch record");
     const uint64_t n = off[k];
+    if (n >= (1ull << 31)) {
+        // insertion offsets carry a flag in bit 31 in the level loop's copy plan
+        set_error("update launch of %llu keys: at most 2^31 - 1 keys per launch", (unsigned long long)n);
+        return GPMA_ERR_CAPACITY;
+    }
     const int grid = update_grid_size(sms, n);
     if (grid == 0) {
         set_error("update kernel cannot be resident");
@@ -2370,12 +2388,12 @@ gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t
     A.sort_status = buf.sort_status;
     A.check_keys = check_keys;
     A.leaf = buf.leaf;
+    A.rkeys = buf.rkeys;
+    A.rvals = buf.rvals;
     A.ileaf = buf.ileaf;
     A.igraph = buf.igraph;
     A.wflag = buf.wflag;
     A.wlive = buf.wlive;
-    A.rkeys = buf.rkeys;
-    A.rvals = buf.rvals;
     A.chunk_cnt = buf.chunk_cnt;
     A.cta_cnt = buf.cta_cnt;
     A.st = reinterpret_cast<DeviceStatus *>(slot);
