@@ -399,7 +399,8 @@ def run_gpu(args):
 
             line["served"] = {
                 "graphs": served["graphs"], "requests": served["requests"], "failed": served["failed"],
-                "identical_results": served["identical_results"],
+                "identical_results": served["identical_results"], "lanes": served["lanes"],
+                "max_inflight_rounds": served["server_stats"]["max_inflight_rounds"],
                 "light_load": {"rate_per_s": light["rate_per_s"], "served": lat(light, "served"),
                                "plain": lat(light, "plain")},
                 "saturation": {"rate_per_s": sat["rate_per_s"], "speedup_sustained": sat["speedup_sustained"],
@@ -677,14 +678,17 @@ def run_batched(args, stream):
 def run_served(args, stream):
     """Served configuration: 32 R-MAT graphs drawn as in the batched one plus
     two R-MAT graphs of scale 22 (edge factor 16), first halves resident;
-    Poisson arrivals over `served_seconds` simulated seconds, 70% update
-    batches (log-uniform 1k-1M keys, sliding window, 1:1 insert:delete) and 30%
-    BFS queries (1-64 sources from nodes with out-edges), each on a uniformly
-    drawn graph; HBM admission budget 120 GB. The server runs continuous
-    batching in virtual time (the clock advances by each round's measured wall
-    time). The plain drop-in serves the same trace one request at a time
-    (gpma_update / gpma_bfs_multi per request, FIFO) on its own copy of the
-    graphs. Latency = completion - arrival."""
+    Poisson arrivals, 70% update batches (log-uniform 1k-1M keys, sliding
+    window, 1:1 insert:delete) and 30% BFS queries (1-64 sources from nodes
+    with out-edges), each on a uniformly drawn graph; HBM admission budget
+    120 GB. The server runs its native serving loop in real time with
+    `served_lanes` rounds in flight (continuous batching: a round starts as
+    soon as a request has arrived and a lane is free); the trace's arrivals
+    are seconds on the server's clock. The plain drop-in serves the same trace
+    one request at a time (gpma_update / gpma_bfs_multi per request, FIFO) on
+    its own copy of the graphs, each request starting at max(its arrival, the
+    previous one's completion) and taking its measured wall time.
+    Latency = completion - arrival."""
     import torch
 
     import gpma_bfs_gb300 as G
@@ -704,7 +708,8 @@ def run_served(args, stream):
     trace = S.make_trace(specs, phases, seed=5)
 
     # ---- served form ----------------------------------------------------------
-    srv = G.Server(hbm_budget_bytes=120 << 30, max_round_keys=1 << 24, stream=stream)
+    srv = G.Server(hbm_budget_bytes=120 << 30, max_round_keys=1 << 24, max_queued_keys=1 << 40, stream=stream,
+                   lanes=args.served_lanes, input_ring_bytes=4 << 30)
     gids = [srv.add_graph(nn, len(kk)) for nn, kk in specs]
     streams = [SlidingStream(kk) for _, kk in specs]
     t0 = time.time()
@@ -713,10 +718,11 @@ def run_served(args, stream):
     torch.cuda.synchronize()
     load_s = time.time() - t0
     w0 = time.perf_counter()
-    out = S.replay_served(srv, gids, streams, trace)
+    out = S.replay_served_live(srv, gids, streams, trace)
     served_wall = time.perf_counter() - w0
     layouts_s = [srv.graph(gid).export_layout()[0] for gid in gids]
     committed = srv.committed_bytes()
+    stats = out["stats"]
     srv.close()
     del streams
 
@@ -731,36 +737,24 @@ def run_served(args, stream):
         g.close()
 
     # per phase: sustained rates over the phase's makespan, latency per type
-    rounds = out["rounds"]
-    rphase = [int(trace.phase[r["requests"][0]]) for r in rounds]
     res = []
     for p, (rate, seconds) in enumerate(phases):
         sel = trace.phase == p
         upd = sel & (trace.kind == 0)
         keys = int(out["keys"][upd].sum())
-        rs = [r for r, q in zip(rounds, rphase) if q == p]
-        edges = int(sum(r["edges"] for r in rs))
         t_start = trace.phase_start[p]
         span_s = float(out["done"][sel].max() - t_start) if sel.any() else 0.0
         span_p = float(done_p[sel].max() - t_start) if sel.any() else 0.0
-        busy = float(sum(r["seconds"] for r in rs))
         busy_pl = float(busy_p[sel].sum())
 
         def rates(span):
             return {"requests_per_s": int(sel.sum()) / span if span else None,
-                    "edge_updates_per_s": keys / span if span else None,
-                    "bfs_gteps": edges / span / 1e9 if span else None}
+                    "edge_updates_per_s": keys / span if span else None}
 
         res.append({
             "rate_per_s": rate, "seconds": seconds, "requests": int(sel.sum()), "updates": int(upd.sum()),
-            "bfs_queries": int((sel & (trace.kind == 1)).sum()), "update_keys": keys, "edges_traversed": edges,
-            "served": {"rounds": len(rs), "requests_per_round": int(sel.sum()) / max(1, len(rs)),
-                       "max_updates_per_round": max((r["updates"] for r in rs), default=0),
-                       "max_graphs_searched_per_round": max((r["bfs_graphs"] for r in rs), default=0),
-                       "busy_s": busy, "makespan_s": span_s, "utilisation": busy / seconds,
-                       "update_device_ms": float(sum(r["update_ms"] for r in rs)),
-                       "bfs_device_ms": float(sum(r["bfs_ms"] for r in rs)),
-                       **rates(span_s),
+            "bfs_queries": int((sel & (trace.kind == 1)).sum()), "update_keys": keys,
+            "served": {"rounds": int(len(np.unique(out["round"][sel]))), "makespan_s": span_s, **rates(span_s),
                        "update_latency": S.latency_summary(trace, out["done"], p, 0),
                        "bfs_latency": S.latency_summary(trace, out["done"], p, 1)},
             "plain": {"busy_s": busy_pl, "makespan_s": span_p, "utilisation": busy_pl / seconds, **rates(span_p),
@@ -768,13 +762,24 @@ def run_served(args, stream):
                       "bfs_latency": S.latency_summary(trace, done_p, p, 1)},
             "speedup_sustained": span_p / span_s if span_s else None,
         })
+    # the light phase's slowest served requests (kind, keys or sources, latency, wait before its round)
+    light = np.nonzero(trace.phase == 0)[0]
+    lat = out["done"][light] - trace.arrival[light]
+    slow = [{"kind": "update" if trace.kind[i] == 0 else "bfs", "graph": int(trace.graph[i]),
+             "size": int(out["keys"][i]) if trace.kind[i] == 0 else int(len(trace.sources[i])),
+             "arrival_s": float(trace.arrival[i]), "latency_ms": 1e3 * float(out["done"][i] - trace.arrival[i]),
+             "wait_ms": 1e3 * float(out["start"][i] - trace.arrival[i]), "plain_ms": 1e3 * float(busy_p[i])}
+            for i in light[np.argsort(-lat)[:12]]]
     return {
+        "slowest_light": slow,
         "workload": f"32 R-MAT graphs (edges log-uniform [10k, 2M]) + 2 R-MAT scale {args.served_big_scale} "
                     f"(edge factor 16); Poisson arrivals, 70% updates (log-uniform 1k-1M keys, 1:1 "
-                    f"insert:delete), 30% BFS (1-64 sources), uniform graph choice; HBM budget 120 GB; phases "
-                    + ", ".join(f"{r:g}/s for {s:g} simulated s" for r, s in phases),
+                    f"insert:delete), 30% BFS (1-64 sources), uniform graph choice; HBM budget 120 GB; "
+                    f"native serving loop, {args.served_lanes} lanes, real time; phases "
+                    + ", ".join(f"{r:g}/s for {s:g} s" for r, s in phases),
         "graphs": len(specs), "edges_total": int(sum(len(kk) for _, kk in specs)), "requests": len(trace),
         "failed": int((~out["ok"]).sum()), "committed_bytes": int(committed),
+        "lanes": args.served_lanes, "server_stats": stats,
         "phases": res,
         "identical_results": bool(same_reach and same_layout),
         "driver_wall_s": served_wall,
@@ -1047,13 +1052,14 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the built-in tuning (no sweep before timing)")
     ap.add_argument("--batched-graphs", type=int, default=256, help="graphs of the batched configuration (0: skip)")
     ap.add_argument("--batched-steps", type=int, default=5)
-    ap.add_argument("--served-seconds", type=float, default=600.0,
-                    help="simulated seconds of served traffic (0: skip the served configuration)")
-    ap.add_argument("--served-rate", type=float, default=20.0, help="served request arrivals per simulated second")
+    ap.add_argument("--served-seconds", type=float, default=30.0,
+                    help="seconds of served traffic at the light rate, in real time (0: skip the served configuration)")
+    ap.add_argument("--served-rate", type=float, default=20.0, help="served request arrivals per second (light load)")
+    ap.add_argument("--served-lanes", type=int, default=2, help="rounds the server keeps in flight")
     ap.add_argument("--served-big-scale", type=int, default=22, help="R-MAT scale of the two large served graphs")
     ap.add_argument("--served-burst-rate", type=float, default=20000.0,
-                    help="arrivals per simulated second of the saturating phase that follows")
-    ap.add_argument("--served-burst-seconds", type=float, default=1.0)
+                    help="arrivals per second of the saturating phase that follows")
+    ap.add_argument("--served-burst-seconds", type=float, default=0.25)
     ap.add_argument("--sweep", action="store_true",
                     help="only the large-graph batch sweep (R-MAT scale 24, edge factor 32): its own JSON line")
     ap.add_argument("--sweep-scale", type=int, default=24)

@@ -87,7 +87,14 @@ class _StepStats(ctypes.Structure):
 class _ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_round_keys", ctypes.c_uint64),
                 ("max_round_bfs_graphs", ctypes.c_uint32), ("max_queued", ctypes.c_uint32),
-                ("max_queued_keys", ctypes.c_uint64), ("flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("max_queued_keys", ctypes.c_uint64), ("flags", ctypes.c_uint32), ("lanes", ctypes.c_uint32),
+                ("input_ring_bytes", ctypes.c_uint64)]
+
+
+class _ServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("rounds", "requests", "keys", "edges")] + \
+        [(n, ctypes.c_double) for n in ("busy_seconds", "update_ms", "bfs_ms")] + \
+        [(n, ctypes.c_uint32) for n in ("max_round_requests", "max_inflight_rounds")]
 
 
 class _RequestInfo(ctypes.Structure):
@@ -151,6 +158,11 @@ def lib() -> ctypes.CDLL:
         "gpma_server_last_round": (st, [P, P, u32, ctypes.POINTER(u32)]),
         "gpma_server_queued": (st, [P, ctypes.POINTER(u64), ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_double)]),
         "gpma_server_committed_bytes": (st, [P, ctypes.POINTER(u64)]),
+        "gpma_server_start": (st, [P]),
+        "gpma_server_clock": (st, [P, ctypes.POINTER(ctypes.c_double)]),
+        "gpma_server_drain": (st, [P, ctypes.c_double]),
+        "gpma_server_stop": (st, [P]),
+        "gpma_server_get_stats": (st, [P, ctypes.POINTER(_ServerStats)]),
         "gpma_get_tuning": (st, [ctypes.POINTER(_Tuning)]),
         "gpma_bfs_level_profile": (st, [P, P, P, P, u32, ctypes.POINTER(u32)]),
         "gpma_set_tuning": (st, [ctypes.POINTER(_Tuning)]),
@@ -831,19 +843,27 @@ PLAN_ONLY = 1
 
 class Server:
     """Served form (no reference counterpart): resident graphs, update batches
-    and BFS queries with continuous batching, in virtual time.
+    and BFS queries with continuous batching.
 
     ``submit_update`` / ``submit_bfs`` queue requests with their arrival time
     (raising GPMAError with status ERR_BUSY when the queue is full);
-    ``run_round(now)`` runs one round over what has arrived and returns its
-    description; ``poll(id)`` gives a request's state, times and BFS reach.
+    ``poll(id)`` gives a request's state, times and BFS reach. Either the
+    caller drives rounds (``run_round(now)``, on any clock, e.g. virtual time)
+    or ``start()`` runs the native serving loop: one worker thread per lane on
+    the server's own wall clock (``clock()``), rounds starting as soon as a
+    request's arrival has passed and a lane is free; ``drain()`` waits for the
+    queue to empty, ``stop()`` ends the loop. With ``lanes`` > 1 that many
+    rounds are in flight at once, each on its own stream and buffers.
+    ``input_ring_bytes`` sizes a pinned host ring that queued update batches
+    are copied into at submission (uploads from pinned memory, however long
+    a batch waited).
     """
 
     def __init__(self, hbm_budget_bytes: int = 120 << 30, max_round_keys: int = 1 << 24,
                  max_round_bfs_graphs: int = 4096, max_queued: int = 1 << 20, max_queued_keys: int = 1 << 28,
-                 plan_only: bool = False, stream=None):
+                 plan_only: bool = False, stream=None, lanes: int = 1, input_ring_bytes: int = 0):
         cfg = _ServerConfig(int(hbm_budget_bytes), int(max_round_keys), int(max_round_bfs_graphs), int(max_queued),
-                            int(max_queued_keys), PLAN_ONLY if plan_only else 0, 0)
+                            int(max_queued_keys), PLAN_ONLY if plan_only else 0, int(lanes), int(input_ring_bytes))
         h = ctypes.c_void_p()
         _check(lib().gpma_server_create(ctypes.byref(cfg), _stream_ptr(stream), ctypes.byref(h)), "gpma_server_create")
         self._h = h
@@ -936,3 +956,24 @@ class Server:
         b = ctypes.c_uint64()
         _check(lib().gpma_server_committed_bytes(self._h, ctypes.byref(b)), "gpma_server_committed_bytes")
         return b.value
+
+    def start(self) -> None:
+        """Starts the serving loop (the server's clock starts at 0)."""
+        _check(lib().gpma_server_start(self._h), "gpma_server_start")
+
+    def clock(self) -> float:
+        t = ctypes.c_double()
+        _check(lib().gpma_server_clock(self._h, ctypes.byref(t)), "gpma_server_clock")
+        return t.value
+
+    def drain(self, timeout: float = 600.0) -> None:
+        """Waits until nothing is queued or running (raises on a failed round or the timeout)."""
+        _check(lib().gpma_server_drain(self._h, float(timeout)), "gpma_server_drain")
+
+    def stop(self) -> None:
+        _check(lib().gpma_server_stop(self._h), "gpma_server_stop")
+
+    def stats(self) -> dict:
+        st = _ServerStats()
+        _check(lib().gpma_server_get_stats(self._h, ctypes.byref(st)), "gpma_server_get_stats")
+        return {name: getattr(st, name) for name, _ in _ServerStats._fields_}

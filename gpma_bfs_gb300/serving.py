@@ -1,4 +1,4 @@
-"""Served-form traffic: request traces and their replay in virtual time.
+"""Served-form traffic: request traces and their replay.
 
 ``make_trace`` draws Poisson arrivals of update batches and BFS queries over
 resident graphs, in phases of (rate, seconds). ``replay_served`` feeds a trace
@@ -9,6 +9,8 @@ by its measured wall time; an idle server jumps to the next arrival).
 plain drop-in calls (``update_gpma`` / ``gpma_bfs_multi``), FIFO, on its own
 graphs, with the same clock rule. Both return per-request completion times
 and BFS reach, so results and latencies can be compared request by request.
+``replay_served_live`` replays a trace in real time through the server's
+native serving loop (worker threads per lane on the server's clock).
 """
 from __future__ import annotations
 
@@ -98,6 +100,53 @@ def replay_served(srv: Server, gids, streams, trace: Trace):
     return {"done": np.array([x["done"] for x in infos]), "ok": np.array([x["state"] == 1 for x in infos]),
             "keys": np.array([x["keys"] for x in infos], np.int64), "reach": [x["reached"] for x in infos],
             "rounds": rounds}
+
+
+def replay_served_live(srv: Server, gids, streams, trace: Trace, timeout: float = 600.0):
+    """The trace in real time through the server's native serving loop:
+    every request is submitted in arrival order with its arrival on the
+    server's clock, ahead of time -- as many as the queue limits take before
+    the loop starts (clock 0), the rest while it runs (ERR_BUSY holds the
+    submitter back) -- and runs once the clock has passed its arrival, in a
+    round of whichever lane is free. Returns per-request arrays as
+    replay_served does, plus the server's round totals."""
+    n = len(trace)
+    ids = []
+    started = False
+    try:
+        j = 0
+        held = None
+        while j < n:
+            g = int(trace.graph[j])
+            try:
+                if trace.kind[j] == 0:
+                    k, v = held if held is not None else streams[g].step(int(trace.size[j]))
+                    ids.append(srv.submit_update(gids[g], k, v, float(trace.arrival[j])))
+                else:
+                    ids.append(srv.submit_bfs(gids[g], trace.sources[j], float(trace.arrival[j])))
+            except GPMAError as e:
+                if e.status != ERR_BUSY:
+                    raise
+                held = (k, v) if trace.kind[j] == 0 else None
+                if not started:
+                    srv.start()
+                    started = True
+                time.sleep(0.0005)  # the queue is full: rounds free its slots
+                continue
+            held = None
+            j += 1
+        if not started:
+            srv.start()
+            started = True
+        srv.drain(timeout)
+    finally:
+        if started:
+            srv.stop()
+    infos = [srv.poll(i, release=True) for i in ids]
+    return {"done": np.array([x["done"] for x in infos]), "start": np.array([x["start"] for x in infos]),
+            "ok": np.array([x["state"] == 1 for x in infos]), "round": np.array([x["round"] for x in infos]),
+            "keys": np.array([x["keys"] for x in infos], np.int64), "reach": [x["reached"] for x in infos],
+            "stats": srv.stats()}
 
 
 def replay_plain(graphs: list[GPMA], streams, trace: Trace, stream=None, level_buffer=None, sync=None):

@@ -232,10 +232,22 @@ GPMA_API gpma_status gpma_batch_step_get_stats(const gpma_batch_step *st, gpma_s
  * batched update launch followed by one multi-source BFS launch. Requests that
  * arrive while a round runs join a later round. A graph's requests therefore
  * take effect in arrival order and every result equals what the same requests
- * give applied to that graph alone. Time is virtual: the caller passes the
- * current time to each round; a round's updates complete at that time plus
- * the measured wall-clock time of its update launch, its searches at that
- * time plus the whole round's.
+ * give applied to that graph alone. Time is the caller's: it passes the
+ * current time to each round (a virtual clock, or the wall clock since some
+ * start); a round's updates complete at that time plus the measured
+ * wall-clock time of its update launch, its searches at that time plus the
+ * whole round's; a request runs only once the time passed reaches its
+ * arrival, so requests may be submitted ahead of it.
+ *
+ * Lanes. With lanes = k > 1 the server keeps k rounds in flight: each lane
+ * has its own stream, batch buffers and pinned staging, gpma_server_run_round
+ * may be called from k host threads at once (each call takes a free lane, or
+ * returns an empty round when all k are busy), and a graph whose requests are
+ * in one lane's round is left out of the other lanes' rounds until that round
+ * completes, so a graph's requests still run in arrival order. Requests that
+ * arrive while one round is on the GPU start in another lane without waiting
+ * for it. The submit, poll, cancel and query calls may run concurrently with
+ * rounds. With one lane (the default) rounds run one after another.
  *
  * Admission. A graph is admitted only if its estimated device bytes fit the
  * HBM budget; an update joins a round only if the graph's worst-case growth
@@ -255,14 +267,18 @@ typedef struct gpma_server_config {
     uint32_t max_queued;           /* waiting requests */
     uint64_t max_queued_keys;      /* waiting update keys (host copies) */
     uint32_t flags;                /* GPMA_SERVER_PLAN_ONLY */
-    uint32_t reserved;
+    uint32_t lanes;                /* rounds in flight at once, 1..4 (0: 1) */
+    uint64_t input_ring_bytes;     /* pinned host ring that queued update batches are copied into at submission
+                                      (rounds upload them from there; a batch that finds it full stays in
+                                      pageable memory); 0: none */
 } gpma_server_config;
 
 typedef enum gpma_request_state {
     GPMA_REQ_QUEUED = 0,
     GPMA_REQ_DONE = 1,
     GPMA_REQ_FAILED = 2,
-    GPMA_REQ_CANCELLED = 3  /* withdrawn by gpma_server_cancel before a round took it */
+    GPMA_REQ_CANCELLED = 3, /* withdrawn by gpma_server_cancel before a round took it */
+    GPMA_REQ_RUNNING = 4    /* taken by a round that has not completed yet */
 } gpma_request_state;
 
 typedef struct gpma_request_info {
@@ -314,9 +330,9 @@ GPMA_API gpma_status gpma_server_submit_update(gpma_server *s, uint32_t graph_id
  * and must stay valid until then. */
 GPMA_API gpma_status gpma_server_submit_bfs(gpma_server *s, uint32_t graph_id, const uint32_t *sources, uint32_t k,
                                             double arrival, uint32_t *levels, uint64_t *request_id);
-/* Runs one round at virtual time `now` over the requests that arrived by
- * then; info (optional) describes it. A round with nothing to run returns
- * GPMA_OK with info->updates == info->bfs_requests == 0. */
+/* Runs one round at time `now` over the requests that arrived by then, on a
+ * free lane; info (optional) describes it. A round with nothing to run (or no
+ * free lane) returns GPMA_OK with info->updates == info->bfs_requests == 0. */
 GPMA_API gpma_status gpma_server_run_round(gpma_server *s, double now, gpma_round_info *info);
 /* A request's state and result; release != 0 forgets a finished request. */
 GPMA_API gpma_status gpma_server_poll(gpma_server *s, uint64_t request_id, int release, gpma_request_info *out);
@@ -328,8 +344,35 @@ GPMA_API gpma_status gpma_server_poll(gpma_server *s, uint64_t request_id, int r
  * without that update. GPMA_ERR_INVALID for an unknown request or one that
  * has already run. No reference counterpart. */
 GPMA_API gpma_status gpma_server_cancel(gpma_server *s, uint64_t request_id);
-/* Ids of the requests the last round ran, in execution order (updates, then
- * searches graph by graph, lanes ascending). */
+/* Serving loop. gpma_server_start starts the server's clock at 0 and one
+ * worker thread per lane; each runs rounds as soon as a queued request's
+ * arrival (on that clock) has passed and a lane is free, and sleeps
+ * otherwise (woken by submissions and completed rounds). Requests may be
+ * submitted ahead of their arrival. gpma_server_clock reads the clock;
+ * gpma_server_drain waits until no request is queued or running
+ * (GPMA_ERR_TIMEOUT after timeout_seconds) and returns the first error a
+ * round of the loop met; gpma_server_stop ends the loop after the rounds in
+ * flight (gpma_server_destroy does too). While the loop runs, do not call
+ * gpma_server_run_round. No reference counterpart. */
+GPMA_API gpma_status gpma_server_start(gpma_server *s);
+GPMA_API gpma_status gpma_server_clock(const gpma_server *s, double *now);
+GPMA_API gpma_status gpma_server_drain(gpma_server *s, double timeout_seconds);
+GPMA_API gpma_status gpma_server_stop(gpma_server *s);
+/* Totals over every round run so far (by gpma_server_run_round or the loop). */
+typedef struct gpma_server_stats {
+    uint64_t rounds;              /* rounds that ran requests */
+    uint64_t requests;            /* requests they completed or failed */
+    uint64_t keys;                /* update keys applied */
+    uint64_t edges;               /* edges traversed by their searches, all lanes */
+    double busy_seconds;          /* sum of their wall-clock times (lanes overlap: may exceed elapsed time) */
+    double update_ms;             /* device time of their update launches */
+    double bfs_ms;                /* device time of their search launches */
+    uint32_t max_round_requests;  /* most requests in one round */
+    uint32_t max_inflight_rounds; /* most rounds in flight at once */
+} gpma_server_stats;
+GPMA_API gpma_status gpma_server_get_stats(const gpma_server *s, gpma_server_stats *out);
+/* Ids of the requests the last round run by the calling host thread ran, in
+ * execution order (updates, then searches graph by graph, lanes ascending). */
 GPMA_API gpma_status gpma_server_last_round(const gpma_server *s, uint64_t *ids, uint32_t capacity, uint32_t *count);
 /* Waiting requests and waiting update keys; earliest arrival among queue heads
  * (+infinity when nothing waits). */

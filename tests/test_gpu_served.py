@@ -125,3 +125,65 @@ def test_served_budget_rejects_growth(built_lib):
     assert all(np.array_equal(x, y) for x, y in zip(before, after))
     assert srv.poll(r2)["state"] == 1
     srv.close()
+
+
+def test_served_live_two_lanes_equal_alone(built_lib):
+    """The native serving loop with two lanes in real time: rounds of
+    different graphs are in flight at once (each lane its own stream and
+    buffers), batches are uploaded from the pinned input ring or from host
+    vectors, and still every search's reach and levels and every graph's
+    final layout equal the same requests applied to each graph alone."""
+    import gpma_bfs_gb300 as G
+    from gpma_bfs_gb300.workloads import SlidingStream
+
+    rng = np.random.default_rng(22)
+    specs = []
+    for i in range(16):
+        scale = int(rng.integers(8, 14))
+        src, dst = G.gen_rmat(scale, 8, seed=700 + i)
+        specs.append((1 << scale, G.edges_to_keys(src, dst)))
+    loads = [SlidingStream(k).load() for _, k in specs]
+    _, trace = _trace(rng, specs, 600, rate=3000.0)
+
+    # a small pinned input ring: some batches are staged there (wrapping
+    # around), the others stay in host vectors
+    srv = G.Server(max_round_keys=20_000, max_round_bfs_graphs=8, lanes=2, input_ring_bytes=256 << 10)
+    gids = [srv.add_graph(n, len(k)) for n, k in specs]
+    for gid, (k, v) in zip(gids, loads):
+        G.update_gpma(srv.graph(gid), k, v)
+    import torch
+
+    torch.cuda.synchronize()
+    srv.start()
+    ids = []
+    for t, g, kind, p in trace:  # all submitted ahead; each runs once the clock passes its arrival
+        if kind == 0:
+            ids.append(srv.submit_update(gids[g], p[0], p[1], t))
+        else:
+            ids.append(srv.submit_bfs(gids[g], p[0], t, levels=p[1]))
+    srv.drain(120.0)
+    srv.stop()
+    st = srv.stats()
+    assert st["requests"] == len(trace)
+    assert st["max_inflight_rounds"] == 2  # the lanes overlapped
+    infos = [srv.poll(i) for i in ids]
+    assert all(x["state"] == 1 and x["start"] >= x["arrival"] - 1e-9 for x in infos)
+
+    alone = [G.GPMA(n) for n, _ in specs]
+    for g, (k, v) in zip(alone, loads):
+        G.update_gpma(g, k, v)
+    for (t, g, kind, p), rid, info in zip(trace, ids, infos):
+        if kind == 0:
+            G.update_gpma(alone[g], p[0], p[1])
+            continue
+        lv, reached = G.gpma_bfs_multi(alone[g], p[0])
+        assert np.array_equal(info["reached"], reached), f"request {rid} (graph {g})"
+        if p[1]:
+            assert np.array_equal(srv.levels(rid), lv), f"levels of request {rid}"
+    for i, gid in enumerate(gids):
+        a = srv.graph(gid).export_layout()
+        b = alone[i].export_layout()
+        assert all(np.array_equal(x, y) for x, y in zip(a, b)), f"graph {i}"
+    for g in alone:
+        g.close()
+    srv.close()

@@ -256,3 +256,77 @@ def test_cancelled_update_frees_the_graph_for_its_searches(G):
     assert ran == [first]  # g0's update waits for the next round, its search with it
     ran, first, late, b = scenario(cancel=True)
     assert ran == [first, b]
+
+
+def test_serving_loop_runs_requests_after_their_arrival(G):
+    """The native serving loop (two lanes, plan-only): requests submitted
+    ahead of their arrival run once the server's clock passes it, every one
+    exactly once, per graph in arrival order with at most one update per
+    round, and drain returns once nothing is queued or running."""
+    import gpma_bfs_gb300.serving as S
+    from gpma_bfs_gb300.workloads import SlidingStream
+
+    rng = np.random.default_rng(11)
+    specs = []
+    for i in range(5):
+        n = 1 << int(rng.integers(6, 9))
+        keys = np.unique(rng.integers(0, n, 4 * n).astype(np.uint64) << np.uint64(32)
+                         | rng.integers(0, n, 4 * n).astype(np.uint64))
+        specs.append((n, rng.permutation(keys)))
+    trace = S.make_trace(specs, [(2000.0, 0.1), (20000.0, 0.02)], seed=12, min_batch=10, max_batch=300)
+    srv = G.Server(plan_only=True, lanes=2, max_round_keys=500)
+    gids = [srv.add_graph(n, len(k)) for n, k in specs]
+    out = S.replay_served_live(srv, gids, [SlidingStream(k) for _, k in specs], trace, timeout=30.0)
+    assert out["ok"].all() and len(out["done"]) == len(trace)
+    assert np.all(out["start"] >= trace.arrival - 1e-9)  # nothing ran before it arrived
+    st = out["stats"]
+    assert st["requests"] == len(trace) and st["rounds"] >= 1
+    for g in range(len(specs)):
+        idx = np.nonzero(trace.graph == g)[0]
+        rounds = out["round"][idx]
+        assert np.all(np.diff(rounds) >= 0)  # a graph's requests in arrival order
+        for k in np.unique(rounds):
+            assert (trace.kind[idx][rounds == k] == 0).sum() <= 1
+    assert srv.queued()[0] == 0
+    srv.close()
+
+
+def test_serving_loop_start_stop_and_lane_limits(G):
+    with pytest.raises(G.GPMAError):
+        G.Server(plan_only=True, lanes=5)
+    s = G.Server(plan_only=True, lanes=3)
+    g = s.add_graph(16, 10)
+    s.start()
+    with pytest.raises(G.GPMAError):
+        s.start()  # already running
+    t = s.clock()
+    rid = s.submit_bfs(g, [1], arrival=t + 0.05)
+    assert s.poll(rid)["state"] == 0  # not yet arrived
+    s.drain(10.0)
+    p = s.poll(rid)
+    assert p["state"] == 1 and p["start"] >= t + 0.05
+    s.stop()
+    s.stop()  # idempotent
+    s.close()
+
+
+def test_input_ring_takes_what_fits_and_reuses_space(G):
+    """Queued batches go to the input ring while it has room (the rest stay in
+    host vectors); completed and cancelled requests give their space back,
+    also across the ring's wrap-around, and every request still runs once."""
+    s = G.Server(plan_only=True, input_ring_bytes=4096, max_round_keys=1 << 20)
+    g = [s.add_graph(64, 1000) for _ in range(3)]
+    rng = np.random.default_rng(5)
+    ids = []
+    for step in range(40):
+        for gi in g:
+            n = int(rng.integers(1, 200))  # 9 B per key: up to 1.8 KB, so the ring fills and wraps
+            ids.append(s.submit_update(gi, *_upd(n), arrival=float(step)))
+        if step % 7 == 3:
+            s.cancel(ids[-1])
+        s.run_round(float(step))
+    while s.queued()[0]:
+        s.run_round(1e9)
+    states = [s.poll(i)["state"] for i in ids]
+    assert all(x in (1, 3) for x in states) and states.count(3) == 6
+    s.close()
