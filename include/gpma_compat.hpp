@@ -16,6 +16,16 @@
 // for mismatched key/value counts (as multidev.cuh:107-108) and bad
 // arguments, std::runtime_error otherwise (the reference printed and went on,
 // utils.cuh:56-61).
+//
+// The structure's members read as the reference's fields (gpma.cuh:31-50):
+// gpma.keys, gpma.values and gpma.row_offset are views of the device arrays
+// (data() gives the current device address, as RAW_PTR(gpma.keys) expects;
+// size(); [i] copies one element to the host; to_host() the whole array);
+// gpma.segment_length and gpma.tree_height convert to SIZE_TYPE and
+// gpma.lower_element / gpma.upper_element to the threshold vectors, always
+// for the current geometry (the array grows and shrinks with updates). Each
+// of them can also be called, e.g. gpma.segment_length() or gpma.keys() for
+// a host copy.
 #pragma once
 
 #include "gpma_gb300.h"
@@ -52,52 +62,124 @@ inline void check(gpma_status s, const char *where) {
     throw std::runtime_error(msg);
 }
 
+namespace detail {
+
+inline gpma_geometry geometry_of(gpma_graph *h) {
+    gpma_geometry g;
+    check(gpma_get_geometry(h, &g), "GPMA::geometry");
+    return g;
+}
+
+// A view of one device array of the structure (0 keys, 1 values, 2 row_offset).
+template <typename T, int WHICH>
+class DeviceArray {
+  public:
+    explicit DeviceArray(gpma_graph *const *h) : h_(h) {}
+    T *data() const {
+        const uint64_t *k = nullptr;
+        const uint8_t *v = nullptr;
+        const uint32_t *r = nullptr;
+        check(gpma_device_arrays(*h_, &k, &v, &r), "GPMA device array");
+        const void *p = WHICH == 0 ? (const void *)k : WHICH == 1 ? (const void *)v : (const void *)r;
+        return static_cast<T *>(const_cast<void *>(p));
+    }
+    size_t size() const {
+        const gpma_geometry g = geometry_of(*h_);
+        return WHICH == 2 ? (size_t)g.row_num + 1 : (size_t)g.size;
+    }
+    std::vector<T> to_host() const {
+        std::vector<T> out(size());
+        void *dst[3] = {nullptr, nullptr, nullptr};
+        dst[WHICH] = out.data();
+        check(gpma_export_layout(*h_, static_cast<uint64_t *>(dst[0]), static_cast<uint8_t *>(dst[1]),
+                                 static_cast<uint32_t *>(dst[2]), nullptr),
+              "GPMA device array");
+        return out;
+    }
+    std::vector<T> operator()() const { return to_host(); }
+    T operator[](size_t i) const {
+        const std::vector<T> all = to_host();
+        if (i >= all.size())
+            throw std::invalid_argument("GPMA device array: index out of range");
+        return all[i];
+    }
+
+  private:
+    gpma_graph *const *h_;
+};
+
+// segment_length / tree_height: the current geometry's value.
+template <int WHICH>
+class GeometryValue {
+  public:
+    explicit GeometryValue(gpma_graph *const *h) : h_(h) {}
+    operator SIZE_TYPE() const {
+        const gpma_geometry g = geometry_of(*h_);
+        return WHICH == 0 ? g.segment_length : g.tree_height;
+    }
+    SIZE_TYPE operator()() const { return static_cast<SIZE_TYPE>(*this); }
+
+  private:
+    gpma_graph *const *h_;
+};
+
+// lower_element / upper_element: the current density thresholds per level.
+template <int WHICH>
+class Thresholds {
+  public:
+    explicit Thresholds(gpma_graph *const *h) : h_(h) {}
+    std::vector<SIZE_TYPE> operator()() const {
+        const SIZE_TYPE height = geometry_of(*h_).tree_height;
+        std::vector<SIZE_TYPE> lo(height + 1), hi(height + 1);
+        check(gpma_get_thresholds(*h_, lo.data(), hi.data()), "GPMA::thresholds");
+        return WHICH == 0 ? lo : hi;
+    }
+    operator std::vector<SIZE_TYPE>() const { return (*this)(); }
+    SIZE_TYPE operator[](size_t level) const {
+        const std::vector<SIZE_TYPE> t = (*this)();
+        if (level >= t.size())
+            throw std::invalid_argument("GPMA thresholds: level out of range");
+        return t[level];
+    }
+    size_t size() const { return (size_t)geometry_of(*h_).tree_height + 1; }
+
+  private:
+    gpma_graph *const *h_;
+};
+
+}  // namespace detail
+
 template <dev_type_t DEV = GPU>
 class GPMA {
     static_assert(DEV == GPU, "this library has no CPU structure: the update and BFS run on the GPU only");
 
   public:
-    explicit GPMA(SIZE_TYPE row_num, void *stream = nullptr) : row_num(row_num) {
+    explicit GPMA(SIZE_TYPE row_num, void *stream = nullptr)
+        : keys(&handle_), values(&handle_), row_offset(&handle_), segment_length(&handle_), tree_height(&handle_),
+          lower_element(&handle_), upper_element(&handle_), row_num(row_num) {
         check(gpma_create(row_num, stream, &handle_), "GPMA(row_num)");
     }
     ~GPMA() { gpma_destroy(handle_); }
     GPMA(const GPMA &) = delete;
     GPMA &operator=(const GPMA &) = delete;
 
-    int get_size() const { return (int)geometry().size; }
-    SIZE_TYPE segment_length() const { return geometry().segment_length; }
-    SIZE_TYPE tree_height() const { return geometry().tree_height; }
-    std::vector<SIZE_TYPE> lower_element() const { return thresholds().first; }
-    std::vector<SIZE_TYPE> upper_element() const { return thresholds().second; }
-
-    // Host copies of the device arrays (GPMA::keys, values, row_offset).
-    std::vector<KEY_TYPE> keys() const {
-        std::vector<KEY_TYPE> k(geometry().size);
-        check(gpma_export_layout(handle_, k.data(), nullptr, nullptr, nullptr), "GPMA::keys");
-        return k;
-    }
-    std::vector<SIZE_TYPE> row_offset() const {
-        std::vector<SIZE_TYPE> r((size_t)row_num + 1);
-        check(gpma_export_layout(handle_, nullptr, nullptr, r.data(), nullptr), "GPMA::row_offset");
-        return r;
-    }
+    int get_size() const { return (int)detail::geometry_of(handle_).size; }
 
     gpma_graph *handle() const { return handle_; }
-    const SIZE_TYPE row_num;
 
   private:
-    gpma_geometry geometry() const {
-        gpma_geometry g;
-        check(gpma_get_geometry(handle_, &g), "GPMA::geometry");
-        return g;
-    }
-    std::pair<std::vector<SIZE_TYPE>, std::vector<SIZE_TYPE>> thresholds() const {
-        SIZE_TYPE h = tree_height();
-        std::vector<SIZE_TYPE> lo(h + 1), hi(h + 1);
-        check(gpma_get_thresholds(handle_, lo.data(), hi.data()), "GPMA::thresholds");
-        return {lo, hi};
-    }
-    gpma_graph *handle_ = nullptr;
+    gpma_graph *handle_ = nullptr;  // declared before the views that refer to it
+
+  public:
+    // the reference's fields (gpma.cuh:31-50), read through the library
+    const detail::DeviceArray<KEY_TYPE, 0> keys;
+    const detail::DeviceArray<VALUE_TYPE, 1> values;
+    const detail::DeviceArray<SIZE_TYPE, 2> row_offset;
+    const detail::GeometryValue<0> segment_length;
+    const detail::GeometryValue<1> tree_height;
+    const detail::Thresholds<0> lower_element;
+    const detail::Thresholds<1> upper_element;
+    const SIZE_TYPE row_num;
 };
 
 template <dev_type_t DEV>

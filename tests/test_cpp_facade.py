@@ -10,10 +10,11 @@ ROOT = Path(__file__).resolve().parent.parent
 LIBDIR = ROOT / "gpma_bfs_gb300"
 
 
-def build_demo(tmp_path) -> Path:
-    exe = tmp_path / "facade_demo"
-    subprocess.run(["g++", "-O2", "-std=c++17", f"-I{ROOT / 'include'}", str(ROOT / "tests/cpp/facade_demo.cpp"),
-                    f"-L{LIBDIR}", "-lgpma_gb300", f"-Wl,-rpath,{LIBDIR}", "-o", str(exe)],
+def build_demo(tmp_path, name="facade_demo") -> Path:
+    exe = tmp_path / name
+    subprocess.run(["g++", "-O2", "-std=c++17", "-Wall", "-Werror", f"-I{ROOT / 'include'}",
+                    str(ROOT / f"tests/cpp/{name}.cpp"), f"-L{LIBDIR}", "-lgpma_gb300", f"-Wl,-rpath,{LIBDIR}",
+                    "-o", str(exe)],
                    check=True, capture_output=True, text=True)
     return exe
 
@@ -21,6 +22,7 @@ def build_demo(tmp_path) -> Path:
 def test_facade_compiles_and_links(tmp_path, built_lib):
     exe = build_demo(tmp_path)
     assert exe.exists()
+    assert build_demo(tmp_path, "facade_fields").exists()  # field-style reads compile
     # no GPU needed for argument handling
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert "Invalid arguments." in r.stdout
@@ -50,3 +52,12 @@ def test_facade_demo_matches_oracle(tmp_path, built_lib):
         o.update(np.concatenate([ins, dels]), np.r_[np.ones(step, np.uint8), np.zeros(step, np.uint8)])
     want.append(o.bfs(0)[1])
     assert got == want
+
+
+@pytest.mark.gpu
+def test_facade_fields_read_the_structure(tmp_path, built_lib):
+    """gpma.keys / row_offset / segment_length / tree_height / lower_element
+    read like the reference's fields, for the geometry after an update."""
+    exe = build_demo(tmp_path, "facade_fields")
+    out = subprocess.run([str(exe), "300"], capture_output=True, text=True, check=True).stdout
+    assert "guards_bad 0" in out and "ptr 1" in out
