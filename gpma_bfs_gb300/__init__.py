@@ -65,13 +65,13 @@ class _Profile(ctypes.Structure):
     _fields_ = [("sort_ms", ctypes.c_double), ("locate_ms", ctypes.c_double), ("group_ms", ctypes.c_double),
                 ("levels_ms", ctypes.c_double), ("update_kernel_ms", ctypes.c_double), ("rebuild_ms", ctypes.c_double),
                 ("bfs_ms", ctypes.c_double), ("update_kernels", ctypes.c_uint64), ("bfs_kernels", ctypes.c_uint64),
-                ("kernel_launches", ctypes.c_uint64), ("bfs_edges", ctypes.c_uint64)]
+                ("kernel_launches", ctypes.c_uint64), ("bfs_edges", ctypes.c_uint64), ("sort_fallbacks", ctypes.c_uint64)]
 
 
 class _Tuning(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint32) for n in ("bfs_dense_div", "bfs_blocks_per_sm", "ms_dense_div",
-                                               "ms_blocks_per_sm", "update_blocks_per_sm")] + \
-               [("reserved", ctypes.c_uint32 * 3)]
+                                               "ms_blocks_per_sm", "update_blocks_per_sm", "update_sort")] + \
+               [("reserved", ctypes.c_uint32 * 2)]
 
 
 class _TestHooks(ctypes.Structure):
@@ -552,7 +552,8 @@ def components(gpma: GPMA, out=None, stream=None):
     return out, c.value, r.value
 
 
-TUNING_FIELDS = ("bfs_dense_div", "bfs_blocks_per_sm", "ms_dense_div", "ms_blocks_per_sm", "update_blocks_per_sm")
+TUNING_FIELDS = ("bfs_dense_div", "bfs_blocks_per_sm", "ms_dense_div", "ms_blocks_per_sm", "update_blocks_per_sm",
+                 "update_sort")
 
 
 def get_tuning() -> dict:

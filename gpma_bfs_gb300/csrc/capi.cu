@@ -917,6 +917,7 @@ gpma_status gpma_get_tuning(gpma_tuning *out) {
     out->ms_dense_div = g_tuning.ms_dense_div;
     out->ms_blocks_per_sm = g_tuning.ms_blocks_per_sm;
     out->update_blocks_per_sm = g_tuning.update_blocks_per_sm;
+    out->update_sort = g_tuning.update_sort;
     return GPMA_OK;
 }
 
@@ -930,11 +931,16 @@ gpma_status gpma_set_tuning(const gpma_tuning *t) {
         set_error("gpma_set_tuning: CTAs per SM above %d", MAX_BLOCKS_PER_SM);
         return GPMA_ERR_INVALID;
     }
+    if (t->update_sort > 1) {
+        set_error("gpma_set_tuning: update_sort %u is not 0 (buckets) or 1 (digit passes)", t->update_sort);
+        return GPMA_ERR_INVALID;
+    }
     g_tuning.bfs_dense_div = t->bfs_dense_div;
     g_tuning.bfs_blocks_per_sm = t->bfs_blocks_per_sm;
     g_tuning.ms_dense_div = t->ms_dense_div;
     g_tuning.ms_blocks_per_sm = t->ms_blocks_per_sm;
     g_tuning.update_blocks_per_sm = t->update_blocks_per_sm;
+    g_tuning.update_sort = t->update_sort;
     return GPMA_OK;
 }
 

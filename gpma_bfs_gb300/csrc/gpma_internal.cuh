@@ -95,7 +95,8 @@ struct DeviceStatus {
     uint32_t significant;   // single graph: >= SIGNIFICANT_INSERTS insertions (host rebuild)
     uint32_t inserts;       // insertions after delete/modify (all graphs)
     uint32_t levels;        // level iterations executed
-    uint32_t pad[3];
+    uint32_t sort_fallback; // a bucket of the bucket sort held more than one item: digit passes instead
+    uint32_t pad[2];
     unsigned long long accepted_windows;
     unsigned long long accepted_slots;
     GridBarrier bar;
@@ -113,7 +114,10 @@ struct GraphDesc {
     uint8_t *svals;
     uint64_t *heads;  // heads[s] == keys[s * seg]: the keys the locate descent compares
     uint32_t row_num, size, seg, log2seg, height;
-    uint32_t pad[3];
+    // bucket of a key for this launch's bucket sort: its row's slots
+    // interpolated by its column (qbits: bits of the largest column), shifted
+    // right by qshift, capped at qnbm1
+    uint32_t qbits, qshift, qnbm1;
     uint32_t lower[MAX_LEVELS];
     uint32_t upper[MAX_LEVELS];
 };
@@ -163,14 +167,20 @@ struct BatchBuffers {
     uint64_t sort_status_cap = 0;
     uint32_t *sort_hist = nullptr;     // [graph][8][256] digit counts
     uint32_t hist_cap = 0;             // graphs
+    uint32_t *qcnt = nullptr;          // bucket sort: keys per bucket (zeroed per update)
+    uint32_t *qstart = nullptr;        // bucket sort: bucket offsets within their scan chunk
+    uint64_t q_cap = 0;                // buckets
     // per-graph tables, one upload per launch from pinned memory:
     // [GraphDesc x gcap][batch offsets x (gcap + 1)][sort tile offsets x (gcap + 1)]
+    // [bucket offsets x (gcap + 1)][bucket-sort item offsets x (gcap + 1)]
     uint32_t gcap = 0;
     unsigned char *d_tab = nullptr;
     unsigned char *h_tab = nullptr;    // pinned
     GraphDesc *gd = nullptr;           // views into d_tab
     uint32_t *boff = nullptr;
     uint32_t *toff = nullptr;
+    uint32_t *qoff = nullptr;
+    uint32_t *qtoff = nullptr;
     // status, double-buffered: a slot is [DeviceStatus][GraphStatus x gcap]
     // (GraphStatus from STAT_GS_OFFSET); each launch zeroes the other slot and
     // the sort state it used, so steady-state launches need no memsets
@@ -481,6 +491,7 @@ struct Tuning {
     uint32_t ms_dense_div = 8;
     uint32_t ms_blocks_per_sm = 8;
     uint32_t update_blocks_per_sm = 0;  // 0: chosen per launch (3-CTA build from 1M keys)
+    uint32_t update_sort = 0;           // 0: bucket sort (digit passes for crowded buckets), 1: digit passes
 };
 extern Tuning g_tuning;
 // CTAs per SM for a kernel that fits `fit` per SM, given a tuned request (0 = fit).

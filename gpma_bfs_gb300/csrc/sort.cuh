@@ -15,6 +15,10 @@
 //      each digit run leaves as a contiguous burst.
 // Tiles are claimed in counter order by co-resident CTAs, so every look-back
 // waits only on tiles that are already being processed.
+//
+// The default is a bucket sort with no look-back and four grid barriers
+// (bsort_* below); the digit passes above remain for batches that crowd one
+// bucket (a burst into a few rows, a bulk load with hub rows).
 #pragma once
 
 #include "gpma_internal.cuh"
@@ -230,6 +234,299 @@ __device__ void sort_tile(int pass, uint32_t tile, const uint64_t *__restrict__ 
         out_v[pos] = s_vals[i];
     }
     __syncthreads();
+}
+
+// ---- bucket sort ----------------------------------------------------------------
+// Each graph's slot array is cut into a power of two of equal slot ranges,
+// sized on the host for about BSORT_AVG keys each; a key's bucket is the range
+// its row's slots fall in, interpolated linearly by its column (bucket_of).
+// Rows hold slots in proportion to their degree, so power-law hub rows spread
+// over several buckets as long as the batch follows the graph's own degrees
+// (a sliding window does). Four phases, one grid barrier after each:
+//   Q1 every key takes a rank in its bucket (one atomic per key);
+//   Q2 the bucket counts are scanned chunk by chunk (one chunk per CTA); a
+//      bucket of more than BSORT_MAX_BUCKET keys sends the launch to the digit
+//      passes;
+//   Q3 every key is written to its bucket's range at its rank, with its batch
+//      index and its bucket's first position and size;
+//   Q4 items of whole buckets (item j of a graph holds the buckets that start
+//      in [j, j + 1) * BSORT_ITEM of its range, at most BSORT_CAP keys) are
+//      staged in shared memory; each key's place in its bucket is the number
+//      of keys of the bucket before it in (key, batch index) order (a bucket
+//      holds a few dozen keys), or, in an item with a bucket of more than
+//      BSORT_RANK_MAX keys, the item is sorted by a bitonic network; each
+//      value is gathered by its batch index.
+// Equal keys end in batch order, so the result is the stable sort's whatever
+// order the ranks were taken in.
+constexpr uint32_t BSORT_ITEM = 1024;
+constexpr uint32_t BSORT_CAP = 4 * BSORT_ITEM;
+constexpr uint32_t BSORT_MAX_BUCKET = BSORT_CAP - BSORT_ITEM;
+constexpr uint32_t BSORT_AVG = 32;
+constexpr uint32_t BSORT_RANK_MAX = 256;
+constexpr int BSORT_ILP = 4;
+constexpr size_t BSORT_SMEM_ITEMS = (size_t)BSORT_CAP * 12;  // keys, then indices
+// the chunk prefix (one word per CTA) follows the item in shared memory
+constexpr uint32_t BSORT_MAX_GRID = (uint32_t)((UPDATE_SMEM - BSORT_SMEM_ITEMS) / 4);
+static_assert(BSORT_SMEM_ITEMS < UPDATE_SMEM, "bucket sort exceeds the update kernel's smem");
+
+struct BucketSort {
+    const uint32_t *qoff;   // first bucket of each graph, G + 1
+    const uint32_t *qtoff;  // first item of each graph, G + 1
+    uint32_t nq;            // buckets of all graphs
+    uint32_t *qcnt;         // keys per bucket (zero at launch, zeroed again after use)
+    uint32_t *qstart;       // bucket offsets within their scan chunk
+    uint32_t *rank;         // per batch key: its rank in its bucket
+    uint32_t *idx;          // per scattered key: its batch index
+    uint32_t *bfirst;       // per scattered key: its bucket's first position
+    uint32_t *bsize;        // per scattered key: its bucket's size
+};
+
+// Bucket of `key` within its graph: the slot row_offset[src] + (row length x
+// column) >> qbits (qbits: bits of the largest column), shifted right by
+// qshift and capped at qnbm1; keys of rows past row_num go to the last bucket.
+// Monotone in the key (a row's interpolated slots stay below the next row's
+// first), so buckets in order hold keys in order.
+__device__ __forceinline__ uint32_t bucket_of(uint64_t key, const GraphDesc &D) {
+    const uint32_t src = (uint32_t)(key >> 32);
+    if (src >= D.row_num)
+        return D.qnbm1;
+    const uint64_t a = D.row_offset[src], e = D.row_offset[src + 1];
+    const uint64_t dmax = (1ull << D.qbits) - 1;
+    const uint64_t dst = key & 0xFFFFFFFFull;
+    const uint64_t slot = a + (((e - a) * (dst < dmax ? dst : dmax)) >> D.qbits);
+    const uint64_t b = slot >> D.qshift;
+    return b < D.qnbm1 ? (uint32_t)b : D.qnbm1;
+}
+
+__device__ __forceinline__ uint32_t bucket_global(const GraphDesc *gd, const BucketSort &Q, uint32_t g, uint64_t key) {
+    return Q.qoff[g] + bucket_of(key, gd[g]);
+}
+
+__device__ __forceinline__ void bsort_range(uint32_t n, uint32_t &lo, uint32_t &hi) {
+    const uint32_t per = (n + gridDim.x - 1) / gridDim.x;
+    lo = min(n, blockIdx.x * per);
+    hi = min(n, lo + per);
+}
+
+// Graph of batch position i for a thread walking upwards from graph g (a
+// search only for the first position).
+__device__ __forceinline__ uint32_t graph_at(const uint32_t *boff, uint32_t G, uint32_t i, uint32_t g) {
+    if (G == 1)
+        return 0;
+    if (g == 0xFFFFFFFFu)
+        return segment_of(boff, G, i);
+    while (boff[g + 1] <= i)
+        ++g;
+    return g;
+}
+
+// Q1: ranks (and the reserved-column check of the digit histogram).
+__device__ void bsort_rank(const uint64_t *keys, const uint32_t *boff, uint32_t G, const GraphDesc *gd,
+                           const BucketSort &Q, DeviceStatus *st, bool check_keys) {
+    uint32_t lo, hi;
+    bsort_range(boff[G], lo, hi);
+    uint32_t bad = 0, g = 0xFFFFFFFFu;
+    for (uint32_t i0 = lo + threadIdx.x; i0 < hi; i0 += BSORT_ILP * BLOCK) {
+        uint64_t k[BSORT_ILP];
+        uint32_t b[BSORT_ILP], r[BSORT_ILP];
+#pragma unroll
+        for (int j = 0; j < BSORT_ILP; ++j) {
+            const uint32_t i = i0 + j * BLOCK;
+            k[j] = i < hi ? keys[i] : 0ull;
+        }
+#pragma unroll
+        for (int j = 0; j < BSORT_ILP; ++j) {
+            const uint32_t i = i0 + j * BLOCK;
+            if (i < hi) {
+                bad |= (uint32_t)((k[j] & COL_NONE) == COL_NONE);
+                g = graph_at(boff, G, i, g);
+                b[j] = bucket_global(gd, Q, g, k[j]);
+            }
+        }
+        // all atomics in flight before the first rank is stored
+#pragma unroll
+        for (int j = 0; j < BSORT_ILP; ++j)
+            if (i0 + j * BLOCK < hi)
+                r[j] = atomicAdd(Q.qcnt + b[j], 1u);
+#pragma unroll
+        for (int j = 0; j < BSORT_ILP; ++j)
+            if (i0 + j * BLOCK < hi)
+                Q.rank[i0 + j * BLOCK] = r[j];
+    }
+    if (__syncthreads_or(bad) && check_keys && threadIdx.x == 0)
+        atomicOr(&st->invalid_keys, 1u);
+}
+
+// Q2: chunk-local exclusive offsets of the buckets, the chunk's total into
+// chunk_tot[blockIdx.x]; flags the fallback when a bucket is too large.
+__device__ void bsort_scan(const BucketSort &Q, uint32_t *chunk_tot, DeviceStatus *st, uint32_t *tmp) {
+    const uint32_t per = (Q.nq + gridDim.x - 1) / gridDim.x;
+    const uint32_t b0 = min(Q.nq, blockIdx.x * per), b1 = min(Q.nq, b0 + per);
+    uint32_t run = 0, big = 0;
+    for (uint32_t x = b0; x < b1; x += BLOCK) {
+        const uint32_t b = x + threadIdx.x;
+        const uint32_t c = b < b1 ? __ldcg(Q.qcnt + b) : 0u;
+        big |= (uint32_t)(c > BSORT_MAX_BUCKET);
+        uint32_t tot;
+        const uint32_t ex = block_excl_scan(c, &tot, tmp);
+        if (b < b1)
+            Q.qstart[b] = run + ex;
+        run += tot;
+    }
+    if (threadIdx.x == 0)
+        chunk_tot[blockIdx.x] = run;
+    if (__syncthreads_or(big) && threadIdx.x == 0)
+        atomicOr(&st->sort_fallback, 1u);
+}
+
+// Exclusive prefix of the chunk totals into shared memory (gridDim.x words).
+__device__ void bsort_chunk_prefix(const uint32_t *chunk_tot, uint32_t *cpre, uint32_t *tmp) {
+    uint32_t run = 0;
+    for (uint32_t x = 0; x < gridDim.x; x += BLOCK) {
+        const uint32_t j = x + threadIdx.x;
+        const uint32_t c = j < gridDim.x ? __ldcg(chunk_tot + j) : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_excl_scan(c, &tot, tmp);
+        if (j < gridDim.x)
+            cpre[j] = run + ex;
+        run += tot;
+    }
+    __syncthreads();
+}
+
+// First batch position of bucket b.
+__device__ __forceinline__ uint32_t bsort_start(const BucketSort &Q, const uint32_t *cpre, uint32_t per, uint32_t b) {
+    return cpre[b / per] + __ldcg(Q.qstart + b);
+}
+
+// Q3: scatter of keys (and batch indices) into their buckets' ranges.
+__device__ void bsort_scatter(const uint64_t *keys, uint64_t *out, const uint32_t *boff,
+                              uint32_t G, const GraphDesc *gd, const BucketSort &Q, const uint32_t *cpre) {
+    uint32_t lo, hi;
+    bsort_range(boff[G], lo, hi);
+    const uint32_t per = (Q.nq + gridDim.x - 1) / gridDim.x;
+    uint32_t g = 0xFFFFFFFFu;
+    for (uint32_t i0 = lo + threadIdx.x; i0 < hi; i0 += BSORT_ILP * BLOCK) {
+        uint64_t k[BSORT_ILP];
+        uint32_t r[BSORT_ILP], b[BSORT_ILP], f[BSORT_ILP], c[BSORT_ILP];
+#pragma unroll
+        for (int j = 0; j < BSORT_ILP; ++j) {
+            const uint32_t i = i0 + j * BLOCK;
+            k[j] = i < hi ? keys[i] : 0ull;
+            r[j] = i < hi ? Q.rank[i] : 0u;  // written by this thread in Q1
+        }
+#pragma unroll
+        for (int j = 0; j < BSORT_ILP; ++j) {
+            const uint32_t i = i0 + j * BLOCK;
+            if (i < hi) {
+                g = graph_at(boff, G, i, g);
+                b[j] = bucket_global(gd, Q, g, k[j]);
+                f[j] = bsort_start(Q, cpre, per, b[j]);
+                c[j] = __ldcg(Q.qcnt + b[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < BSORT_ILP; ++j) {
+            const uint32_t i = i0 + j * BLOCK;
+            if (i < hi) {
+                const uint32_t pos = f[j] + r[j];
+                out[pos] = k[j];
+                Q.idx[pos] = i;
+                Q.bfirst[pos] = f[j];
+                Q.bsize[pos] = c[j];
+            }
+        }
+    }
+}
+
+// Bitonic sort of s_k/s_i[0..N) (N a power of two) by (key, index).
+__device__ __forceinline__ void bsort_bitonic(uint64_t *s_k, uint32_t *s_i, uint32_t N) {
+    for (uint32_t k = 2; k <= N; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < (N >> 1); i += BLOCK) {
+                const uint32_t a = ((i & ~(j - 1)) << 1) | (i & (j - 1));
+                const uint32_t c = a + j;
+                const uint64_t ka = s_k[a], kc = s_k[c];
+                const uint32_t ia = s_i[a], ic = s_i[c];
+                const bool gt = ka > kc || (ka == kc && ia > ic);
+                if (gt == ((a & k) == 0)) {
+                    s_k[a] = kc;
+                    s_k[c] = ka;
+                    s_i[a] = ic;
+                    s_i[c] = ia;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Q4: sort of every item; keys sk -> out_k, values in_v (by batch index) -> out_v.
+__device__ void bsort_items(const uint64_t *sk, uint64_t *__restrict__ out_k, const uint8_t *__restrict__ in_v,
+                            uint8_t *__restrict__ out_v, const uint32_t *boff, uint32_t G, const BucketSort &Q,
+                            unsigned char *smem) {
+    uint64_t *s_k = reinterpret_cast<uint64_t *>(smem);
+    uint32_t *s_i = reinterpret_cast<uint32_t *>(smem + (size_t)BSORT_CAP * 8);
+    __shared__ uint32_t s_range[2];
+    const uint32_t items = Q.qtoff[G];
+    for (uint32_t t = blockIdx.x; t < items; t += gridDim.x) {
+        const uint32_t g = G == 1 ? 0u : segment_of(Q.qtoff, G, t);
+        if (threadIdx.x < 2) {
+            // the first bucket start at or after the item's nominal start
+            const uint32_t gh = boff[g + 1];
+            uint32_t p = boff[g] + (t - Q.qtoff[g] + threadIdx.x) * BSORT_ITEM;
+            if (p >= gh) {
+                p = gh;
+            } else {
+                const uint32_t f = __ldcg(Q.bfirst + p);
+                if (f != p)
+                    p = f + __ldcg(Q.bsize + p);
+            }
+            s_range[threadIdx.x] = p;
+        }
+        __syncthreads();
+        const uint32_t p0 = s_range[0], p1 = s_range[1];
+        __syncthreads();
+        const uint32_t m = p1 - p0;  // < BSORT_ITEM + BSORT_MAX_BUCKET = BSORT_CAP
+        if (m == 0)
+            continue;
+        uint32_t big = 0;
+        for (uint32_t r = threadIdx.x; r < m; r += BLOCK) {
+            s_k[r] = __ldcg(sk + p0 + r);
+            s_i[r] = __ldcg(Q.idx + p0 + r);
+            big |= (uint32_t)(__ldcg(Q.bsize + p0 + r) > BSORT_RANK_MAX);
+        }
+        if (!__syncthreads_or(big)) {
+            // place = bucket start + keys of the bucket ordered before this one
+            // (consecutive threads share a bucket: the scan reads broadcast)
+            for (uint32_t r = threadIdx.x; r < m; r += BLOCK) {
+                const uint64_t k = s_k[r];
+                const uint32_t i = s_i[r];
+                const uint32_t f = __ldcg(Q.bfirst + p0 + r) - p0;
+                const uint32_t e = f + __ldcg(Q.bsize + p0 + r);
+                uint32_t before = 0;
+                for (uint32_t q = f; q < e; ++q) {
+                    const uint64_t kq = s_k[q];
+                    before += (uint32_t)(kq < k || (kq == k && s_i[q] < i));
+                }
+                out_k[p0 + f + before] = k;
+                out_v[p0 + f + before] = in_v[i];
+            }
+        } else {
+            const uint32_t N = m <= 1 ? 1u : 1u << (32 - __clz(m - 1));
+            for (uint32_t r = m + threadIdx.x; r < N; r += BLOCK) {
+                s_k[r] = KEY_NONE;
+                s_i[r] = 0xFFFFFFFFu;  // pads sort after every real key
+            }
+            __syncthreads();
+            bsort_bitonic(s_k, s_i, N);
+            for (uint32_t r = threadIdx.x; r < m; r += BLOCK) {
+                out_k[p0 + r] = s_k[r];
+                out_v[p0 + r] = in_v[s_i[r]];
+            }
+        }
+        __syncthreads();
+    }
 }
 
 }  // namespace gpma

@@ -80,6 +80,7 @@ struct UpdateArgs {
     uint32_t *sort_hist;    // [G + 1][8][256] digit counts (zeroed per update)
     uint32_t *sort_tiles;   // 8 tile counters (zeroed per update)
     uint32_t *sort_status;  // look-back words, 8 x tiles x 256 (zeroed per update)
+    BucketSort q;           // bucket sort state (q.nq == 0: digit passes only)
     bool check_keys;
     uint32_t *leaf;
     uint64_t *ikeys[2];
@@ -815,37 +816,65 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             A.top[j] = D.heads[(size_t)j << hstep];
     }
 
-    // S: stable radix sort of each graph's batch (gpma.cuh:977); digit passes
-    // are separated by grid barriers, digits constant over all batches skipped.
-    sort_histogram(A.bk[0], A.boff, A.G, A.sort_hist, st, A.check_keys, reinterpret_cast<uint32_t *>(smem));
-    if (!grid_barrier(&st->bar, &st->err, A.stall, A.stall_limit_ns))
-        return;
-    if (ld_volatile(&st->invalid_keys) != 0)
-        return;  // reserved-column keys: reject the batch before any change
-    uint32_t sel = 0;
-    {
-        const uint32_t trivial = sort_trivial_mask(A.sort_hist + (size_t)(A.G == 1 ? 0 : A.G) * 2048, A.n);
-        const uint32_t tiles = A.toff[A.G];
-        for (int p = 0; p < 8; ++p) {
-            if (trivial & (1u << p))
-                continue;
-            const uint64_t *ink = sel ? A.bk[1] : A.bk[0];
-            const uint8_t *inv = sel ? A.bv[1] : A.bv[0];
-            uint64_t *outk = sel ? A.bk[0] : A.bk[1];
-            uint8_t *outv = sel ? A.bv[0] : A.bv[1];
-            // CTA b takes tiles b, b + G, b + 2G, ... in order: every look-back
-            // waits on lower tiles only, and the lowest unfinished tile never
-            // waits on anything unfinished, so the pass always progresses
-            for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
-                sort_tile(p, tile, ink, inv, outk, outv, A.boff, A.toff, A.G, A.sort_hist, A.sort_status, st, smem,
-                          tmp);
-            sel ^= 1u;
+    // S: stable sort of each graph's batch (gpma.cuh:977): the bucket sort,
+    // or digit passes separated by grid barriers (digits constant over all
+    // batches skipped) when it is off or a bucket is crowded.
+    const uint64_t *bk = A.bk[0];
+    const uint8_t *bv = A.bv[1];
+    bool digits = A.q.nq == 0;
+    if (!digits) {
+        bsort_rank(A.bk[0], A.boff, A.G, A.gd, A.q, st, A.check_keys);
+        if (!grid_barrier(&st->bar, &st->err, A.stall, A.stall_limit_ns))
+            return;
+        if (ld_volatile(&st->invalid_keys) != 0)
+            return;  // reserved-column keys: reject the batch before any change
+        bsort_scan(A.q, A.cta_cnt, st, tmp);
+        if (!grid_barrier(&st->bar, &st->err))
+            return;
+        digits = cta_broadcast_read(&st->sort_fallback) != 0;
+        if (!digits) {
+            // scatter bk[0] -> bk[1] (+ batch indices), then items bk[1] -> bk[0], values bv[0] -> bv[1]
+            uint32_t *cpre = reinterpret_cast<uint32_t *>(smem + BSORT_SMEM_ITEMS);
+            bsort_chunk_prefix(A.cta_cnt, cpre, tmp);
+            bsort_scatter(A.bk[0], A.bk[1], A.boff, A.G, A.gd, A.q, cpre);
+            if (!grid_barrier(&st->bar, &st->err))
+                return;
+            bsort_items(A.bk[1], A.bk[0], A.bv[0], A.bv[1], A.boff, A.G, A.q, smem);
             if (!grid_barrier(&st->bar, &st->err))
                 return;
         }
     }
-    const uint64_t *bk = sel ? A.bk[1] : A.bk[0];
-    const uint8_t *bv = sel ? A.bv[1] : A.bv[0];
+    if (digits) {
+        sort_histogram(A.bk[0], A.boff, A.G, A.sort_hist, st, A.check_keys, reinterpret_cast<uint32_t *>(smem));
+        if (!grid_barrier(&st->bar, &st->err, A.q.nq == 0 ? A.stall : 0u, A.stall_limit_ns))
+            return;
+        if (ld_volatile(&st->invalid_keys) != 0)
+            return;  // reserved-column keys: reject the batch before any change
+        uint32_t sel = 0;
+        {
+            const uint32_t trivial = sort_trivial_mask(A.sort_hist + (size_t)(A.G == 1 ? 0 : A.G) * 2048, A.n);
+            const uint32_t tiles = A.toff[A.G];
+            for (int p = 0; p < 8; ++p) {
+                if (trivial & (1u << p))
+                    continue;
+                const uint64_t *ink = sel ? A.bk[1] : A.bk[0];
+                const uint8_t *inv = sel ? A.bv[1] : A.bv[0];
+                uint64_t *outk = sel ? A.bk[0] : A.bk[1];
+                uint8_t *outv = sel ? A.bv[0] : A.bv[1];
+                // CTA b takes tiles b, b + G, b + 2G, ... in order: every look-back
+                // waits on lower tiles only, and the lowest unfinished tile never
+                // waits on anything unfinished, so the pass always progresses
+                for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
+                    sort_tile(p, tile, ink, inv, outk, outv, A.boff, A.toff, A.G, A.sort_hist, A.sort_status, st, smem,
+                              tmp);
+                sel ^= 1u;
+                if (!grid_barrier(&st->bar, &st->err))
+                    return;
+            }
+        }
+        bk = sel ? A.bk[1] : A.bk[0];
+        bv = sel ? A.bv[1] : A.bv[0];
+    }
     const uint32_t G = gridDim.x;
 
     uint32_t scan_id = 0;
@@ -914,6 +943,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             A.sort_hist[i] = 0;
         for (uint32_t i = gt; i < A.status_words; i += nt)
             A.sort_status[i] = 0;
+        for (uint32_t i = gt; i < A.q.nq; i += nt)
+            A.q.qcnt[i] = 0;
         if (gt < 8)
             A.sort_tiles[gt] = 0;
         for (uint32_t i = gt; i < A.next_slot_words; i += nt)
@@ -2196,6 +2227,8 @@ void free_buffers(BatchBuffers &b) {
     dev_free(b.top);
     dev_free(b.sort_status);
     dev_free(b.sort_hist);
+    dev_free(b.qcnt);
+    dev_free(b.qstart);
     dev_free(b.d_tab);
     dev_free(b.d_stat);
     dev_free(b.chunk_cnt);
@@ -2207,7 +2240,7 @@ void free_buffers(BatchBuffers &b) {
     b.h_tab = nullptr;
     b.h_stat = nullptr;
     b.gd = nullptr;
-    b.boff = b.toff = nullptr;
+    b.boff = b.toff = b.qoff = b.qtoff = nullptr;
     b.stat_slot = 0;
     b.dirty = true;
     b.cap = 0;
@@ -2215,6 +2248,7 @@ void free_buffers(BatchBuffers &b) {
     b.hist_cap = 0;
     b.chunk_cap = 0;
     b.sort_status_cap = 0;
+    b.q_cap = 0;
 }
 
 gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
@@ -2275,9 +2309,9 @@ gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
             cudaFreeHost(b.h_stat);
         b.h_tab = b.h_stat = nullptr;
         b.gd = nullptr;
-        b.boff = b.toff = nullptr;
+        b.boff = b.toff = b.qoff = b.qtoff = nullptr;
         b.gcap = 0;
-        const size_t tab = sizeof(GraphDesc) * gc + 2 * sizeof(uint32_t) * (gc + 1);
+        const size_t tab = sizeof(GraphDesc) * gc + 4 * sizeof(uint32_t) * (gc + 1);
         const size_t slot = (STAT_GS_OFFSET + sizeof(GraphStatus) * gc + 255) & ~size_t(255);
         GPMA_TRY(dev_alloc(&b.d_tab, tab));
         GPMA_TRY(dev_alloc(&b.d_stat, 2 * slot));
@@ -2289,6 +2323,8 @@ gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
         b.gd = reinterpret_cast<GraphDesc *>(b.d_tab);
         b.boff = reinterpret_cast<uint32_t *>(b.d_tab + sizeof(GraphDesc) * gc);
         b.toff = b.boff + gc + 1;
+        b.qoff = b.toff + gc + 1;
+        b.qtoff = b.qoff + gc + 1;
         b.stat_slot = slot;
         b.parity = 0;
         b.dirty = true;
@@ -2339,6 +2375,36 @@ gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t
             h_toff[i] = h_toff[i - 1] + (uint32_t)((ni + SORT_TILE - 1) / SORT_TILE);
         }
     }
+    // bucket sort: per graph, 2^qlog equal slot ranges (about BSORT_AVG keys
+    // each) and one item per BSORT_ITEM keys
+    uint32_t *h_qoff = h_toff + buf.gcap + 1;
+    uint32_t *h_qtoff = h_qoff + buf.gcap + 1;
+    const bool buckets = g_tuning.update_sort == 0 && (uint32_t)grid <= BSORT_MAX_GRID;
+    uint64_t nq = 0;
+    h_qoff[0] = h_qtoff[0] = 0;
+    for (uint32_t i = 0; i < k; ++i) {
+        const uint64_t ni = off[i + 1] - off[i];
+        const uint32_t rows = graphs[i]->row_num;
+        const uint32_t lsize = graphs[i]->geo.size ? fls32(graphs[i]->geo.size) - 1 : 0;  // size: a power of two
+        uint32_t qlog = 0;
+        while (qlog < lsize && (uint64_t(BSORT_AVG) << qlog) < ni)
+            ++qlog;
+        h_gd[i].qbits = std::max<uint32_t>(1, fls32(rows > 2 ? rows - 1 : 1));  // columns < 2^qbits
+        h_gd[i].qshift = lsize - qlog;
+        h_gd[i].qnbm1 = (1u << qlog) - 1;
+        nq += ni ? (1ull << qlog) : 0;
+        h_qoff[i + 1] = (uint32_t)nq;
+        h_qtoff[i + 1] = h_qtoff[i] + (uint32_t)((ni + BSORT_ITEM - 1) / BSORT_ITEM);
+    }
+    if (buckets && nq > buf.q_cap) {
+        dev_free(buf.qcnt);
+        dev_free(buf.qstart);
+        buf.q_cap = 0;
+        GPMA_TRY(dev_alloc(&buf.qcnt, nq));
+        GPMA_TRY(dev_alloc(&buf.qstart, nq));
+        buf.q_cap = nq;
+        buf.dirty = true;
+    }
     const uint32_t tiles = h_toff[k];
     const uint64_t status_words = 8ull * tiles * 256;
     if (status_words > buf.sort_status_cap) {
@@ -2360,7 +2426,7 @@ gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t
         buf.chunk_cap = chunk_need;
     }
     // the upload covers the tables up to the last tile offset in use
-    *tab_bytes = reinterpret_cast<unsigned char *>(h_toff + k + 1) - buf.h_tab;
+    *tab_bytes = reinterpret_cast<unsigned char *>(h_qtoff + k + 1) - buf.h_tab;
     unsigned char *slot = buf.d_stat + buf.parity * buf.stat_slot;
     unsigned char *next = buf.d_stat + (buf.parity ^ 1) * buf.stat_slot;
     UpdateArgs A;
@@ -2386,6 +2452,17 @@ gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t
     A.sort_hist = buf.sort_hist;
     A.sort_tiles = buf.sort_tiles;
     A.sort_status = buf.sort_status;
+    if (buckets && n > 0) {
+        A.q.qoff = buf.qoff;
+        A.q.qtoff = buf.qtoff;
+        A.q.nq = (uint32_t)nq;
+        A.q.qcnt = buf.qcnt;
+        A.q.qstart = buf.qstart;
+        A.q.rank = buf.ileaf;  // all four first written after the sort
+        A.q.idx = buf.leaf;
+        A.q.bfirst = buf.wa[0];
+        A.q.bsize = buf.wb[0];
+    }
     A.check_keys = check_keys;
     A.leaf = buf.leaf;
     A.rkeys = buf.rkeys;
@@ -2417,6 +2494,8 @@ gpma_status update_clear(BatchBuffers &buf, cudaStream_t s) {
     GPMA_CUDA(cudaMemsetAsync(buf.sort_hist, 0, sizeof(uint32_t) * buf.hist_cap * 2048, s));
     GPMA_CUDA(cudaMemsetAsync(buf.sort_tiles, 0, 8 * sizeof(uint32_t), s));
     GPMA_CUDA(cudaMemsetAsync(buf.sort_status, 0, buf.sort_status_cap * sizeof(uint32_t), s));
+    if (buf.q_cap)
+        GPMA_CUDA(cudaMemsetAsync(buf.qcnt, 0, buf.q_cap * sizeof(uint32_t), s));
     buf.dirty = false;
     return GPMA_OK;
 }
@@ -2441,6 +2520,7 @@ gpma_status update_finish(gpma_graph *const *graphs, uint32_t k, BatchBuffers &b
         prof->locate_ms += span(1, 2);
         prof->group_ms += span(2, 3);
         prof->levels_ms += span(3, 4);
+        prof->sort_fallbacks += h.sort_fallback != 0;
     }
     if (h.invalid_keys) {
         set_error("update batch holds keys whose column is 0xFFFFFFFF (reserved for row guards and empty slots)");

@@ -420,7 +420,7 @@ GPMA_API gpma_status gpma_validate(gpma_graph *g, uint64_t *bad, void *stream);
  * No reference counterpart (the reference printed wall-clock deltas,
  * rdebug.hpp:8-17). */
 typedef struct gpma_profile {
-    double sort_ms;          /* inside the update kernel: batch radix sort */
+    double sort_ms;          /* inside the update kernel: batch sort */
     double locate_ms;        /* inside the update kernel: leaf locate + delete/modify */
     double group_ms;         /* inside the update kernel: insertion compaction + grouping */
     double levels_ms;        /* inside the update kernel: the level loop */
@@ -431,6 +431,8 @@ typedef struct gpma_profile {
     uint64_t bfs_kernels;    /* launches of BFS traversal kernels */
     uint64_t kernel_launches;
     uint64_t bfs_edges;      /* edges scanned from reached nodes by multi-source BFS, summed over sources */
+    uint64_t sort_fallbacks; /* update launches whose bucket sort met a bucket of more than 3072 keys and
+                                sorted by digit passes instead */
 } gpma_profile;
 GPMA_API gpma_status gpma_set_profiling(gpma_graph *g, int enabled);
 GPMA_API gpma_status gpma_get_profile(const gpma_graph *g, gpma_profile *out);
@@ -461,7 +463,11 @@ typedef struct gpma_tuning {
     uint32_t ms_blocks_per_sm;     /* multi-source BFS grid */
     uint32_t update_blocks_per_sm; /* persistent update kernel: 1-2 use the 128-register build, 3 the 80-register
                                       one (more warps, some spills); 0 lets each launch choose (3 from 1M keys) */
-    uint32_t reserved[3];
+    uint32_t update_sort;          /* batch sort inside the update kernel: 0 buckets (equal slot ranges of the
+                                      array, a key placed by its row's slots) ranked, scattered and sorted in
+                                      shared memory, with the digit passes taken when one bucket holds more than
+                                      3072 keys; 1 digit passes always */
+    uint32_t reserved[2];
 } gpma_tuning;
 GPMA_API gpma_status gpma_get_tuning(gpma_tuning *out);
 GPMA_API gpma_status gpma_set_tuning(const gpma_tuning *t);
