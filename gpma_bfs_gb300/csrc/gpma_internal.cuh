@@ -168,8 +168,12 @@ struct BatchBuffers {
     uint32_t *sort_hist = nullptr;     // [graph][8][256] digit counts
     uint32_t hist_cap = 0;             // graphs
     uint32_t *qcnt = nullptr;          // bucket sort: keys per bucket (zeroed per update)
-    uint32_t *qstart = nullptr;        // bucket sort: bucket offsets within their scan chunk
+    uint64_t *qinfo = nullptr;         // bucket sort: offset within the scan chunk | count << 32
     uint64_t q_cap = 0;                // buckets
+    uint64_t *qrec = nullptr;          // bucket sort: 16-byte records (two words per key)
+    uint64_t qrec_cap = 0;             // keys
+    uint32_t *qbound = nullptr;        // bucket sort: first position of every item
+    uint64_t qbound_cap = 0;           // items
     // per-graph tables, one upload per launch from pinned memory:
     // [GraphDesc x gcap][batch offsets x (gcap + 1)][sort tile offsets x (gcap + 1)]
     // [bucket offsets x (gcap + 1)][bucket-sort item offsets x (gcap + 1)]

@@ -242,43 +242,50 @@ __device__ void sort_tile(int pass, uint32_t tile, const uint64_t *__restrict__ 
 // its row's slots fall in, interpolated linearly by its column (bucket_of).
 // Rows hold slots in proportion to their degree, so power-law hub rows spread
 // over several buckets as long as the batch follows the graph's own degrees
-// (a sliding window does). Four phases, one grid barrier after each:
-//   Q1 every key takes a rank in its bucket (one atomic per key);
+// (a sliding window does). Four phases, one grid barrier after each; every
+// key costs about three scattered 32-byte sectors (its row's offsets, its
+// bucket's atomic, its record), the rest is coalesced:
+//   Q1 every key takes a rank in its bucket (one atomic per key); rank and
+//      bucket are stored per key;
 //   Q2 the bucket counts are scanned chunk by chunk (one chunk per CTA); a
 //      bucket of more than BSORT_MAX_BUCKET keys sends the launch to the digit
 //      passes;
-//   Q3 every key is written to its bucket's range at its rank, with its batch
-//      index and its bucket's first position and size;
+//   Q3 every key's record (key, batch index, bucket, value: 16 bytes) is
+//      written to its bucket's range at its rank; the key that lands on an
+//      item's nominal start records the item's bound;
 //   Q4 items of whole buckets (item j of a graph holds the buckets that start
-//      in [j, j + 1) * BSORT_ITEM of its range, at most BSORT_CAP keys) are
-//      staged in shared memory; each key's place in its bucket is the number
-//      of keys of the bucket before it in (key, batch index) order (a bucket
+//      in [j, j + 1) * BSORT_ITEM of its range, fewer than BSORT_CAP keys) are
+//      staged in shared memory; a key's place in its bucket is the number of
+//      keys of the bucket before it in (key, batch index) order (a bucket
 //      holds a few dozen keys), or, in an item with a bucket of more than
-//      BSORT_RANK_MAX keys, the item is sorted by a bitonic network; each
-//      value is gathered by its batch index.
+//      BSORT_RANK_MAX keys, the item is sorted by a bitonic network.
 // Equal keys end in batch order, so the result is the stable sort's whatever
 // order the ranks were taken in.
 constexpr uint32_t BSORT_ITEM = 1024;
-constexpr uint32_t BSORT_CAP = 4 * BSORT_ITEM;
-constexpr uint32_t BSORT_MAX_BUCKET = BSORT_CAP - BSORT_ITEM;
+constexpr uint32_t BSORT_MAX_BUCKET = 1024;
+constexpr uint32_t BSORT_CAP = BSORT_ITEM + BSORT_MAX_BUCKET;
 constexpr uint32_t BSORT_AVG = 32;
 constexpr uint32_t BSORT_RANK_MAX = 256;
+constexpr uint32_t BSORT_MAX_BUCKETS = 1u << 24;  // bucket ids share a word with the value
 constexpr int BSORT_ILP = 4;
-constexpr size_t BSORT_SMEM_ITEMS = (size_t)BSORT_CAP * 12;  // keys, then indices
-// the chunk prefix (one word per CTA) follows the item in shared memory
-constexpr uint32_t BSORT_MAX_GRID = (uint32_t)((UPDATE_SMEM - BSORT_SMEM_ITEMS) / 4);
-static_assert(BSORT_SMEM_ITEMS < UPDATE_SMEM, "bucket sort exceeds the update kernel's smem");
+constexpr uint32_t BSORT_PER_THREAD = BSORT_CAP / BLOCK;  // item entries per thread
+// Q4 stages the item (a key, a packed word and the bucket's place in the item
+// per entry) in shared memory, followed by the chunk prefix (one word per
+// CTA) that Q3 and Q4 read
+constexpr size_t BSORT_SMEM_ITEM = (size_t)BSORT_CAP * 20;
+constexpr uint32_t BSORT_MAX_GRID = (uint32_t)((UPDATE_SMEM - BSORT_SMEM_ITEM) / 4);
+static_assert(BSORT_SMEM_ITEM < UPDATE_SMEM && BSORT_CAP % BLOCK == 0, "bucket sort item layout");
 
 struct BucketSort {
     const uint32_t *qoff;   // first bucket of each graph, G + 1
     const uint32_t *qtoff;  // first item of each graph, G + 1
-    uint32_t nq;            // buckets of all graphs
+    uint32_t nq;            // buckets of all graphs (< BSORT_MAX_BUCKETS)
     uint32_t *qcnt;         // keys per bucket (zero at launch, zeroed again after use)
-    uint32_t *qstart;       // bucket offsets within their scan chunk
+    unsigned long long *qinfo;  // per bucket: offset within its scan chunk | count << 32
     uint32_t *rank;         // per batch key: its rank in its bucket
-    uint32_t *idx;          // per scattered key: its batch index
-    uint32_t *bfirst;       // per scattered key: its bucket's first position
-    uint32_t *bsize;        // per scattered key: its bucket's size
+    uint32_t *bkt;          // per batch key: its bucket
+    uint4 *rec;             // per sorted position: key (x, y), batch index (z), bucket << 8 | value (w)
+    uint32_t *bound;        // per item: its first position
 };
 
 // Bucket of `key` within its graph: the slot row_offset[src] + (row length x
@@ -296,10 +303,6 @@ __device__ __forceinline__ uint32_t bucket_of(uint64_t key, const GraphDesc &D) 
     const uint64_t slot = a + (((e - a) * (dst < dmax ? dst : dmax)) >> D.qbits);
     const uint64_t b = slot >> D.qshift;
     return b < D.qnbm1 ? (uint32_t)b : D.qnbm1;
-}
-
-__device__ __forceinline__ uint32_t bucket_global(const GraphDesc *gd, const BucketSort &Q, uint32_t g, uint64_t key) {
-    return Q.qoff[g] + bucket_of(key, gd[g]);
 }
 
 __device__ __forceinline__ void bsort_range(uint32_t n, uint32_t &lo, uint32_t &hi) {
@@ -320,7 +323,7 @@ __device__ __forceinline__ uint32_t graph_at(const uint32_t *boff, uint32_t G, u
     return g;
 }
 
-// Q1: ranks (and the reserved-column check of the digit histogram).
+// Q1: ranks and buckets (and the reserved-column check of the digit histogram).
 __device__ void bsort_rank(const uint64_t *keys, const uint32_t *boff, uint32_t G, const GraphDesc *gd,
                            const BucketSort &Q, DeviceStatus *st, bool check_keys) {
     uint32_t lo, hi;
@@ -340,7 +343,7 @@ __device__ void bsort_rank(const uint64_t *keys, const uint32_t *boff, uint32_t 
             if (i < hi) {
                 bad |= (uint32_t)((k[j] & COL_NONE) == COL_NONE);
                 g = graph_at(boff, G, i, g);
-                b[j] = bucket_global(gd, Q, g, k[j]);
+                b[j] = Q.qoff[g] + bucket_of(k[j], gd[g]);
             }
         }
         // all atomics in flight before the first rank is stored
@@ -349,16 +352,20 @@ __device__ void bsort_rank(const uint64_t *keys, const uint32_t *boff, uint32_t 
             if (i0 + j * BLOCK < hi)
                 r[j] = atomicAdd(Q.qcnt + b[j], 1u);
 #pragma unroll
-        for (int j = 0; j < BSORT_ILP; ++j)
-            if (i0 + j * BLOCK < hi)
-                Q.rank[i0 + j * BLOCK] = r[j];
+        for (int j = 0; j < BSORT_ILP; ++j) {
+            const uint32_t i = i0 + j * BLOCK;
+            if (i < hi) {
+                Q.rank[i] = r[j];
+                Q.bkt[i] = b[j];
+            }
+        }
     }
     if (__syncthreads_or(bad) && check_keys && threadIdx.x == 0)
         atomicOr(&st->invalid_keys, 1u);
 }
 
-// Q2: chunk-local exclusive offsets of the buckets, the chunk's total into
-// chunk_tot[blockIdx.x]; flags the fallback when a bucket is too large.
+// Q2: chunk-local exclusive offsets and counts of the buckets, the chunk's
+// total into chunk_tot[blockIdx.x]; flags the fallback when a bucket is too large.
 __device__ void bsort_scan(const BucketSort &Q, uint32_t *chunk_tot, DeviceStatus *st, uint32_t *tmp) {
     const uint32_t per = (Q.nq + gridDim.x - 1) / gridDim.x;
     const uint32_t b0 = min(Q.nq, blockIdx.x * per), b1 = min(Q.nq, b0 + per);
@@ -370,7 +377,7 @@ __device__ void bsort_scan(const BucketSort &Q, uint32_t *chunk_tot, DeviceStatu
         uint32_t tot;
         const uint32_t ex = block_excl_scan(c, &tot, tmp);
         if (b < b1)
-            Q.qstart[b] = run + ex;
+            Q.qinfo[b] = (unsigned long long)(run + ex) | ((unsigned long long)c << 32);
         run += tot;
     }
     if (threadIdx.x == 0)
@@ -394,66 +401,61 @@ __device__ void bsort_chunk_prefix(const uint32_t *chunk_tot, uint32_t *cpre, ui
     __syncthreads();
 }
 
-// First batch position of bucket b.
-__device__ __forceinline__ uint32_t bsort_start(const BucketSort &Q, const uint32_t *cpre, uint32_t per, uint32_t b) {
-    return cpre[b / per] + __ldcg(Q.qstart + b);
-}
-
-// Q3: scatter of keys (and batch indices) into their buckets' ranges.
-__device__ void bsort_scatter(const uint64_t *keys, uint64_t *out, const uint32_t *boff,
-                              uint32_t G, const GraphDesc *gd, const BucketSort &Q, const uint32_t *cpre) {
+// Q3: every key's record into its bucket's range; item bounds.
+__device__ void bsort_scatter(const uint64_t *keys, const uint8_t *vals, const uint32_t *boff, uint32_t G,
+                              const BucketSort &Q, const uint32_t *cpre) {
     uint32_t lo, hi;
     bsort_range(boff[G], lo, hi);
     const uint32_t per = (Q.nq + gridDim.x - 1) / gridDim.x;
     uint32_t g = 0xFFFFFFFFu;
     for (uint32_t i0 = lo + threadIdx.x; i0 < hi; i0 += BSORT_ILP * BLOCK) {
         uint64_t k[BSORT_ILP];
-        uint32_t r[BSORT_ILP], b[BSORT_ILP], f[BSORT_ILP], c[BSORT_ILP];
+        uint32_t r[BSORT_ILP], b[BSORT_ILP], v[BSORT_ILP];
+        unsigned long long inf[BSORT_ILP];
 #pragma unroll
         for (int j = 0; j < BSORT_ILP; ++j) {
             const uint32_t i = i0 + j * BLOCK;
-            k[j] = i < hi ? keys[i] : 0ull;
-            r[j] = i < hi ? Q.rank[i] : 0u;  // written by this thread in Q1
+            const bool ok = i < hi;
+            k[j] = ok ? keys[i] : 0ull;
+            v[j] = ok ? vals[i] : 0u;
+            r[j] = ok ? Q.rank[i] : 0u;  // both written by this thread in Q1
+            b[j] = ok ? Q.bkt[i] : 0u;
         }
+#pragma unroll
+        for (int j = 0; j < BSORT_ILP; ++j)
+            inf[j] = i0 + j * BLOCK < hi ? __ldcg(Q.qinfo + b[j]) : 0ull;
 #pragma unroll
         for (int j = 0; j < BSORT_ILP; ++j) {
             const uint32_t i = i0 + j * BLOCK;
             if (i < hi) {
+                const uint32_t f = cpre[b[j] / per] + (uint32_t)inf[j];
+                const uint32_t pos = f + r[j];
+                Q.rec[pos] = make_uint4((uint32_t)k[j], (uint32_t)(k[j] >> 32), i, (b[j] << 8) | v[j]);
                 g = graph_at(boff, G, i, g);
-                b[j] = bucket_global(gd, Q, g, k[j]);
-                f[j] = bsort_start(Q, cpre, per, b[j]);
-                c[j] = __ldcg(Q.qcnt + b[j]);
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < BSORT_ILP; ++j) {
-            const uint32_t i = i0 + j * BLOCK;
-            if (i < hi) {
-                const uint32_t pos = f[j] + r[j];
-                out[pos] = k[j];
-                Q.idx[pos] = i;
-                Q.bfirst[pos] = f[j];
-                Q.bsize[pos] = c[j];
+                const uint32_t rel = pos - boff[g];
+                if (rel % BSORT_ITEM == 0)  // the item starts at the first bucket start at or after here
+                    Q.bound[Q.qtoff[g] + rel / BSORT_ITEM] = f == pos ? pos : f + (uint32_t)(inf[j] >> 32);
             }
         }
     }
 }
 
-// Bitonic sort of s_k/s_i[0..N) (N a power of two) by (key, index).
-__device__ __forceinline__ void bsort_bitonic(uint64_t *s_k, uint32_t *s_i, uint32_t N) {
+// Bitonic sort of s_k/s_x[0..N) (N a power of two) by (key, x); x holds the
+// batch index in its high half, so equal keys order by batch index.
+__device__ __forceinline__ void bsort_bitonic(uint64_t *s_k, uint64_t *s_x, uint32_t N) {
     for (uint32_t k = 2; k <= N; k <<= 1) {
         for (uint32_t j = k >> 1; j > 0; j >>= 1) {
             for (uint32_t i = threadIdx.x; i < (N >> 1); i += BLOCK) {
                 const uint32_t a = ((i & ~(j - 1)) << 1) | (i & (j - 1));
                 const uint32_t c = a + j;
                 const uint64_t ka = s_k[a], kc = s_k[c];
-                const uint32_t ia = s_i[a], ic = s_i[c];
-                const bool gt = ka > kc || (ka == kc && ia > ic);
+                const uint64_t xa = s_x[a], xc = s_x[c];
+                const bool gt = ka > kc || (ka == kc && xa > xc);
                 if (gt == ((a & k) == 0)) {
                     s_k[a] = kc;
                     s_k[c] = ka;
-                    s_i[a] = ic;
-                    s_i[c] = ia;
+                    s_x[a] = xc;
+                    s_x[c] = xa;
                 }
             }
             __syncthreads();
@@ -461,28 +463,22 @@ __device__ __forceinline__ void bsort_bitonic(uint64_t *s_k, uint32_t *s_i, uint
     }
 }
 
-// Q4: sort of every item; keys sk -> out_k, values in_v (by batch index) -> out_v.
-__device__ void bsort_items(const uint64_t *sk, uint64_t *__restrict__ out_k, const uint8_t *__restrict__ in_v,
-                            uint8_t *__restrict__ out_v, const uint32_t *boff, uint32_t G, const BucketSort &Q,
-                            unsigned char *smem) {
+// Q4: sort of every item into out_k / out_v. Thread t holds entries t + j *
+// BLOCK of the item; every global load of a step is issued before the first
+// use, and entries live in shared memory between steps.
+__device__ void bsort_items(uint64_t *__restrict__ out_k, uint8_t *__restrict__ out_v, const uint32_t *boff,
+                            uint32_t G, const BucketSort &Q, const uint32_t *cpre, unsigned char *smem) {
     uint64_t *s_k = reinterpret_cast<uint64_t *>(smem);
-    uint32_t *s_i = reinterpret_cast<uint32_t *>(smem + (size_t)BSORT_CAP * 8);
+    uint64_t *s_x = reinterpret_cast<uint64_t *>(smem + (size_t)BSORT_CAP * 8);  // index << 32 | bucket << 8 | value
+    uint32_t *s_b = reinterpret_cast<uint32_t *>(smem + (size_t)BSORT_CAP * 16);  // bucket: first | size << 16
     __shared__ uint32_t s_range[2];
+    const uint32_t per = (Q.nq + gridDim.x - 1) / gridDim.x;
     const uint32_t items = Q.qtoff[G];
     for (uint32_t t = blockIdx.x; t < items; t += gridDim.x) {
-        const uint32_t g = G == 1 ? 0u : segment_of(Q.qtoff, G, t);
         if (threadIdx.x < 2) {
-            // the first bucket start at or after the item's nominal start
-            const uint32_t gh = boff[g + 1];
-            uint32_t p = boff[g] + (t - Q.qtoff[g] + threadIdx.x) * BSORT_ITEM;
-            if (p >= gh) {
-                p = gh;
-            } else {
-                const uint32_t f = __ldcg(Q.bfirst + p);
-                if (f != p)
-                    p = f + __ldcg(Q.bsize + p);
-            }
-            s_range[threadIdx.x] = p;
+            const uint32_t g = G == 1 ? 0u : segment_of(Q.qtoff, G, t);
+            s_range[threadIdx.x] = threadIdx.x == 0 || t + 1 < Q.qtoff[g + 1] ? __ldcg(Q.bound + t + threadIdx.x)
+                                                                               : boff[g + 1];
         }
         __syncthreads();
         const uint32_t p0 = s_range[0], p1 = s_range[1];
@@ -491,38 +487,73 @@ __device__ void bsort_items(const uint64_t *sk, uint64_t *__restrict__ out_k, co
         if (m == 0)
             continue;
         uint32_t big = 0;
-        for (uint32_t r = threadIdx.x; r < m; r += BLOCK) {
-            s_k[r] = __ldcg(sk + p0 + r);
-            s_i[r] = __ldcg(Q.idx + p0 + r);
-            big |= (uint32_t)(__ldcg(Q.bsize + p0 + r) > BSORT_RANK_MAX);
+        {
+            uint4 e[BSORT_PER_THREAD];
+#pragma unroll
+            for (uint32_t j = 0; j < BSORT_PER_THREAD; ++j) {
+                const uint32_t r = threadIdx.x + j * BLOCK;
+                if (r < m)
+                    e[j] = __ldcg(Q.rec + p0 + r);
+            }
+            unsigned long long qi[BSORT_PER_THREAD];
+#pragma unroll
+            for (uint32_t j = 0; j < BSORT_PER_THREAD; ++j) {
+                const uint32_t r = threadIdx.x + j * BLOCK;
+                if (r < m) {
+                    s_k[r] = ((uint64_t)e[j].y << 32) | e[j].x;
+                    s_x[r] = ((uint64_t)e[j].z << 32) | e[j].w;
+                    qi[j] = __ldcg(Q.qinfo + (e[j].w >> 8));
+                }
+            }
+#pragma unroll
+            for (uint32_t j = 0; j < BSORT_PER_THREAD; ++j) {
+                const uint32_t r = threadIdx.x + j * BLOCK;
+                if (r < m) {
+                    const uint32_t size = (uint32_t)(qi[j] >> 32);
+                    const uint32_t first = cpre[(e[j].w >> 8) / per] + (uint32_t)qi[j] - p0;
+                    s_b[r] = first | (size << 16);  // both <= BSORT_CAP
+                    big |= (uint32_t)(size > BSORT_RANK_MAX);
+                }
+            }
         }
         if (!__syncthreads_or(big)) {
-            // place = bucket start + keys of the bucket ordered before this one
-            // (consecutive threads share a bucket: the scan reads broadcast)
+            // place = first slot of the bucket + its keys ordered before this one
             for (uint32_t r = threadIdx.x; r < m; r += BLOCK) {
-                const uint64_t k = s_k[r];
-                const uint32_t i = s_i[r];
-                const uint32_t f = __ldcg(Q.bfirst + p0 + r) - p0;
-                const uint32_t e = f + __ldcg(Q.bsize + p0 + r);
-                uint32_t before = 0;
-                for (uint32_t q = f; q < e; ++q) {
-                    const uint64_t kq = s_k[q];
-                    before += (uint32_t)(kq < k || (kq == k && s_i[q] < i));
+                const uint64_t k = s_k[r], x = s_x[r];
+                const uint32_t fb = s_b[r];
+                const uint32_t first = fb & 0xFFFFu, last = first + (fb >> 16);
+                // both words loaded unconditionally, eight entries per step:
+                // the loads of a step overlap instead of one latency per entry
+                uint32_t before = 0, q = first;
+                for (; q + 8 <= last; q += 8) {
+                    uint64_t kq[8], xq[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        kq[u] = s_k[q + u];
+                        xq[u] = s_x[q + u];
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u)
+                        before += (uint32_t)(kq[u] < k) | ((uint32_t)(kq[u] == k) & (uint32_t)(xq[u] < x));
                 }
-                out_k[p0 + f + before] = k;
-                out_v[p0 + f + before] = in_v[i];
+                for (; q < last; ++q) {
+                    const uint64_t kq = s_k[q], xq = s_x[q];
+                    before += (uint32_t)(kq < k) | ((uint32_t)(kq == k) & (uint32_t)(xq < x));
+                }
+                out_k[p0 + first + before] = k;
+                out_v[p0 + first + before] = (uint8_t)x;
             }
         } else {
             const uint32_t N = m <= 1 ? 1u : 1u << (32 - __clz(m - 1));
             for (uint32_t r = m + threadIdx.x; r < N; r += BLOCK) {
                 s_k[r] = KEY_NONE;
-                s_i[r] = 0xFFFFFFFFu;  // pads sort after every real key
+                s_x[r] = ~0ull;  // pads sort after every real key
             }
             __syncthreads();
-            bsort_bitonic(s_k, s_i, N);
+            bsort_bitonic(s_k, s_x, N);
             for (uint32_t r = threadIdx.x; r < m; r += BLOCK) {
                 out_k[p0 + r] = s_k[r];
-                out_v[p0 + r] = in_v[s_i[r]];
+                out_v[p0 + r] = (uint8_t)s_x[r];
             }
         }
         __syncthreads();

@@ -833,13 +833,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             return;
         digits = cta_broadcast_read(&st->sort_fallback) != 0;
         if (!digits) {
-            // scatter bk[0] -> bk[1] (+ batch indices), then items bk[1] -> bk[0], values bv[0] -> bv[1]
-            uint32_t *cpre = reinterpret_cast<uint32_t *>(smem + BSORT_SMEM_ITEMS);
+            // records of bk[0] / bv[0] scattered into buckets, then items sorted into bk[0] / bv[1]
+            uint32_t *cpre = reinterpret_cast<uint32_t *>(smem + BSORT_SMEM_ITEM);
             bsort_chunk_prefix(A.cta_cnt, cpre, tmp);
-            bsort_scatter(A.bk[0], A.bk[1], A.boff, A.G, A.gd, A.q, cpre);
+            bsort_scatter(A.bk[0], A.bv[0], A.boff, A.G, A.q, cpre);
             if (!grid_barrier(&st->bar, &st->err))
                 return;
-            bsort_items(A.bk[1], A.bk[0], A.bv[0], A.bv[1], A.boff, A.G, A.q, smem);
+            bsort_items(A.bk[0], A.bv[1], A.boff, A.G, A.q, cpre, smem);
             if (!grid_barrier(&st->bar, &st->err))
                 return;
         }
@@ -2228,7 +2228,9 @@ void free_buffers(BatchBuffers &b) {
     dev_free(b.sort_status);
     dev_free(b.sort_hist);
     dev_free(b.qcnt);
-    dev_free(b.qstart);
+    dev_free(b.qinfo);
+    dev_free(b.qrec);
+    dev_free(b.qbound);
     dev_free(b.d_tab);
     dev_free(b.d_stat);
     dev_free(b.chunk_cnt);
@@ -2249,6 +2251,8 @@ void free_buffers(BatchBuffers &b) {
     b.chunk_cap = 0;
     b.sort_status_cap = 0;
     b.q_cap = 0;
+    b.qrec_cap = 0;
+    b.qbound_cap = 0;
 }
 
 gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
@@ -2396,14 +2400,27 @@ gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t
         h_qoff[i + 1] = (uint32_t)nq;
         h_qtoff[i + 1] = h_qtoff[i] + (uint32_t)((ni + BSORT_ITEM - 1) / BSORT_ITEM);
     }
-    if (buckets && nq > buf.q_cap) {
+    const bool use_buckets = buckets && n > 0 && nq < BSORT_MAX_BUCKETS;
+    if (use_buckets && nq > buf.q_cap) {
         dev_free(buf.qcnt);
-        dev_free(buf.qstart);
+        dev_free(buf.qinfo);
         buf.q_cap = 0;
         GPMA_TRY(dev_alloc(&buf.qcnt, nq));
-        GPMA_TRY(dev_alloc(&buf.qstart, nq));
+        GPMA_TRY(dev_alloc(&buf.qinfo, nq));
         buf.q_cap = nq;
         buf.dirty = true;
+    }
+    if (use_buckets && n > buf.qrec_cap) {
+        dev_free(buf.qrec);
+        buf.qrec_cap = 0;
+        GPMA_TRY(dev_alloc(&buf.qrec, 2 * buf.cap));  // 16 bytes per key
+        buf.qrec_cap = buf.cap;
+    }
+    if (use_buckets && h_qtoff[k] > buf.qbound_cap) {
+        dev_free(buf.qbound);
+        buf.qbound_cap = 0;
+        GPMA_TRY(dev_alloc(&buf.qbound, h_qtoff[k]));
+        buf.qbound_cap = h_qtoff[k];
     }
     const uint32_t tiles = h_toff[k];
     const uint64_t status_words = 8ull * tiles * 256;
@@ -2452,16 +2469,16 @@ gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t
     A.sort_hist = buf.sort_hist;
     A.sort_tiles = buf.sort_tiles;
     A.sort_status = buf.sort_status;
-    if (buckets && n > 0) {
+    if (use_buckets) {
         A.q.qoff = buf.qoff;
         A.q.qtoff = buf.qtoff;
         A.q.nq = (uint32_t)nq;
         A.q.qcnt = buf.qcnt;
-        A.q.qstart = buf.qstart;
-        A.q.rank = buf.ileaf;  // all four first written after the sort
-        A.q.idx = buf.leaf;
-        A.q.bfirst = buf.wa[0];
-        A.q.bsize = buf.wb[0];
+        A.q.qinfo = reinterpret_cast<unsigned long long *>(buf.qinfo);
+        A.q.rank = buf.ileaf;  // both first written after the sort
+        A.q.bkt = buf.igraph;
+        A.q.rec = reinterpret_cast<uint4 *>(buf.qrec);
+        A.q.bound = buf.qbound;
     }
     A.check_keys = check_keys;
     A.leaf = buf.leaf;
