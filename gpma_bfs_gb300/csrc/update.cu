@@ -279,17 +279,57 @@ __device__ __forceinline__ void cta_range(uint32_t N, uint32_t &lo, uint32_t &hi
     hi = min(N, lo + per);
 }
 
-// Sum of cnt[0..blockIdx.x) and of cnt[0..gridDim.x).
-__device__ __forceinline__ void cta_prefix(const uint32_t *cnt, uint32_t &base, uint32_t &total, uint32_t *tmp) {
-    uint32_t a = 0, t = 0;
-    for (uint32_t j = threadIdx.x; j < gridDim.x; j += BLOCK) {
-        uint32_t c = ld_volatile(cnt + j);
-        t += c;
-        if (j < blockIdx.x)
-            a += c;
+// Four sums over the CTA in one shared-memory round (every thread gets them).
+__device__ __forceinline__ uint4 block_sum4(uint4 x) {
+    __shared__ uint4 s_red[BLOCK / 32];
+    x.x = __reduce_add_sync(0xFFFFFFFFu, x.x);
+    x.y = __reduce_add_sync(0xFFFFFFFFu, x.y);
+    x.z = __reduce_add_sync(0xFFFFFFFFu, x.z);
+    x.w = __reduce_add_sync(0xFFFFFFFFu, x.w);
+    __syncthreads();  // readers of the previous sums are done
+    if ((threadIdx.x & 31) == 0)
+        s_red[threadIdx.x >> 5] = x;
+    __syncthreads();
+    uint4 r = make_uint4(0, 0, 0, 0);
+#pragma unroll
+    for (int w = 0; w < BLOCK / 32; ++w) {
+        const uint4 q = s_red[w];
+        r.x += q.x;
+        r.y += q.y;
+        r.z += q.z;
+        r.w += q.w;
     }
-    base = block_sum(a, tmp);
-    total = block_sum(t, tmp);
+    return r;
+}
+
+// Sum of ca[0..blockIdx.x) and of ca[0..gridDim.x), and the same of cb (or
+// zeros without cb): per-CTA counts written before the last grid barrier. A
+// thread's loads are all issued before the first is used.
+__device__ __forceinline__ void cta_prefix2(const uint32_t *ca, const uint32_t *cb, uint32_t &base_a,
+                                            uint32_t &total_a, uint32_t &base_b, uint32_t &total_b) {
+    uint4 s = make_uint4(0, 0, 0, 0);
+    for (uint32_t j0 = 0; j0 < gridDim.x; j0 += 4 * BLOCK) {
+        uint32_t va[4], vb[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t j = j0 + u * BLOCK + threadIdx.x;
+            va[u] = j < gridDim.x ? __ldcg(ca + j) : 0u;
+            vb[u] = cb && j < gridDim.x ? __ldcg(cb + j) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const bool before = j0 + u * BLOCK + threadIdx.x < blockIdx.x;
+            s.x += before ? va[u] : 0u;
+            s.y += va[u];
+            s.z += before ? vb[u] : 0u;
+            s.w += vb[u];
+        }
+    }
+    s = block_sum4(s);
+    base_a = s.x;
+    total_a = s.y;
+    base_b = s.z;
+    total_b = s.w;
 }
 
 // ---- redispatch of a chunk of a window ------------------------------------
@@ -428,6 +468,46 @@ __device__ __forceinline__ void store_slots(uint64_t *keys, uint8_t *vals, uint3
     }
 }
 
+// Descriptor of window w (a stand-in past r1).
+__device__ __forceinline__ void read_window(const Windows &L, uint32_t w, uint32_t r1, uint32_t g_none, uint32_t &g,
+                                            uint32_t &node, uint32_t &a, uint32_t &b) {
+    g = g_none;
+    node = a = b = 0;
+    if (w < r1) {
+        g = L.graph[w];
+        node = L.node[w];
+        a = L.a[w];
+        b = L.b[w];
+    }
+}
+
+// Lane gl's K slots of window w (values packed, byte j of vp for slot j) and
+// its pending insertion gl; false past r1.
+template <uint32_t W, uint32_t K>
+__device__ __forceinline__ bool load_window(const UpdateArgs &A, const uint64_t *pk, const uint8_t *pv, uint32_t w,
+                                            uint32_t r1, uint32_t gl, uint32_t g, uint32_t node, uint32_t a,
+                                            uint32_t b, uint64_t (&k)[K], uint64_t &vp, uint64_t &pk0,
+                                            uint8_t &pv0) {
+    const GraphDesc &D = A.gd[g];
+    const bool has = w < r1 && in_bounds(&A.st->err, (uint64_t)node + W <= D.size && a <= b && b <= A.n, BS_WINDOW);
+    pk0 = 0;
+    pv0 = 0;
+    vp = 0;
+    if (has) {
+        const uint32_t t0 = node + gl * K;
+        uint8_t v[K];
+        load_slots<K>(D.keys, D.vals, t0, k, v);
+#pragma unroll
+        for (uint32_t j = 0; j < K; ++j)
+            vp |= (uint64_t)v[j] << (8 * j);
+        if (gl < b - a) {
+            pk0 = pk[a + gl];
+            pv0 = pv[a + gl];
+        }
+    }
+    return has;
+}
+
 template <uint32_t W>
 __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32_t r1, uint32_t level,
                              const uint64_t *pk, const uint8_t *pv, unsigned char *smem, unsigned long long &acc) {
@@ -445,50 +525,39 @@ __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
     uint8_t *cv = pend_v + W;
     uint8_t *mv = cv + W;
     const uint32_t total_warps = gridDim.x * (BLOCK / 32);
+    const uint32_t step = total_warps * GPW;
     const uint32_t g_r0 = L.graph[r0];  // stands in for groups without a window
-    // the next round's window descriptor is read while this round works
+    // A round's descriptor is read two rounds ahead and its slots (with its
+    // first pending insertions) one round ahead, so the loads of the next
+    // round are in flight while this one merges.
     uint32_t wbase = r0 + (blockIdx.x * (BLOCK / 32) + warp) * GPW;
-    uint32_t n_g = g_r0, n_node = 0, n_a = 0, n_b = 0;
-    if (wbase + grp < r1) {
-        n_g = L.graph[wbase + grp];
-        n_node = L.node[wbase + grp];
-        n_a = L.a[wbase + grp];
-        n_b = L.b[wbase + grp];
-    }
-    for (; wbase < r1; wbase += total_warps * GPW) {
+    uint32_t c_g, c_node, c_a, c_b, n_g, n_node, n_a, n_b;
+    read_window(L, wbase + grp, r1, g_r0, c_g, c_node, c_a, c_b);
+    read_window(L, wbase + step + grp, r1, g_r0, n_g, n_node, n_a, n_b);
+    static_assert(K <= 8, "values of a lane's slots are carried packed in one word");
+    uint64_t k[K], vp;
+    uint64_t pk0;
+    uint8_t pv0;
+    bool has = load_window<W, K>(A, pk, pv, wbase + grp, r1, gl, c_g, c_node, c_a, c_b, k, vp, pk0, pv0);
+    for (; wbase < r1; wbase += step) {
         const uint32_t w = wbase + grp;
-        const GraphDesc &D = A.gd[n_g];
-        const uint32_t node = n_node, a = n_a, b = n_b;
-        const bool has =
-            w < r1 && in_bounds(&A.st->err, (uint64_t)node + W <= D.size && a <= b && b <= A.n, BS_WINDOW);
+        const GraphDesc &D = A.gd[c_g];
+        const uint32_t node = c_node, a = c_a, b = c_b;
+        uint64_t nk[K], nvp;
+        uint64_t npk0;
+        uint8_t npv0;
+        const bool n_has = load_window<W, K>(A, pk, pv, w + step, r1, gl, n_g, n_node, n_a, n_b, nk, nvp, npk0, npv0);
+        uint8_t v[K];
+#pragma unroll
+        for (uint32_t j = 0; j < K; ++j)
+            v[j] = (uint8_t)(vp >> (8 * j));
+        uint32_t m_g, m_node, m_a, m_b;
+        read_window(L, w + 2 * step, r1, g_r0, m_g, m_node, m_a, m_b);
         const uint32_t log2seg = D.log2seg, seg_mask = D.seg - 1;
         const uint32_t log2F = (31 - __clz(W)) - log2seg;
         const uint32_t lo = D.lower[level], hi = D.upper[level];
         const uint32_t t0 = node + gl * K;
-        uint64_t k[K];
-        uint8_t v[K];
         uint32_t c_l = 0;
-        // the window's first pending insertions, loaded beside its slots
-        uint64_t pk0 = 0;
-        uint8_t pv0 = 0;
-        if (has) {
-            load_slots<K>(D.keys, D.vals, t0, k, v);
-            if (gl < b - a) {
-                pk0 = pk[a + gl];
-                pv0 = pv[a + gl];
-            }
-        }
-        {
-            const uint32_t wn = w + total_warps * GPW;
-            n_g = g_r0;
-            n_node = n_a = n_b = 0;
-            if (wn < r1) {
-                n_g = L.graph[wn];
-                n_node = L.node[wn];
-                n_a = L.a[wn];
-                n_b = L.b[wn];
-            }
-        }
         if (has) {
 #pragma unroll
             for (uint32_t j = 0; j < K; ++j)
@@ -559,6 +628,22 @@ __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
         if (has && gl == 0)
             A.wflag[w] = accept ? 1u : 0u;
         __syncwarp();
+        // the next round: its slots are (being) loaded, the one after it is read
+        c_g = n_g;
+        c_node = n_node;
+        c_a = n_a;
+        c_b = n_b;
+        n_g = m_g;
+        n_node = m_node;
+        n_a = m_a;
+        n_b = m_b;
+        has = n_has;
+        pk0 = npk0;
+        pv0 = npv0;
+        vp = nvp;
+#pragma unroll
+        for (uint32_t j = 0; j < K; ++j)
+            k[j] = nk[j];
     }
 }
 
@@ -968,8 +1053,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         if (!grid_barrier(&st->bar, &st->err))
             return;
     }
-    uint32_t base, m;
-    cta_prefix(CNT(scan_id), base, m, tmp);
+    uint32_t base, m, unused_b, unused_t;
+    cta_prefix2(CNT(scan_id), nullptr, base, m, unused_b, unused_t);
     const uint32_t out_lo = base;
     // GROUP_ITEMS consecutive items per thread and one scan per round
     for (uint32_t r0 = lo; r0 < hi; r0 += GROUP_ITEMS * BLOCK) {
@@ -1026,24 +1111,48 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         const uint32_t *ins_cnt = CNT(scan_id);
         const uint32_t *head_cnt = CNT(scan_id ^ 1);
         uint32_t carry = 0, before = 0, all = 0;
-        for (uint32_t c0 = 0; c0 < G; c0 += BLOCK) {
-            const uint32_t c = c0 + threadIdx.x;
-            const uint32_t n_c = c < G ? ld_volatile(ins_cnt + c) : 0u;
-            uint32_t tot;
-            const uint32_t b_c = carry + block_excl_scan(n_c, &tot, tmp);  // first output of CTA c
-            carry += tot;
-            uint32_t h = 0;
-            if (c < G && n_c) {
-                h = ld_volatile(head_cnt + c);
-                if (b_c > 0 && A.ileaf[b_c] == A.ileaf[b_c - 1] && A.igraph[b_c] == A.igraph[b_c - 1])
-                    --h;
+        // two CTAs' counts per thread per step, each kind of load issued for
+        // both before the first is used
+        for (uint32_t c0 = 0; c0 < G; c0 += 2 * BLOCK) {
+            uint32_t n_c[2], h_c[2], b_c[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const uint32_t c = c0 + u * BLOCK + threadIdx.x;
+                n_c[u] = c < G ? __ldcg(ins_cnt + c) : 0u;
+                h_c[u] = c < G ? __ldcg(head_cnt + c) : 0u;
             }
-            all += h;
-            if (c < blockIdx.x)
-                before += h;
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                uint32_t tot;
+                b_c[u] = carry + block_excl_scan(n_c[u], &tot, tmp);  // first output of CTA c
+                carry += tot;
+            }
+            uint32_t l0[2], l1[2], g0[2], g1[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const bool chk = n_c[u] && b_c[u] > 0;
+                l0[u] = chk ? A.ileaf[b_c[u]] : 0u;
+                l1[u] = chk ? A.ileaf[b_c[u] - 1] : 1u;
+                g0[u] = chk ? A.igraph[b_c[u]] : 0u;
+                g1[u] = chk ? A.igraph[b_c[u] - 1] : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const uint32_t c = c0 + u * BLOCK + threadIdx.x;
+                uint32_t h = 0;
+                if (c < G && n_c[u]) {
+                    h = h_c[u];
+                    if (l0[u] == l1[u] && g0[u] == g1[u])  // continues the previous CTA's last run
+                        --h;
+                }
+                all += h;
+                if (c < blockIdx.x)
+                    before += h;
+            }
         }
-        nw = block_sum(all, tmp);
-        base = block_sum(before, tmp);
+        const uint4 t = block_sum4(make_uint4(all, before, 0, 0));
+        nw = t.x;
+        base = t.y;
     }
     for (uint32_t r0 = out_lo; r0 < out_hi; r0 += GROUP_ITEMS * BLOCK) {
         const uint32_t j0 = r0 + GROUP_ITEMS * threadIdx.x;
@@ -1164,35 +1273,47 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         cta_range(nw, lo, hi);
         {
             uint32_t ch = 0, ci = 0;
-            for (uint32_t w = lo + threadIdx.x; w < hi; w += BLOCK) {
-                // the window's and its left neighbour's fields in one round
-                const uint32_t f0 = A.wflag[w], fl = w > 0 ? A.wflag[w - 1] : 1u;
-                const uint32_t g = L.graph[w], gl = w > 0 ? L.graph[w - 1] : 0u;
-                const uint32_t nd = L.node[w], ndl = w > 0 ? L.node[w - 1] : 0u;
-                const uint32_t wa = L.a[w], wb = L.b[w];
-                if (f0)
-                    continue;
-                const GraphDesc &Dg = A.gd[g];
-                if (level >= Dg.height)
-                    continue;  // root window: to the remaining buffer
-                const uint32_t W = Dg.seg << level;
-                ci += wb - wa;
-                const uint32_t par = nd & ~W;
-                const bool merged = w > 0 && !fl && gl == g && (ndl & ~W) == par;
-                ch += merged ? 0u : 1u;
+            constexpr int CU = 2;  // windows per thread per step, their fields loaded together
+            for (uint32_t w0 = lo + threadIdx.x; w0 < hi; w0 += CU * BLOCK) {
+                uint32_t f0[CU], fl[CU], g[CU], gl[CU], nd[CU], ndl[CU], wa[CU], wb[CU];
+#pragma unroll
+                for (int u = 0; u < CU; ++u) {
+                    // the window's and its left neighbour's fields
+                    const uint32_t w = w0 + u * BLOCK;
+                    const bool ok = w < hi;
+                    f0[u] = ok ? A.wflag[w] : 1u;
+                    fl[u] = ok && w > 0 ? A.wflag[w - 1] : 1u;
+                    g[u] = ok ? L.graph[w] : 0u;
+                    gl[u] = ok && w > 0 ? L.graph[w - 1] : 0u;
+                    nd[u] = ok ? L.node[w] : 0u;
+                    ndl[u] = ok && w > 0 ? L.node[w - 1] : 0u;
+                    wa[u] = ok ? L.a[w] : 0u;
+                    wb[u] = ok ? L.b[w] : 0u;
+                }
+#pragma unroll
+                for (int u = 0; u < CU; ++u) {
+                    if (f0[u])
+                        continue;  // accepted (or past the range)
+                    const GraphDesc &Dg = A.gd[g[u]];
+                    if (level >= Dg.height)
+                        continue;  // root window: to the remaining buffer
+                    const uint32_t W = Dg.seg << level;
+                    ci += wb[u] - wa[u];
+                    const uint32_t par = nd[u] & ~W;
+                    const bool merged = w0 + u * BLOCK > 0 && !fl[u] && gl[u] == g[u] && (ndl[u] & ~W) == par;
+                    ch += merged ? 0u : 1u;
+                }
             }
-            uint32_t th = block_sum(ch, tmp);
-            uint32_t ti = block_sum(ci, tmp);
+            const uint4 t = block_sum4(make_uint4(ch, ci, 0, 0));
             if (threadIdx.x == 0) {
-                CNT(scan_id)[blockIdx.x] = th;
-                CNTI(scan_id)[blockIdx.x] = ti;
+                CNT(scan_id)[blockIdx.x] = t.x;
+                CNTI(scan_id)[blockIdx.x] = t.y;
             }
         }
         if (!grid_barrier(&st->bar, &st->err))
             return;
         uint32_t nw_next, base_i, total_i;
-        cta_prefix(CNT(scan_id), base, nw_next, tmp);
-        cta_prefix(CNTI(scan_id), base_i, total_i, tmp);
+        cta_prefix2(CNT(scan_id), CNTI(scan_id), base, nw_next, base_i, total_i);
         if (nw_next == 0 && level < A.min_height) {
             // every window of this level was accepted and none can be a root
             // window: nothing to carry, no next level (counted as the loop's
