@@ -468,46 +468,6 @@ __device__ __forceinline__ void store_slots(uint64_t *keys, uint8_t *vals, uint3
     }
 }
 
-// Descriptor of window w (a stand-in past r1).
-__device__ __forceinline__ void read_window(const Windows &L, uint32_t w, uint32_t r1, uint32_t g_none, uint32_t &g,
-                                            uint32_t &node, uint32_t &a, uint32_t &b) {
-    g = g_none;
-    node = a = b = 0;
-    if (w < r1) {
-        g = L.graph[w];
-        node = L.node[w];
-        a = L.a[w];
-        b = L.b[w];
-    }
-}
-
-// Lane gl's K slots of window w (values packed, byte j of vp for slot j) and
-// its pending insertion gl; false past r1.
-template <uint32_t W, uint32_t K>
-__device__ __forceinline__ bool load_window(const UpdateArgs &A, const uint64_t *pk, const uint8_t *pv, uint32_t w,
-                                            uint32_t r1, uint32_t gl, uint32_t g, uint32_t node, uint32_t a,
-                                            uint32_t b, uint64_t (&k)[K], uint64_t &vp, uint64_t &pk0,
-                                            uint8_t &pv0) {
-    const GraphDesc &D = A.gd[g];
-    const bool has = w < r1 && in_bounds(&A.st->err, (uint64_t)node + W <= D.size && a <= b && b <= A.n, BS_WINDOW);
-    pk0 = 0;
-    pv0 = 0;
-    vp = 0;
-    if (has) {
-        const uint32_t t0 = node + gl * K;
-        uint8_t v[K];
-        load_slots<K>(D.keys, D.vals, t0, k, v);
-#pragma unroll
-        for (uint32_t j = 0; j < K; ++j)
-            vp |= (uint64_t)v[j] << (8 * j);
-        if (gl < b - a) {
-            pk0 = pk[a + gl];
-            pv0 = pv[a + gl];
-        }
-    }
-    return has;
-}
-
 template <uint32_t W>
 __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32_t r1, uint32_t level,
                              const uint64_t *pk, const uint8_t *pv, unsigned char *smem, unsigned long long &acc) {
@@ -525,39 +485,50 @@ __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
     uint8_t *cv = pend_v + W;
     uint8_t *mv = cv + W;
     const uint32_t total_warps = gridDim.x * (BLOCK / 32);
-    const uint32_t step = total_warps * GPW;
     const uint32_t g_r0 = L.graph[r0];  // stands in for groups without a window
-    // A round's descriptor is read two rounds ahead and its slots (with its
-    // first pending insertions) one round ahead, so the loads of the next
-    // round are in flight while this one merges.
+    // the next round's window descriptor is read while this round works
     uint32_t wbase = r0 + (blockIdx.x * (BLOCK / 32) + warp) * GPW;
-    uint32_t c_g, c_node, c_a, c_b, n_g, n_node, n_a, n_b;
-    read_window(L, wbase + grp, r1, g_r0, c_g, c_node, c_a, c_b);
-    read_window(L, wbase + step + grp, r1, g_r0, n_g, n_node, n_a, n_b);
-    static_assert(K <= 8, "values of a lane's slots are carried packed in one word");
-    uint64_t k[K], vp;
-    uint64_t pk0;
-    uint8_t pv0;
-    bool has = load_window<W, K>(A, pk, pv, wbase + grp, r1, gl, c_g, c_node, c_a, c_b, k, vp, pk0, pv0);
-    for (; wbase < r1; wbase += step) {
+    uint32_t n_g = g_r0, n_node = 0, n_a = 0, n_b = 0;
+    if (wbase + grp < r1) {
+        n_g = L.graph[wbase + grp];
+        n_node = L.node[wbase + grp];
+        n_a = L.a[wbase + grp];
+        n_b = L.b[wbase + grp];
+    }
+    for (; wbase < r1; wbase += total_warps * GPW) {
         const uint32_t w = wbase + grp;
-        const GraphDesc &D = A.gd[c_g];
-        const uint32_t node = c_node, a = c_a, b = c_b;
-        uint64_t nk[K], nvp;
-        uint64_t npk0;
-        uint8_t npv0;
-        const bool n_has = load_window<W, K>(A, pk, pv, w + step, r1, gl, n_g, n_node, n_a, n_b, nk, nvp, npk0, npv0);
-        uint8_t v[K];
-#pragma unroll
-        for (uint32_t j = 0; j < K; ++j)
-            v[j] = (uint8_t)(vp >> (8 * j));
-        uint32_t m_g, m_node, m_a, m_b;
-        read_window(L, w + 2 * step, r1, g_r0, m_g, m_node, m_a, m_b);
+        const GraphDesc &D = A.gd[n_g];
+        const uint32_t node = n_node, a = n_a, b = n_b;
+        const bool has =
+            w < r1 && in_bounds(&A.st->err, (uint64_t)node + W <= D.size && a <= b && b <= A.n, BS_WINDOW);
         const uint32_t log2seg = D.log2seg, seg_mask = D.seg - 1;
         const uint32_t log2F = (31 - __clz(W)) - log2seg;
         const uint32_t lo = D.lower[level], hi = D.upper[level];
         const uint32_t t0 = node + gl * K;
+        uint64_t k[K];
+        uint8_t v[K];
         uint32_t c_l = 0;
+        // the window's first pending insertions, loaded beside its slots
+        uint64_t pk0 = 0;
+        uint8_t pv0 = 0;
+        if (has) {
+            load_slots<K>(D.keys, D.vals, t0, k, v);
+            if (gl < b - a) {
+                pk0 = pk[a + gl];
+                pv0 = pv[a + gl];
+            }
+        }
+        {
+            const uint32_t wn = w + total_warps * GPW;
+            n_g = g_r0;
+            n_node = n_a = n_b = 0;
+            if (wn < r1) {
+                n_g = L.graph[wn];
+                n_node = L.node[wn];
+                n_a = L.a[wn];
+                n_b = L.b[wn];
+            }
+        }
         if (has) {
 #pragma unroll
             for (uint32_t j = 0; j < K; ++j)
@@ -628,22 +599,6 @@ __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
         if (has && gl == 0)
             A.wflag[w] = accept ? 1u : 0u;
         __syncwarp();
-        // the next round: its slots are (being) loaded, the one after it is read
-        c_g = n_g;
-        c_node = n_node;
-        c_a = n_a;
-        c_b = n_b;
-        n_g = m_g;
-        n_node = m_node;
-        n_a = m_a;
-        n_b = m_b;
-        has = n_has;
-        pk0 = npk0;
-        pv0 = npv0;
-        vp = nvp;
-#pragma unroll
-        for (uint32_t j = 0; j < K; ++j)
-            k[j] = nk[j];
     }
 }
 
