@@ -118,11 +118,17 @@ __device__ __forceinline__ uint32_t visit_slots(const BfsArgs &A, const uint32_t
     for (uint32_t j = 0; j < N; ++j)
         if (!seen[j])
             seen[j] = A.visited[w[j] >> 5];
+    // every claim in flight before the first result is used
+#pragma unroll
+    for (uint32_t j = 0; j < N; ++j) {
+        const uint32_t bit = 1u << (w[j] & 31);
+        seen[j] = (seen[j] & bit) ? bit : atomicOr(&A.visited[w[j] >> 5], bit);
+    }
     uint32_t fresh = 0;
 #pragma unroll
     for (uint32_t j = 0; j < N; ++j) {
         const uint32_t bit = 1u << (w[j] & 31);
-        if (!(seen[j] & bit) && !(atomicOr(&A.visited[w[j] >> 5], bit) & bit)) {
+        if (!(seen[j] & bit)) {
             A.levels[w[j]] = next_level;
             atomicOr(&front_next[w[j] >> 5], bit);
             ++fresh;
@@ -155,11 +161,17 @@ __device__ __forceinline__ uint32_t dense_visit8(const BfsArgs &A, const uint64_
         c[j] = c[j] && (word[j] & 1u);
         word[j] = c[j] ? A.visited[dst[j] >> 5] : 0xFFFFFFFFu;
     }
+    // every claim in flight before the first result is used
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const uint32_t bit = 1u << (dst[j] & 31);
+        word[j] = (!c[j] || (word[j] & bit)) ? bit : atomicOr(&A.visited[dst[j] >> 5], bit);
+    }
     uint32_t fresh = 0;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         const uint32_t bit = 1u << (dst[j] & 31);
-        if (c[j] && !(word[j] & bit) && !(atomicOr(&A.visited[dst[j] >> 5], bit) & bit)) {
+        if (!(word[j] & bit)) {
             A.levels[dst[j]] = next_level;
             atomicOr(&front_next[dst[j] >> 5], bit);
             ++fresh;
