@@ -222,16 +222,33 @@ __device__ __forceinline__ uint32_t frontier_pass(const BfsArgs &A, uint32_t *fr
       uint32_t pending = __ballot_sync(0xFFFFFFFFu, mine != 0u);
       if (CLEAR && mine)
           front_cur[wl] = 0;
+      // a word's row offsets are read while the previous word is walked
+      uint32_t nb = 0, nr1 = 0;
+      if (pending) {
+          const uint32_t src = __ffs(pending) - 1;
+          if (__shfl_sync(0xFFFFFFFFu, mine, src) & (1u << lane)) {
+              const uint32_t u = ((gwarp + (it + src) * nwarps) << 5) + lane;
+              nb = A.ro[u];
+              nr1 = A.ro[u + 1];
+          }
+      }
       while (pending) {
         const uint32_t src = __ffs(pending) - 1;
         pending &= pending - 1;
-        const uint32_t wi = gwarp + (it + src) * nwarps;
         const uint32_t f = __shfl_sync(0xFFFFFFFFu, mine, src);
+        const uint32_t rb = nb, r1 = nr1;
+        nb = nr1 = 0;
+        if (pending) {
+            const uint32_t src2 = __ffs(pending) - 1;
+            if (__shfl_sync(0xFFFFFFFFu, mine, src2) & (1u << lane)) {
+                const uint32_t u2 = ((gwarp + (it + src2) * nwarps) << 5) + lane;
+                nb = A.ro[u2];
+                nr1 = A.ro[u2 + 1];
+            }
+        }
         uint32_t b = 0, e = 0, len = 0;
         if (f & (1u << lane)) {
-            const uint32_t u = (wi << 5) + lane;
-            const uint32_t r1 = A.ro[u + 1];
-            b = A.ro[u];
+            b = rb;
             e = min(r1, A.size);
             if (!in_bounds(A.ctl + CTL_ERR, b <= r1 && r1 <= A.size, BS_ROW))
                 b = e;  // an inconsistent row_offset: the row is skipped
