@@ -98,7 +98,11 @@ struct BfsArgs {
 
 // N edge slots of one lane (SIZE_NONE: absent): every key, value and
 // visited word is loaded before any claim, so each lane keeps several
-// requests in flight. Returns the number of nodes this lane claimed.
+// requests in flight. A target that was unvisited when its word was read is
+// claimed without waiting for a result: every lane that saw it unvisited sets
+// its visited bit, its level (next_level, the same from every claimer) and
+// its next-frontier bit, all idempotent. Returns the number of such claims
+// (at least the nodes this lane reached first, more when lanes raced).
 template <uint32_t N>
 __device__ __forceinline__ uint32_t visit_slots(const BfsArgs &A, const uint32_t (&sl)[N], uint32_t next_level,
                                                 uint32_t *front_next) {
@@ -118,17 +122,12 @@ __device__ __forceinline__ uint32_t visit_slots(const BfsArgs &A, const uint32_t
     for (uint32_t j = 0; j < N; ++j)
         if (!seen[j])
             seen[j] = A.visited[w[j] >> 5];
-    // every claim in flight before the first result is used
-#pragma unroll
-    for (uint32_t j = 0; j < N; ++j) {
-        const uint32_t bit = 1u << (w[j] & 31);
-        seen[j] = (seen[j] & bit) ? bit : atomicOr(&A.visited[w[j] >> 5], bit);
-    }
     uint32_t fresh = 0;
 #pragma unroll
     for (uint32_t j = 0; j < N; ++j) {
         const uint32_t bit = 1u << (w[j] & 31);
         if (!(seen[j] & bit)) {
+            atomicOr(&A.visited[w[j] >> 5], bit);
             A.levels[w[j]] = next_level;
             atomicOr(&front_next[w[j] >> 5], bit);
             ++fresh;
@@ -161,17 +160,13 @@ __device__ __forceinline__ uint32_t dense_visit8(const BfsArgs &A, const uint64_
         c[j] = c[j] && (word[j] & 1u);
         word[j] = c[j] ? A.visited[dst[j] >> 5] : 0xFFFFFFFFu;
     }
-    // every claim in flight before the first result is used
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        const uint32_t bit = 1u << (dst[j] & 31);
-        word[j] = (!c[j] || (word[j] & bit)) ? bit : atomicOr(&A.visited[dst[j] >> 5], bit);
-    }
+    // claims as in visit_slots: idempotent, none waits for a result
     uint32_t fresh = 0;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         const uint32_t bit = 1u << (dst[j] & 31);
-        if (!(word[j] & bit)) {
+        if (c[j] && !(word[j] & bit)) {
+            atomicOr(&A.visited[dst[j] >> 5], bit);
             A.levels[dst[j]] = next_level;
             atomicOr(&front_next[dst[j] >> 5], bit);
             ++fresh;
@@ -298,16 +293,14 @@ __device__ __forceinline__ uint32_t frontier_pass(const BfsArgs &A, uint32_t *fr
     return fresh;
 }
 
-// Nodes first reached at level i: one atomic per warp into the counter the
-// next level reads. Returns the warp's total (every lane; lane 0 adds it to
-// the reached count at the end).
-__device__ __forceinline__ uint32_t level_count(const BfsArgs &A, uint32_t i, uint32_t fresh, uint32_t lane) {
+// Claims of level i (the next frontier's size, or a little more when lanes
+// raced for a node): one atomic per warp into the counter the next level reads.
+__device__ __forceinline__ void level_count(const BfsArgs &A, uint32_t i, uint32_t fresh, uint32_t lane) {
 #pragma unroll
     for (int d = 16; d >= 1; d >>= 1)
         fresh += __shfl_xor_sync(0xFFFFFFFFu, fresh, d);
     if (lane == 0 && fresh)
         atomicAdd(A.ctl + CTL_CNT + (i + 1) % 3, fresh);
-    return fresh;
 }
 
 // A level whose frontier holds fewer than n / DENSE_GATE nodes is walked
@@ -327,7 +320,6 @@ __global__ void __launch_bounds__(BLOCK, 5) bfs_kernel(BfsArgs A) {
     const uint32_t gwarp = blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5);
     const uint32_t nwarps = gridDim.x * (BLOCK / 32);
     const uint32_t words = (A.n + 31) >> 5;
-    uint32_t added = 0;
     uint32_t last_frontier = 0;
     uint32_t i = 0;
     for (;; ++i) {
@@ -390,7 +382,7 @@ __global__ void __launch_bounds__(BLOCK, 5) bfs_kernel(BfsArgs A) {
                 return;
             for (uint32_t w = gtid; w < words; w += nthreads)
                 front_cur[w] = 0;
-            added += level_count(A, i, fresh, lane);
+            level_count(A, i, fresh, lane);
             if (!grid_barrier(bar, err, stall, A.stall_limit_ns))
                 return;
             continue;
@@ -421,7 +413,7 @@ __global__ void __launch_bounds__(BLOCK, 5) bfs_kernel(BfsArgs A) {
                     fresh += visit_slots<CHUNK_LANE_SLOTS>(A, sl, next_level, front_next);
                 }
             }
-            added += level_count(A, i, fresh, lane);
+            level_count(A, i, fresh, lane);
             if (!grid_barrier(bar, err, stall, A.stall_limit_ns))
                 return;
             continue;
@@ -443,12 +435,19 @@ __global__ void __launch_bounds__(BLOCK, 5) bfs_kernel(BfsArgs A) {
                 fresh += visit_slots<CHUNK_LANE_SLOTS>(A, sl, next_level, front_next);
             }
         }
-        added += level_count(A, i, fresh, lane);
+        level_count(A, i, fresh, lane);
         if (!grid_barrier(bar, err, stall, A.stall_limit_ns))
             return;
     }
-    if (lane == 0 && added)
-        atomicAdd(A.ctl + CTL_REACHED, added);
+    // reached nodes: the visited bits (a claim count may hold a node twice)
+    uint32_t reached = 0;
+    for (uint32_t w = blockIdx.x * BLOCK + threadIdx.x; w < words; w += gridDim.x * BLOCK)
+        reached += __popc(A.visited[w]);
+#pragma unroll
+    for (int d = 16; d >= 1; d >>= 1)
+        reached += __shfl_xor_sync(0xFFFFFFFFu, reached, d);
+    if (lane == 0 && reached)
+        atomicAdd(A.ctl + CTL_REACHED, reached);
     if (blockIdx.x == 0 && threadIdx.x == 0)
         A.ctl[CTL_LEVELS] = i;
 }
@@ -463,7 +462,7 @@ __global__ void bfs_init_kernel(uint32_t *levels, uint32_t *visited, uint32_t *f
     ctl[CTL_SLOTS + 0] = 0;
     ctl[CTL_SLOTS + 1] = 0;
     ctl[CTL_SLOTS + 2] = 0;
-    ctl[CTL_REACHED] = 1;
+    ctl[CTL_REACHED] = 0;  // the kernel counts the visited bits at the end
 }
 
 gpma_status ensure_bfs(gpma_graph *g) {

@@ -442,8 +442,9 @@ GPMA_API gpma_status gpma_batch_set_profiling(gpma_batch *b, int enabled);
 GPMA_API gpma_status gpma_batch_get_profile(const gpma_batch *b, gpma_profile *out);
 GPMA_API gpma_status gpma_batch_reset_profile(gpma_batch *b);
 /* Per level of the last gpma_bfs run with profiling on: its duration (ms, from
- * %globaltimer stamps at level starts), its frontier size and whether it swept
- * the whole array (dense). Up to `capacity` entries; *levels = levels run
+ * %globaltimer stamps at level starts), its frontier size (counted as the
+ * previous level's claims: a node that several lanes found unvisited at once
+ * counts once per lane) and whether it swept the whole array (dense). Up to `capacity` entries; *levels = levels run
  * (0 when the last BFS was not profiled). */
 GPMA_API gpma_status gpma_bfs_level_profile(const gpma_graph *g, double *ms, uint32_t *frontier, uint8_t *dense,
                                             uint32_t capacity, uint32_t *levels);
