@@ -390,6 +390,12 @@ def run_gpu(args):
                 "step_ms": {"eager": batched["update_bfs_steps"]["eager_ms"],
                             "graph": batched["update_bfs_steps"]["graph_ms"],
                             "identical": batched["update_bfs_steps"]["identical"]}}
+            many = batched.get("recorded_steps")
+            if many:
+                line["batched"]["recorded_steps"] = {
+                    "steps": many["steps"], "graph_launches": many["graph_launches"],
+                    "graph_ms_per_step": many["graph_ms_per_step"], "eager_ms_per_step": many["eager_ms_per_step"],
+                    "updates_per_s": many["updates_per_s"], "identical": many["identical"]}
         if served:
             light, sat = served["phases"][0], served["phases"][-1]
 
@@ -650,6 +656,45 @@ def run_batched(args, stream):
         np.array_equal(x.export_layout()[0], y.export_layout()[0]) for x, y in zip(graphs_b, graphs_p))
     rec_stats = rec.stats()
     rec.close()
+
+    # the same for S steps recorded in ONE graph launch (gpma_batch_step_run_many)
+    # against S pairs of eager calls; the batches are device-resident up front
+    S = args.graph_steps
+    many = None
+    if S > 1:
+        ks, vs, offs = [], [], []
+        for _ in range(S):
+            sizes = np.exp(rng.uniform(np.log(100), np.log(200_000), k)).astype(np.int64)
+            parts = [s.step(int(z)) for s, z in zip(streams, sizes)]
+            for sp, z in zip(streams_p, sizes):
+                sp.step(int(z))
+            offs.append(np.concatenate([[0], np.cumsum([len(p[0]) for p in parts])]).astype(np.uint64))
+            ks.append(torch.from_numpy(np.concatenate([p[0] for p in parts]).view(np.int64)).cuda())
+            vs.append(torch.from_numpy(np.concatenate([p[1] for p in parts])).cuda())
+        rec_many = b2.step(graphs_p)
+        got_e = []
+
+        def eager_many():
+            for t in range(S):
+                b.update_packed(graphs_b, ks[t], vs[t], offs[t], stream)
+                got_e.append(b.bfs_multi(graphs_b, sources, stream=stream)[1])
+
+        got_r = {}
+
+        def recorded_many():
+            got_r["r"] = rec_many.run_many(ks, vs, offs, sources, stream=stream)
+
+        t_em, t_rm = timed(eager_many), timed(recorded_many)
+        same_many = all(all(np.array_equal(x, y) for x, y in zip(got_e[t], got_r["r"][t])) for t in range(S)) and all(
+            np.array_equal(x.export_layout()[0], y.export_layout()[0]) for x, y in zip(graphs_b, graphs_p))
+        ms_stats = rec_many.stats()
+        rec_many.close()
+        n_many = int(sum(int(o[-1]) for o in offs))
+        many = {"steps": S, "graph_ms_per_step": t_rm / S, "eager_ms_per_step": t_em / S,
+                "updates_per_s": n_many / (t_rm * 1e-3), "identical": same_many,
+                "graph_launches": ms_stats["graph_launches"], "graph_builds": ms_stats["builds"],
+                "host_runs": ms_stats["host_runs"]}
+        del ks, vs
     b2.close()
     b.close()
     total_edges = int(sum(len(kk) for _, kk in specs))
@@ -671,6 +716,7 @@ def run_batched(args, stream):
         "update_bfs_steps": {"eager_ms": statistics.median(te), "graph_ms": statistics.median(tr),
                              "identical": same_steps, "graph_launches": rec_stats["graph_launches"],
                              "graph_builds": rec_stats["builds"], "host_runs": rec_stats["host_runs"]},
+        "recorded_steps": many,
         "setup_s": {"generate": gen_s},
     }
 
@@ -1052,6 +1098,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the built-in tuning (no sweep before timing)")
     ap.add_argument("--batched-graphs", type=int, default=256, help="graphs of the batched configuration (0: skip)")
     ap.add_argument("--batched-steps", type=int, default=5)
+    ap.add_argument("--graph-steps", type=int, default=50,
+                    help="batched steps recorded in one CUDA graph launch, against as many eager steps (0/1: skip)")
     ap.add_argument("--served-seconds", type=float, default=30.0,
                     help="seconds of served traffic at the light rate, in real time (0: skip the served configuration)")
     ap.add_argument("--served-rate", type=float, default=20.0, help="served request arrivals per second (light load)")

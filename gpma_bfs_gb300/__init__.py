@@ -196,6 +196,7 @@ def lib() -> ctypes.CDLL:
         "gpma_batch_step_create": (st, [P, P, u32, ctypes.POINTER(P)]),
         "gpma_batch_step_destroy": (st, [P]),
         "gpma_batch_step_run": (st, [P, P, P, P, P, P, P, P]),
+        "gpma_batch_step_run_many": (st, [P, u32, P, P, P, P, P, P, P]),
         "gpma_batch_step_get_stats": (st, [P, ctypes.POINTER(_StepStats)]),
     }
     for name, (res, args) in sig.items():
@@ -821,6 +822,43 @@ class BatchStep:
             parts.append(reached[o:o + len(x)])
             o += len(x)
         return parts
+
+    def run_many(self, keys, values, offsets, sources, stream=None):
+        """Several steps in one recorded graph launch: step t applies keys[t] /
+        values[t] (device tensors or device pointers) with offsets[t] (len(graphs)
+        + 1 entries), each followed by the multi-source BFS from `sources`.
+        Returns, per step, the reached counts per graph."""
+        k, steps = len(self.graphs), len(keys)
+        if len(values) != steps or len(offsets) != steps or len(sources) != k:
+            raise ValueError("one key, value and offset array per step, one source list per graph")
+        off = np.ascontiguousarray(np.stack([np.asarray(o, np.uint64) for o in offsets])) if steps else \
+            np.zeros((0, k + 1), np.uint64)
+        if off.shape != (steps, k + 1):
+            raise ValueError("offsets must have len(graphs) + 1 entries per step")
+        keep, kp, vp = [], (ctypes.c_void_p * max(steps, 1))(), (ctypes.c_void_p * max(steps, 1))()
+        for t in range(steps):
+            if len(keys[t]) != len(values[t]) or int(off[t, -1]) > len(keys[t]):
+                raise ValueError(f"step {t}: offsets past the key array or key/value lengths differ")
+            a, ka = _ptr(keys[t])
+            b, kb = _ptr(values[t])
+            keep += [ka, kb]
+            kp[t], vp[t] = a, b
+        srcs = [np.ascontiguousarray(np.asarray(x, np.uint32)) for x in sources]
+        sp = (ctypes.c_void_p * k)(*[x.ctypes.data for x in srcs])
+        ns = (ctypes.c_uint32 * k)(*[len(x) for x in srcs])
+        per = sum(len(x) for x in srcs)
+        reached = np.zeros(steps * per, np.uint64)
+        _check(lib().gpma_batch_step_run_many(self.handle, steps, kp, vp, off.ctypes.data, sp, ns,
+                                              reached.ctypes.data, _stream_ptr(stream)), "gpma_batch_step_run_many")
+        del keep
+        out = []
+        for t in range(steps):
+            parts, o = [], t * per
+            for x in srcs:
+                parts.append(reached[o:o + len(x)])
+                o += len(x)
+            out.append(parts)
+        return out
 
     def stats(self) -> dict:
         st = _StepStats()

@@ -174,8 +174,11 @@ struct GatherArgs {
     const uint64_t *dst_off;    // m + 1
     const uint64_t *src_start;  // m
     uint32_t m;
+    const uint32_t *abort;  // non-zero: return at once (a recorded step after one needing host work)
 };
 __global__ void gather_segments_kernel(GatherArgs A) {
+    if (A.abort && *(const volatile uint32_t *)A.abort)
+        return;
     const uint64_t n = A.dst_off[A.m];
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t lo = 0, hi = A.m;
@@ -200,7 +203,7 @@ int small_grid(uint64_t work, int sms) {
 }  // namespace
 
 gpma_status packed_plan(gpma_batch *b, gpma_graph *const *graphs, const uint64_t *keys, const uint8_t *values,
-                        const uint64_t *offsets, uint32_t k, PackedPlan *P) {
+                        const uint64_t *offsets, uint32_t k, PackedPlan *P, const uint32_t *abort) {
     static_assert(sizeof(GatherArgs) <= KernelLaunch::ARG_BYTES, "gather arguments exceed the launch record");
     const uint64_t all = k ? offsets[k] - offsets[0] : 0;
     std::vector<uint32_t> order;
@@ -259,6 +262,7 @@ gpma_status packed_plan(gpma_batch *b, gpma_graph *const *graphs, const uint64_t
     A.dst_off = b->gather_tab;
     A.src_start = b->gather_tab + m + 1;
     A.m = m;
+    A.abort = abort;
     P->gather.set((const void *)gather_segments_kernel, small_grid(total, b->sms), 0, &A, sizeof(A));
     return GPMA_OK;
 }

@@ -410,8 +410,10 @@ gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_
 // reads the copied status, updates the graphs' stats, finishes root rebuilds
 // on the host and flips the status slot. update_needs_host: the status asks
 // for host work or reports an error (the array changed after the kernel).
+// A non-null `abort` (a device word) makes the launch return at once while
+// the word is non-zero (steps recorded after one that needs host work).
 gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t k, BatchBuffers &buf, int sms,
-                        bool check_keys, size_t *tab_bytes, KernelLaunch *L);
+                        bool check_keys, size_t *tab_bytes, KernelLaunch *L, const uint32_t *abort = nullptr);
 gpma_status update_clear(BatchBuffers &buf, cudaStream_t s);
 size_t update_status_bytes(uint32_t k);
 gpma_status update_finish(gpma_graph *const *graphs, uint32_t k, BatchBuffers &buf, const unsigned char *stat,
@@ -476,11 +478,12 @@ struct PackedPlan {
     KernelLaunch gather;
 };
 gpma_status packed_plan(gpma_batch *b, gpma_graph *const *graphs, const uint64_t *keys, const uint8_t *values,
-                        const uint64_t *offsets, uint32_t k, PackedPlan *P);
+                        const uint64_t *offsets, uint32_t k, PackedPlan *P, const uint32_t *abort = nullptr);
 gpma_status packed_stage(gpma_batch *b, const PackedPlan &P, const uint64_t *keys, const uint8_t *values,
                          const uint64_t *offsets, cudaStream_t s, bool with_table = true);
 gpma_status batch_bfs_plan(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs,
-                           const uint32_t *nsrc, uint32_t k, uint32_t *const *stage, BatchBfsPlan *P);
+                           const uint32_t *nsrc, uint32_t k, uint32_t *const *stage, BatchBfsPlan *P,
+                           const uint32_t *abort = nullptr);
 gpma_status batch_bfs_enqueue_readback(gpma_batch *b, const BatchBfsPlan &P, cudaStream_t s);
 gpma_status batch_bfs_finish(gpma_batch *b, const uint32_t *nsrc, uint32_t k, uint64_t *reached);
 void free_bfs(gpma_graph *g);

@@ -67,6 +67,7 @@ struct MsArgs {
     unsigned long long *reached;  // G * 64
     unsigned long long *traversed;
     uint32_t dense_div;    // a level whose union frontier's rows span >= slots / dense_div slots sweeps every slot (0: never)
+    const uint32_t *abort;  // non-zero: return at once (a recorded step after one needing host work)
 };
 
 __device__ __forceinline__ uint32_t graph_of_node(const MsArgs &A, uint32_t u) {
@@ -137,6 +138,8 @@ __device__ __forceinline__ uint32_t ms_row_slots(const MsGraph &Gr, uint32_t v) 
 }
 
 __global__ void __launch_bounds__(BLOCK) msbfs_kernel(MsArgs A) {
+    if (A.abort && *(const volatile uint32_t *)A.abort)
+        return;
     GridBarrier *bar = reinterpret_cast<GridBarrier *>(A.ctl + MS_BAR);
     uint32_t *err = A.ctl + MS_ERR;
     const uint32_t lane = threadIdx.x & 31;
@@ -400,7 +403,8 @@ struct MsTabLayout {
 }  // namespace
 
 gpma_status batch_bfs_plan(gpma_batch *b, gpma_graph *const *graphs, const uint32_t *const *srcs,
-                           const uint32_t *nsrc, uint32_t k, uint32_t *const *stage, BatchBfsPlan *P) {
+                           const uint32_t *nsrc, uint32_t k, uint32_t *const *stage, BatchBfsPlan *P,
+                           const uint32_t *abort) {
     static_assert(sizeof(MsArgs) <= KernelLaunch::ARG_BYTES, "multi-source BFS arguments exceed the launch record");
     const int grid = ms_grid_size(b->sms);
     if (grid == 0) {
@@ -494,6 +498,7 @@ gpma_status batch_bfs_plan(gpma_batch *b, gpma_graph *const *graphs, const uint3
     A.ctl = b->ms_ctl;
     A.reached = reinterpret_cast<unsigned long long *>(b->ms_reached);
     A.traversed = reinterpret_cast<unsigned long long *>(b->ms_reached) + 64ull * k;
+    A.abort = abort;
     P->main.set((const void *)msbfs_kernel, grid, 0, &A, sizeof(A));
     P->ctl_bytes = sizeof(uint32_t) * MS_CTL_WORDS;
     P->reached_bytes = sizeof(unsigned long long) * (64ull * k + 1);

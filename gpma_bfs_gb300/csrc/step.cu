@@ -328,10 +328,56 @@ struct gpma_batch_step {
     size_t h_stat_bytes = 0;
     cudaEvent_t ev[2] = {nullptr, nullptr};
     gpma_step_stats stats{};
+    // several steps recorded in one graph (gpma_batch_step_run_many)
+    struct Multi {
+        uint32_t steps = 0;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        std::vector<cudaGraphNode_t> n_gather, n_update, n_ms;
+        std::vector<gpma::KernelLaunch> gather, upd, ms;
+        std::vector<unsigned char> baked;
+        // pinned: the BFS table once, then per step its gather table, update
+        // table, status slot, BFS control words and BFS counts
+        unsigned char *h_buf = nullptr;
+        size_t h_bytes = 0;
+        size_t mtab = 0, gtab = 0, utab = 0, stat = 0, ctl = 0, reach = 0, per_step = 0;
+        uint32_t *d_abort = nullptr;  // set by the first step that needs host work
+    } multi;
 };
 
 namespace gpma {
 namespace {
+
+// After a recorded step's update: a status that asks for host work (root
+// rebalance, bulk rebuild, invalid keys, an error) or a launch that did not
+// run sets the abort word, and every later gather, update and BFS launch of
+// the recording returns at once.
+struct GateArgs {
+    const unsigned char *stat;
+    uint32_t k;
+    uint32_t *abort;
+};
+__global__ void step_gate_kernel(GateArgs A) {
+    const DeviceStatus &h = *reinterpret_cast<const DeviceStatus *>(A.stat);
+    const GraphStatus *gs = reinterpret_cast<const GraphStatus *>(A.stat + STAT_GS_OFFSET);
+    uint32_t need = 0;
+    for (uint32_t i = threadIdx.x; i < A.k; i += blockDim.x)
+        need |= (uint32_t)(gs[i].remaining > 0);
+    need = __syncthreads_or(need);
+    if (threadIdx.x == 0 && (need || h.err || h.invalid_keys || h.significant || h.stamp[0] == 0))
+        *A.abort = 1u;
+}
+
+void drop_multi_graph(gpma_batch_step *st) {
+    if (st->multi.exec)
+        cudaGraphExecDestroy(st->multi.exec);
+    if (st->multi.graph)
+        cudaGraphDestroy(st->multi.graph);
+    st->multi.exec = nullptr;
+    st->multi.graph = nullptr;
+    st->multi.steps = 0;
+    st->multi.baked.clear();
+}
 
 void drop_batch_graph(gpma_batch_step *st) {
     if (st->exec)
@@ -478,6 +524,225 @@ gpma_status batch_step_run(gpma_batch_step *st, const uint64_t *keys, const uint
     return batch_bfs_finish(b, nsrc, k, reached);
 }
 
+namespace {
+size_t pad16(size_t x) { return (x + 15) & ~size_t(15); }
+}  // namespace
+
+// S steps in one graph launch. Step t's batch is keys[t]/values[t] (device)
+// with offsets at offsets + t * (k + 1); every step searches from the same
+// sources; reached receives S x sum(nsrc) counts. Steps whose parts are empty
+// or bulk-sized, or host batches, run one by one through batch_step_run.
+// Each recorded step is: gather-table upload, gather, update-table upload,
+// update kernel, status copy, gate, BFS clears, multi-source BFS, BFS
+// read-back. A step whose update needs host work stops the rest of the
+// recording (the gate's abort word); its host work, its BFS and the steps
+// after it then run as batch_step_run would, so the results are always those
+// of the per-step calls.
+gpma_status batch_step_run_many(gpma_batch_step *st, uint32_t S, const uint64_t *const *keys,
+                                const uint8_t *const *values, const uint64_t *offsets, const uint32_t *const *srcs,
+                                const uint32_t *nsrc, uint64_t *reached, cudaStream_t s) {
+    gpma_batch *b = st->b;
+    gpma_graph *const *graphs = st->graphs.data();
+    const uint32_t k = (uint32_t)st->graphs.size();
+    uint64_t per_src = 0;
+    for (uint32_t i = 0; i < k; ++i)
+        per_src += nsrc[i];
+    auto off_of = [&](uint32_t t) { return offsets + (size_t)t * (k + 1); };
+    auto reach_of = [&](uint32_t t) { return reached ? reached + (size_t)t * per_src : nullptr; };
+    auto one_by_one = [&](uint32_t from) -> gpma_status {
+        for (uint32_t t = from; t < S; ++t)
+            GPMA_TRY(batch_step_run(st, keys[t], values[t], off_of(t), srcs, nsrc, reach_of(t), s));
+        return GPMA_OK;
+    };
+    bool eligible = S > 1;
+    for (uint32_t t = 0; t < S && eligible; ++t) {
+        eligible = is_device_pointer(keys[t]) && is_device_pointer(values[t]);
+        const uint64_t *o = off_of(t);
+        for (uint32_t i = 0; i < k && eligible; ++i) {
+            const uint64_t c = o[i + 1] - o[i];
+            eligible = c > 0 && c < SIGNIFICANT_INSERTS;
+        }
+    }
+    if (!eligible)
+        return one_by_one(0);
+    auto &M = st->multi;
+    if (!M.d_abort)
+        GPMA_TRY(dev_alloc(&M.d_abort, 1));
+    // Plans of every step: the first pass grows the buffers to what all steps
+    // need, the second records pointers that no later plan moves. Step t's
+    // status goes to slot parity[t], as consecutive launches alternate.
+    std::vector<PackedPlan> pp(S);
+    std::vector<size_t> tabb(S);
+    std::vector<KernelLaunch> upd(S);
+    std::vector<int> parity(S);
+    BatchBfsPlan bp;
+    const int p0 = b->buf.parity;
+    for (int pass = 0; pass < 2; ++pass) {
+        b->buf.parity = p0;
+        for (uint32_t t = 0; t < S; ++t) {
+            GPMA_TRY(packed_plan(b, graphs, keys[t], values[t], off_of(t), k, &pp[t], M.d_abort));
+            GPMA_TRY(update_plan(pp[t].gs.data(), pp[t].off.data(), pp[t].m, b->buf, b->sms, true, &tabb[t], &upd[t],
+                                 M.d_abort));
+            parity[t] = b->buf.parity;
+            b->buf.parity ^= 1;
+            if (pass == 1) {
+                unsigned char *hs = M.h_buf + pad16(M.mtab) + (size_t)t * M.per_step;
+                memcpy(hs, b->h_gather_tab, pp[t].gtab_bytes);
+                memcpy(hs + pad16(M.gtab), b->buf.h_tab, tabb[t]);
+            }
+        }
+        GPMA_TRY(batch_bfs_plan(b, graphs, srcs, nsrc, k, nullptr, &bp, M.d_abort));
+        if (pass == 0) {
+            size_t gtab = 0, utab = 0;
+            for (uint32_t t = 0; t < S; ++t) {
+                gtab = std::max(gtab, pp[t].gtab_bytes);
+                utab = std::max(utab, tabb[t]);
+            }
+            M.mtab = bp.tab_bytes;
+            M.gtab = gtab;
+            M.utab = utab;
+            M.stat = b->buf.stat_slot;
+            M.ctl = bp.ctl_bytes;
+            M.reach = bp.reached_bytes;
+            M.per_step = pad16(M.gtab) + pad16(M.utab) + pad16(M.stat) + pad16(M.ctl) + pad16(M.reach);
+            const size_t need = pad16(M.mtab) + (size_t)S * M.per_step;
+            if (need > M.h_bytes) {
+                drop_multi_graph(st);  // its nodes point into the old staging
+                if (M.h_buf)
+                    cudaFreeHost(M.h_buf);
+                M.h_buf = nullptr;
+                M.h_bytes = 0;
+                GPMA_CUDA(cudaMallocHost((void **)&M.h_buf, need));
+                M.h_bytes = need;
+            }
+        } else {
+            memcpy(M.h_buf, b->h_ms_tab, bp.tab_bytes);
+        }
+    }
+    b->buf.parity = p0;
+    const size_t o_utab = pad16(M.gtab), o_stat = o_utab + pad16(M.utab), o_ctl = o_stat + pad16(M.stat),
+                 o_reach = o_ctl + pad16(M.ctl);
+    // what the nodes hold besides kernel arguments
+    std::vector<unsigned char> baked;
+    put(baked, S);
+    put(baked, (const void *)M.h_buf);
+    put(baked, (const void *)M.d_abort);
+    put(baked, M.per_step);
+    put(baked, (const void *)b->ms_tab);
+    put(baked, (const void *)b->ms_ctl);
+    put(baked, (const void *)b->ms_reached);
+    put(baked, bp.tab_bytes);
+    put(baked, bp.ctl_bytes);
+    put(baked, bp.reached_bytes);
+    for (int i = 0; i < BatchBfsPlan::CLEARS; ++i) {
+        put(baked, bp.clear_ptr[i]);
+        put(baked, bp.clear_bytes[i]);
+    }
+    put(baked, bp.main.func);
+    put(baked, bp.main.grid.x);
+    put(baked, (const void *)b->gather_tab);
+    put(baked, (const void *)b->buf.d_tab);
+    put(baked, (const void *)b->buf.d_stat);
+    put(baked, b->buf.stat_slot);
+    for (uint32_t t = 0; t < S; ++t) {  // (grids are kernel arguments too: refreshed in place)
+        put(baked, pp[t].gtab_bytes);
+        put(baked, pp[t].gather.func);
+        put(baked, tabb[t]);
+        put(baked, upd[t].func);
+        put(baked, upd[t].smem);
+        put(baked, parity[t]);
+        put(baked, pp[t].m);
+    }
+    if (!M.exec || baked != M.baked) {
+        drop_multi_graph(st);
+        GPMA_CUDA(cudaGraphCreate(&M.graph, 0));
+        Chain c{M.graph};
+        GPMA_TRY(c.zero(M.d_abort, sizeof(uint32_t)));
+        GPMA_TRY(c.copy(b->ms_tab, M.h_buf, bp.tab_bytes, cudaMemcpyHostToDevice));
+        M.n_gather.assign(S, nullptr);
+        M.n_update.assign(S, nullptr);
+        M.n_ms.assign(S, nullptr);
+        M.gather.assign(pp.size(), KernelLaunch());
+        M.upd.assign(S, KernelLaunch());
+        M.ms.assign(S, KernelLaunch());
+        for (uint32_t t = 0; t < S; ++t) {
+            unsigned char *hs = M.h_buf + pad16(M.mtab) + (size_t)t * M.per_step;
+            unsigned char *slot = b->buf.d_stat + parity[t] * b->buf.stat_slot;
+            GPMA_TRY(c.copy(b->gather_tab, hs, pp[t].gtab_bytes, cudaMemcpyHostToDevice));
+            GPMA_TRY(c.kernel(pp[t].gather, false, &M.n_gather[t]));
+            GPMA_TRY(c.copy(b->buf.d_tab, hs + o_utab, tabb[t], cudaMemcpyHostToDevice));
+            GPMA_TRY(c.kernel(upd[t], true, &M.n_update[t]));
+            GPMA_TRY(c.copy(hs + o_stat, slot, b->buf.stat_slot, cudaMemcpyDeviceToHost));
+            GateArgs ga{slot, pp[t].m, M.d_abort};
+            KernelLaunch gate;
+            gate.set((const void *)step_gate_kernel, 1, 0, &ga, sizeof(ga));
+            cudaGraphNode_t gn = nullptr;
+            GPMA_TRY(c.kernel(gate, false, &gn));
+            for (int i = 0; i < BatchBfsPlan::CLEARS; ++i)
+                GPMA_TRY(c.zero(bp.clear_ptr[i], bp.clear_bytes[i]));
+            GPMA_TRY(c.kernel(bp.main, true, &M.n_ms[t]));
+            GPMA_TRY(c.copy(hs + o_ctl, b->ms_ctl, bp.ctl_bytes, cudaMemcpyDeviceToHost));
+            GPMA_TRY(c.copy(hs + o_reach, b->ms_reached, bp.reached_bytes, cudaMemcpyDeviceToHost));
+            M.gather[t] = pp[t].gather;
+            M.upd[t] = upd[t];
+            M.ms[t] = bp.main;
+        }
+        GPMA_CUDA(cudaGraphInstantiate(&M.exec, M.graph, 0));
+        M.steps = S;
+        M.baked = baked;
+        st->stats.builds++;
+    } else {
+        for (uint32_t t = 0; t < S; ++t) {
+            GPMA_TRY(refresh_kernel(M.exec, M.n_gather[t], pp[t].gather, M.gather[t], &st->stats.param_updates));
+            GPMA_TRY(refresh_kernel(M.exec, M.n_update[t], upd[t], M.upd[t], &st->stats.param_updates));
+            GPMA_TRY(refresh_kernel(M.exec, M.n_ms[t], bp.main, M.ms[t], &st->stats.param_updates));
+        }
+    }
+    GPMA_TRY(update_clear(b->buf, s));
+    GPMA_CUDA(cudaEventRecord(st->ev[0], s));
+    GPMA_CUDA(cudaGraphLaunch(M.exec, s));
+    GPMA_CUDA(cudaEventRecord(st->ev[1], s));
+    GPMA_CUDA(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, st->ev[0], st->ev[1]) != cudaSuccess) {
+        cudaGetLastError();
+        ms = 0.f;
+    }
+    st->stats.last_ms = ms;
+    st->stats.total_ms += ms;
+    st->stats.graph_launches++;
+    // the steps in order, exactly as batch_step_run finishes one
+    for (uint32_t t = 0; t < S; ++t) {
+        const unsigned char *hs = M.h_buf + pad16(M.mtab) + (size_t)t * M.per_step;
+        const unsigned char *stat = hs + o_stat;
+        if (reinterpret_cast<const DeviceStatus *>(stat)->stamp[0] == 0) {
+            set_error("gpma_batch_step_run_many: recorded step %u did not run", t);
+            b->buf.dirty = true;
+            return GPMA_ERR_DEVICE;
+        }
+        st->stats.runs++;
+        const uint64_t *o = off_of(t);
+        for (uint32_t i = 0; i < k; ++i) {
+            graphs[i]->stats.updates++;
+            graphs[i]->stats.submitted += o[i + 1] - o[i];
+        }
+        b->prof.kernel_launches += 2;  // gather and update; the BFS is counted by its finish
+        const bool host_work = update_needs_host(stat, pp[t].m);
+        GPMA_TRY(update_finish(pp[t].gs.data(), pp[t].m, b->buf, stat, s, nullptr, 0.0));
+        if (host_work) {
+            // the recording stopped after this update: its BFS and the later
+            // steps run on the array the host work left
+            st->stats.host_runs++;
+            GPMA_TRY(batch_bfs_run(b, graphs, srcs, nsrc, k, nullptr, reach_of(t), s));
+            return one_by_one(t + 1);
+        }
+        memcpy(b->h_ms_ctl, hs + o_ctl, bp.ctl_bytes);
+        memcpy(b->h_ms_reached, hs + o_reach, bp.reached_bytes);
+        GPMA_TRY(batch_bfs_finish(b, nsrc, k, reach_of(t)));
+    }
+    return GPMA_OK;
+}
+
 }  // namespace gpma
 
 extern "C" {
@@ -584,6 +849,10 @@ gpma_status gpma_batch_step_destroy(gpma_batch_step *st) {
     if (!st)
         return GPMA_OK;
     gpma::drop_batch_graph(st);
+    gpma::drop_multi_graph(st);
+    if (st->multi.h_buf)
+        cudaFreeHost(st->multi.h_buf);
+    gpma::dev_free(st->multi.d_abort);
     for (int i = 0; i < 2; ++i)
         if (st->ev[i])
             cudaEventDestroy(st->ev[i]);
@@ -593,6 +862,47 @@ gpma_status gpma_batch_step_destroy(gpma_batch_step *st) {
     return GPMA_OK;
 }
 
+namespace {
+
+// Arguments of one batched step (`who` names the entry point in messages).
+gpma_status check_batch_step(const char *who, const gpma_batch_step *st, const uint64_t *keys, const uint8_t *values,
+                             const uint64_t *offsets, const uint32_t *const *srcs, const uint32_t *nsrc) {
+    const uint32_t k = (uint32_t)st->graphs.size();
+    if (offsets[k] > offsets[0] && (!keys || !values)) {
+        gpma::set_error("%s: null keys or values", who);
+        return GPMA_ERR_INVALID;
+    }
+    if (offsets[k] - offsets[0] >= (1ull << 31)) {
+        gpma::set_error("%s: %llu keys in one step exceed 2^31", who, (unsigned long long)(offsets[k] - offsets[0]));
+        return GPMA_ERR_CAPACITY;
+    }
+    uint64_t nodes = 0;
+    for (uint32_t i = 0; i < k; ++i) {
+        if (offsets[i + 1] < offsets[i]) {
+            gpma::set_error("%s: decreasing offsets at %u", who, i);
+            return GPMA_ERR_INVALID;
+        }
+        if (!srcs[i] || nsrc[i] == 0 || nsrc[i] > 64) {
+            gpma::set_error("%s: graph %u: null sources or source count not in 1..64", who, i);
+            return GPMA_ERR_INVALID;
+        }
+        for (uint32_t j = 0; j < nsrc[i]; ++j)
+            if (srcs[i][j] >= st->graphs[i]->row_num) {
+                gpma::set_error("%s: graph %u: source %u out of range (row_num %u)", who, i, srcs[i][j],
+                                st->graphs[i]->row_num);
+                return GPMA_ERR_INVALID;
+            }
+        nodes += st->graphs[i]->row_num;
+    }
+    if (nodes >= (1ull << 32)) {
+        gpma::set_error("%s: %llu nodes in one step exceed 2^32", who, (unsigned long long)nodes);
+        return GPMA_ERR_CAPACITY;
+    }
+    return GPMA_OK;
+}
+
+}  // namespace
+
 gpma_status gpma_batch_step_run(gpma_batch_step *st, const uint64_t *keys, const uint8_t *values,
                                 const uint64_t *offsets, const uint32_t *const *srcs, const uint32_t *nsrc,
                                 uint64_t *reached, void *stream) {
@@ -601,39 +911,26 @@ gpma_status gpma_batch_step_run(gpma_batch_step *st, const uint64_t *keys, const
         gpma::set_error("gpma_batch_step_run: null argument");
         return GPMA_ERR_INVALID;
     }
-    const uint32_t k = (uint32_t)st->graphs.size();
-    if (offsets[k] > offsets[0] && (!keys || !values)) {
-        gpma::set_error("gpma_batch_step_run: null keys or values");
+    GPMA_TRY(check_batch_step("gpma_batch_step_run", st, keys, values, offsets, srcs, nsrc));
+    return gpma::batch_step_run(st, keys, values, offsets, srcs, nsrc, reached, (cudaStream_t)stream);
+}
+
+gpma_status gpma_batch_step_run_many(gpma_batch_step *st, uint32_t steps, const uint64_t *const *keys,
+                                     const uint8_t *const *values, const uint64_t *offsets,
+                                     const uint32_t *const *srcs, const uint32_t *nsrc, uint64_t *reached,
+                                     void *stream) {
+    gpma::CallRange range("gpma_batch_step_run_many");
+    if (!st || !offsets || !srcs || !nsrc || (steps && (!keys || !values))) {
+        gpma::set_error("gpma_batch_step_run_many: null argument");
         return GPMA_ERR_INVALID;
     }
-    if (offsets[k] - offsets[0] >= (1ull << 31)) {
-        gpma::set_error("gpma_batch_step_run: %llu keys in one step exceed 2^31",
-                        (unsigned long long)(offsets[k] - offsets[0]));
-        return GPMA_ERR_CAPACITY;
-    }
-    uint64_t nodes = 0;
-    for (uint32_t i = 0; i < k; ++i) {
-        if (offsets[i + 1] < offsets[i]) {
-            gpma::set_error("gpma_batch_step_run: decreasing offsets at %u", i);
-            return GPMA_ERR_INVALID;
-        }
-        if (!srcs[i] || nsrc[i] == 0 || nsrc[i] > 64) {
-            gpma::set_error("gpma_batch_step_run: graph %u: null sources or source count not in 1..64", i);
-            return GPMA_ERR_INVALID;
-        }
-        for (uint32_t j = 0; j < nsrc[i]; ++j)
-            if (srcs[i][j] >= st->graphs[i]->row_num) {
-                gpma::set_error("gpma_batch_step_run: graph %u: source %u out of range (row_num %u)", i, srcs[i][j],
-                                st->graphs[i]->row_num);
-                return GPMA_ERR_INVALID;
-            }
-        nodes += st->graphs[i]->row_num;
-    }
-    if (nodes >= (1ull << 32)) {
-        gpma::set_error("gpma_batch_step_run: %llu nodes in one step exceed 2^32", (unsigned long long)nodes);
-        return GPMA_ERR_CAPACITY;
-    }
-    return gpma::batch_step_run(st, keys, values, offsets, srcs, nsrc, reached, (cudaStream_t)stream);
+    const uint32_t k = (uint32_t)st->graphs.size();
+    for (uint32_t t = 0; t < steps; ++t)
+        GPMA_TRY(check_batch_step("gpma_batch_step_run_many", st, keys[t], values[t], offsets + (size_t)t * (k + 1),
+                                  srcs, nsrc));
+    if (steps == 0)
+        return GPMA_OK;
+    return gpma::batch_step_run_many(st, steps, keys, values, offsets, srcs, nsrc, reached, (cudaStream_t)stream);
 }
 
 gpma_status gpma_batch_step_get_stats(const gpma_batch_step *st, gpma_step_stats *out) {

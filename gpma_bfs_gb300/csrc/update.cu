@@ -108,6 +108,7 @@ struct UpdateArgs {
     uint32_t stall;
     uint64_t stall_limit_ns;
     uint64_t *top;  // one graph: its LOCATE_CACHE top-of-tree heads gathered contiguously
+    const uint32_t *abort;  // non-zero: return at once (a recorded step after one needing host work)
 };
 
 
@@ -839,6 +840,8 @@ template <int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint32_t tmp[BLOCK / 32 + 1];
+    if (A.abort && ld_volatile(A.abort))
+        return;  // every CTA: nothing written, the status slot stays as the previous launch left it
     DeviceStatus *st = A.st;
     const bool stamper = blockIdx.x == 0 && threadIdx.x == 0;
     if (stamper)
@@ -2414,7 +2417,7 @@ gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
 }
 
 gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t k, BatchBuffers &buf, int sms,
-                        bool check_keys, size_t *tab_bytes, KernelLaunch *L) {
+                        bool check_keys, size_t *tab_bytes, KernelLaunch *L, const uint32_t *abort) {
     static_assert(sizeof(UpdateArgs) <= KernelLaunch::ARG_BYTES, "update arguments exceed the launch record");
     const uint64_t n = off[k];
     if (n >= (1ull << 31)) {
@@ -2572,6 +2575,7 @@ gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t
     A.hist_words = hist_rows * 2048;
     A.status_words = (uint32_t)status_words;
     A.top = buf.top;
+    A.abort = abort;
     A.stall = g_test_hooks.update_stall;
     A.stall_limit_ns = g_test_hooks.update_stall ? g_test_hooks.wait_limit_ns : WAIT_LIMIT_NS;
     L->set(update_kernel_ptr(update_variant(n)), grid, UPDATE_SMEM, &A, sizeof(A));

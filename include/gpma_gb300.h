@@ -220,6 +220,20 @@ GPMA_API gpma_status gpma_batch_step_destroy(gpma_batch_step *st);
 GPMA_API gpma_status gpma_batch_step_run(gpma_batch_step *st, const uint64_t *keys, const uint8_t *values,
                                          const uint64_t *offsets, const uint32_t *const *srcs, const uint32_t *nsrc,
                                          uint64_t *reached, void *stream);
+/* `steps` consecutive steps recorded in one CUDA graph and launched once: step
+ * t applies keys[t]/values[t] (device memory) with offsets at offsets + t * (k
+ * + 1), then searches from srcs/nsrc (the same sources every step); reached
+ * (optional, host) receives steps x sum(nsrc) counts, step by step. The
+ * recording is kept and replayed while the buffers and launch shapes it holds
+ * stay the same (kernel arguments are refreshed in place). A step whose
+ * update needs host work stops the recorded steps after it on the device;
+ * that step and the later ones then finish as gpma_batch_step_run would, as
+ * do all steps when one part is empty or bulk-sized or a batch is in host
+ * memory. Results are always those of the per-step calls. */
+GPMA_API gpma_status gpma_batch_step_run_many(gpma_batch_step *st, uint32_t steps, const uint64_t *const *keys,
+                                              const uint8_t *const *values, const uint64_t *offsets,
+                                              const uint32_t *const *srcs, const uint32_t *nsrc, uint64_t *reached,
+                                              void *stream);
 GPMA_API gpma_status gpma_batch_step_get_stats(const gpma_batch_step *st, gpma_step_stats *out);
 
 /* ---- served form ----------------------------------------------------------

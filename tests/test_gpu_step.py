@@ -149,3 +149,108 @@ def test_batch_step_matches_eager_calls(built_lib):
     br.close()
     for g in ge + gr:
         g.close()
+
+
+def _batched_pair(count, seed):
+    """Two identical sets of graphs (eager and recorded) after the same load."""
+    import gpma_bfs_gb300 as G
+    from gpma_bfs_gb300.workloads import SlidingStream, batched_graphs
+
+    specs = batched_graphs(count, seed=seed, min_edges=5_000, max_edges=200_000)
+    ge = [G.GPMA(n) for n, _ in specs]
+    gr = [G.GPMA(n) for n, _ in specs]
+    se = [SlidingStream(k) for _, k in specs]
+    sr = [SlidingStream(k) for _, k in specs]
+    be, br = G.Batch(), G.Batch()
+    loads = [s.load() for s in se]
+    for s in sr:
+        s.load()
+    off = np.concatenate([[0], np.cumsum([len(x[0]) for x in loads])]).astype(np.uint64)
+    keys, vals = np.concatenate([x[0] for x in loads]), np.concatenate([x[1] for x in loads])
+    be.update_packed(ge, keys, vals, off)
+    br.update_packed(gr, keys, vals, off)
+    return specs, ge, gr, se, be, br
+
+
+def _packed_steps(rng, streams, steps, lo=50, hi=40_000):
+    import torch
+
+    ks, vs, offs = [], [], []
+    for _ in range(steps):
+        sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), len(streams))).astype(np.int64)
+        parts = [s.step(int(z)) for s, z in zip(streams, sizes)]
+        offs.append(np.concatenate([[0], np.cumsum([len(p[0]) for p in parts])]).astype(np.uint64))
+        ks.append(torch.from_numpy(np.concatenate([p[0] for p in parts]).view(np.int64)).cuda())
+        vs.append(torch.from_numpy(np.concatenate([p[1] for p in parts])).cuda())
+    return ks, vs, offs
+
+
+def _check_many(specs, ge, gr, be, got, ks, vs, offs, sources):
+    for t in range(len(ks)):
+        be.update_packed(ge, ks[t], vs[t], offs[t])
+        want = be.bfs_multi(ge, sources)[1]
+        assert all(np.array_equal(x, y) for x, y in zip(want, got[t])), f"step {t}: reach"
+    for i in range(len(specs)):
+        assert all(np.array_equal(x, y) for x, y in zip(ge[i].export_layout(), gr[i].export_layout())), f"graph {i}"
+        assert gr[i].validate() == 0
+
+
+def test_batch_steps_recorded_in_one_graph(built_lib):
+    """Twelve steps of 20 graphs in one graph launch equal the per-step eager
+    calls (every step's reach, the final layouts); the recording is replayed
+    for the next twelve with its kernel arguments refreshed."""
+    specs, ge, gr, se, be, br = _batched_pair(20, seed=31)
+    rng = np.random.default_rng(32)
+    sources = [rng.choice(n, 8, replace=False).astype(np.uint32) for n, _ in specs]
+    step = br.step(gr)
+    for call in range(2):
+        ks, vs, offs = _packed_steps(rng, se, 12)
+        got = step.run_many(ks, vs, offs, sources)
+        _check_many(specs, ge, gr, be, got, ks, vs, offs, sources)
+    st = step.stats()
+    assert st["runs"] == 24 and st["graph_launches"] == 2 and st["host_runs"] == 0
+    assert st["builds"] == 1 and st["param_updates"] > 0
+    step.close()
+    be.close()
+    br.close()
+    for g in ge + gr:
+        g.close()
+
+
+def test_batch_steps_recorded_stop_at_host_work(built_lib):
+    """A step whose update needs host work (a burst of new edges grows one
+    graph past its root) stops the recorded steps after it; that step and the
+    rest finish through the per-step path with identical results."""
+    import torch
+
+    specs, ge, gr, se, be, br = _batched_pair(8, seed=41)
+    rng = np.random.default_rng(42)
+    sources = [rng.choice(n, 4, replace=False).astype(np.uint32) for n, _ in specs]
+    step = br.step(gr)
+    ks, vs, offs = _packed_steps(rng, se, 6)
+    # step 2: graph 0 also receives a burst of new edges, more than its array holds
+    n0 = specs[0][0]
+    size0 = gr[0].geometry()["size"]
+    extra = np.unique((rng.integers(0, n0, 2 * size0).astype(np.uint64) << np.uint64(32)) |
+                      rng.integers(0, n0, 2 * size0).astype(np.uint64))
+    k2 = ks[2].cpu().numpy().view(np.uint64)
+    v2 = vs[2].cpu().numpy()
+    o2 = offs[2]
+    # none of the step's own keys again (a present key given two values in one
+    # batch would be written twice in place, in no fixed order)
+    extra = np.setdiff1d(extra, k2)
+    cut = int(o2[1])
+    k2 = np.concatenate([k2[:cut], extra, k2[cut:]])
+    v2 = np.concatenate([v2[:cut], np.ones(len(extra), np.uint8), v2[cut:]])
+    offs[2] = np.concatenate([[0], o2[1:] + np.uint64(len(extra))]).astype(np.uint64)
+    ks[2] = torch.from_numpy(k2.view(np.int64)).cuda()
+    vs[2] = torch.from_numpy(v2).cuda()
+    got = step.run_many(ks, vs, offs, sources)
+    _check_many(specs, ge, gr, be, got, ks, vs, offs, sources)
+    st = step.stats()
+    assert st["runs"] == 6 and st["host_runs"] >= 1 and st["graph_launches"] >= 1
+    step.close()
+    be.close()
+    br.close()
+    for g in ge + gr:
+        g.close()
