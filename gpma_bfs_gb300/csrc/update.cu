@@ -927,9 +927,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
     if (stamper)
         st->stamp[1] = globaltimer_ns();
 
-    // P1: locate every update, applying deletes / modifies in place. With one
-    // graph, the top of the descent comes from a shared-memory copy of the
-    // first keys at every `stride`-th slot.
+    // P1: locate every update, applying deletes / modifies in place. The top
+    // of the descent comes from a shared-memory copy of the first keys at
+    // every `stride`-th slot (of the one graph, or of each graph in turn).
     {
         const uint64_t *fk = nullptr;
         uint32_t log2stride = 0;
@@ -968,12 +968,40 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             if (threadIdx.x == 0)
                 CNT(scan_id)[blockIdx.x] = t;
         } else {
-            // many graphs: keys interleaved over the grid (measured faster
-            // than contiguous ranges, which mix trees of unequal height)
-            const uint32_t stride = G * BLOCK;
-            for (uint32_t i0 = blockIdx.x * BLOCK + threadIdx.x; i0 < A.n; i0 += LOC_ILP * stride)
-                locate_keys<false>(A, bk, bv, i0, stride, A.n, fk, log2stride);
-            __syncthreads();
+            // many graphs: each CTA takes a contiguous range of the sorted
+            // batches (a graph or two) and, graph by graph, copies the graph's
+            // top-of-tree heads into shared memory, so its keys walk the upper
+            // levels there as with one graph
+            uint64_t *f = reinterpret_cast<uint64_t *>(smem);
+            uint32_t lo, hi;
+            cta_range(A.n, lo, hi);
+            uint32_t pos = lo;
+            while (__syncthreads_or(pos < hi)) {
+                const uint32_t g = segment_of(A.boff, A.G, pos);
+                const uint32_t end = min(hi, A.boff[g + 1]);
+                const GraphDesc &D = A.gd[g];
+                const uint32_t segs = D.size >> D.log2seg;
+                const uint32_t cached = segs < LOCATE_CACHE ? segs : LOCATE_CACHE;
+                const uint32_t l2s = 31 - __clz(D.size / cached);
+                const uint32_t hstep = l2s - D.log2seg;
+                uint64_t hv[LOCATE_CACHE / BLOCK];
+#pragma unroll
+                for (uint32_t r = 0; r < LOCATE_CACHE / BLOCK; ++r) {
+                    const uint32_t j = threadIdx.x + r * BLOCK;
+                    hv[r] = j < cached ? D.heads[(size_t)j << hstep] : 0ull;
+                }
+#pragma unroll
+                for (uint32_t r = 0; r < LOCATE_CACHE / BLOCK; ++r) {
+                    const uint32_t j = threadIdx.x + r * BLOCK;
+                    if (j < cached)
+                        f[j] = hv[r];
+                }
+                __syncthreads();
+                for (uint32_t i0 = pos + threadIdx.x; i0 < end; i0 += LOC_ILP * BLOCK)
+                    locate_keys<false>(A, bk, bv, i0, BLOCK, end, f, l2s);
+                __syncthreads();  // the copy is replaced for the next graph
+                pos = end;
+            }
         }
     }
     if (!grid_barrier(&st->bar, &st->err))
