@@ -388,6 +388,8 @@ gpma_status gpma_update(gpma_graph *g, const uint64_t *keys, const uint8_t *valu
         return GPMA_OK;
     cudaStream_t s = (cudaStream_t)stream;
     GPMA_TRY(ensure_buffers(g->buf, n, 1));
+    if (is_device_pointer(keys) && is_device_pointer(values))
+        return update_device(g, n, s, true, keys, values);  // the kernel reads the caller's batch in place
     GPMA_TRY(copy_in(g, g->buf.bkeys[0], keys, n * sizeof(uint64_t), s));
     GPMA_TRY(copy_in(g, g->buf.bvals[0], values, n, s));
     return update_device(g, n, s);

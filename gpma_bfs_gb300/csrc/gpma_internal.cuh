@@ -185,6 +185,11 @@ struct BatchBuffers {
     uint32_t *toff = nullptr;
     uint32_t *qoff = nullptr;
     uint32_t *qtoff = nullptr;
+    // host copy of what d_tab holds after update_graphs' last upload (an
+    // identical table is not uploaded again); anything else that writes
+    // d_tab clears tab_shadow_valid
+    std::vector<unsigned char> tab_shadow;
+    bool tab_shadow_valid = false;
     // status, double-buffered: a slot is [DeviceStatus][GraphStatus x gcap]
     // (GraphStatus from STAT_GS_OFFSET); each launch zeroes the other slot and
     // the sort state it used, so steady-state launches need no memsets
@@ -398,9 +403,12 @@ gpma_status count_bad_heads(gpma_graph *g, cudaStream_t s, uint64_t *bad);
 // One launch updating graphs[0..k) with the batches already staged in
 // buf.bkeys[0]/bvals[0] at offsets off[0..k]. Graphs must be ordered by
 // segment length. check_keys=false only for the internal guard insertion.
+// in_k / in_v: the batch in device memory elsewhere (read in place) instead.
 gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32_t k, BatchBuffers &buf, int sms,
-                          cudaStream_t s, bool check_keys, bool profiling, cudaEvent_t *ev, gpma_profile *prof);
-gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys = true);
+                          cudaStream_t s, bool check_keys, bool profiling, cudaEvent_t *ev, gpma_profile *prof,
+                          const uint64_t *in_k = nullptr, const uint8_t *in_v = nullptr);
+gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys = true,
+                          const uint64_t *in_k = nullptr, const uint8_t *in_v = nullptr);
 // The three host parts of update_graphs, for callers that enqueue the launch
 // themselves (a CUDA graph step). update_plan sizes the buffers, fills the
 // pinned tables (*tab_bytes of buf.h_tab to upload to buf.d_tab) and records
@@ -412,8 +420,11 @@ gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_
 // for host work or reports an error (the array changed after the kernel).
 // A non-null `abort` (a device word) makes the launch return at once while
 // the word is non-zero (steps recorded after one that needs host work).
+// in_k / in_v (device, optional): the batch is read from there instead of
+// buf.bkeys[0] / buf.bvals[0] (which the sort then only writes).
 gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t k, BatchBuffers &buf, int sms,
-                        bool check_keys, size_t *tab_bytes, KernelLaunch *L, const uint32_t *abort = nullptr);
+                        bool check_keys, size_t *tab_bytes, KernelLaunch *L, const uint32_t *abort = nullptr,
+                        const uint64_t *in_k = nullptr, const uint8_t *in_v = nullptr);
 gpma_status update_clear(BatchBuffers &buf, cudaStream_t s);
 size_t update_status_bytes(uint32_t k);
 gpma_status update_finish(gpma_graph *const *graphs, uint32_t k, BatchBuffers &buf, const unsigned char *stat,

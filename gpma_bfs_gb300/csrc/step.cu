@@ -274,6 +274,7 @@ gpma_status step_run(gpma_step *st, const uint64_t *keys, const uint8_t *values,
         GPMA_TRY(update_clear(g->buf, s));
         const unsigned char *stat = st->h_stat + g->buf.parity * g->buf.stat_slot;
         GPMA_CUDA(cudaEventRecord(st->ev[0], s));
+        g->buf.tab_shadow_valid = false;  // the graph uploads its own table
         GPMA_CUDA(cudaGraphLaunch(st->exec, s));
         GPMA_CUDA(cudaEventRecord(st->ev[1], s));
         GPMA_CUDA(cudaStreamSynchronize(s));
@@ -502,6 +503,7 @@ gpma_status batch_step_run(gpma_batch_step *st, const uint64_t *keys, const uint
     GPMA_TRY(update_clear(b->buf, s));
     const unsigned char *stat = st->h_stat + b->buf.parity * b->buf.stat_slot;
     GPMA_CUDA(cudaEventRecord(st->ev[0], s));
+    b->buf.tab_shadow_valid = false;  // the graph uploads its own table
     GPMA_CUDA(cudaGraphLaunch(st->exec, s));
     GPMA_CUDA(cudaEventRecord(st->ev[1], s));
     GPMA_CUDA(cudaStreamSynchronize(s));
@@ -700,6 +702,7 @@ gpma_status batch_step_run_many(gpma_batch_step *st, uint32_t S, const uint64_t 
     }
     GPMA_TRY(update_clear(b->buf, s));
     GPMA_CUDA(cudaEventRecord(st->ev[0], s));
+    b->buf.tab_shadow_valid = false;  // the graph uploads its own tables
     GPMA_CUDA(cudaGraphLaunch(M.exec, s));
     GPMA_CUDA(cudaEventRecord(st->ev[1], s));
     GPMA_CUDA(cudaStreamSynchronize(s));

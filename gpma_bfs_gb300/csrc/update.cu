@@ -75,7 +75,9 @@ struct UpdateArgs {
     const uint32_t *boff;   // batch offsets, G + 1
     const uint32_t *toff;   // sort tile offsets, G + 1
     uint32_t n;
-    uint64_t *bk[2];        // batches, ping-pong buffers of the radix sort (input in [0])
+    const uint64_t *in_k;   // the batch as submitted (bk[0] or the caller's device buffer; only read)
+    const uint8_t *in_v;
+    uint64_t *bk[2];        // batches, ping-pong buffers of the sort
     uint8_t *bv[2];
     uint32_t *sort_hist;    // [G + 1][8][256] digit counts (zeroed per update)
     uint32_t *sort_tiles;   // 8 tile counters (zeroed per update)
@@ -866,7 +868,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
     const uint8_t *bv = A.bv[1];
     bool digits = A.q.nq == 0;
     if (!digits) {
-        bsort_rank(A.bk[0], A.boff, A.G, A.gd, A.q, st, A.check_keys);
+        bsort_rank(A.in_k, A.boff, A.G, A.gd, A.q, st, A.check_keys);
         if (!grid_barrier(&st->bar, &st->err, A.stall, A.stall_limit_ns))
             return;
         if (ld_volatile(&st->invalid_keys) != 0)
@@ -876,10 +878,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             return;
         digits = cta_broadcast_read(&st->sort_fallback) != 0;
         if (!digits) {
-            // records of bk[0] / bv[0] scattered into buckets, then items sorted into bk[0] / bv[1]
+            // records of the batch scattered into buckets, then items sorted into bk[0] / bv[1]
             uint32_t *cpre = reinterpret_cast<uint32_t *>(smem + BSORT_SMEM_ITEM);
             bsort_chunk_prefix(A.cta_cnt, cpre, tmp);
-            bsort_scatter(A.bk[0], A.bv[0], A.boff, A.G, A.q, cpre);
+            bsort_scatter(A.in_k, A.in_v, A.boff, A.G, A.q, cpre);
             if (!grid_barrier(&st->bar, &st->err))
                 return;
             bsort_items(A.bk[0], A.bv[1], A.boff, A.G, A.q, cpre, smem);
@@ -888,22 +890,24 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         }
     }
     if (digits) {
-        sort_histogram(A.bk[0], A.boff, A.G, A.sort_hist, st, A.check_keys, reinterpret_cast<uint32_t *>(smem));
+        sort_histogram(A.in_k, A.boff, A.G, A.sort_hist, st, A.check_keys, reinterpret_cast<uint32_t *>(smem));
         if (!grid_barrier(&st->bar, &st->err, A.q.nq == 0 ? A.stall : 0u, A.stall_limit_ns))
             return;
         if (ld_volatile(&st->invalid_keys) != 0)
             return;  // reserved-column keys: reject the batch before any change
         uint32_t sel = 0;
+        bool first = true;  // the first pass reads the batch as submitted
         {
             const uint32_t trivial = sort_trivial_mask(A.sort_hist + (size_t)(A.G == 1 ? 0 : A.G) * 2048, A.n);
             const uint32_t tiles = A.toff[A.G];
             for (int p = 0; p < 8; ++p) {
                 if (trivial & (1u << p))
                     continue;
-                const uint64_t *ink = sel ? A.bk[1] : A.bk[0];
-                const uint8_t *inv = sel ? A.bv[1] : A.bv[0];
+                const uint64_t *ink = first ? A.in_k : (sel ? A.bk[1] : A.bk[0]);
+                const uint8_t *inv = first ? A.in_v : (sel ? A.bv[1] : A.bv[0]);
                 uint64_t *outk = sel ? A.bk[0] : A.bk[1];
                 uint8_t *outv = sel ? A.bv[0] : A.bv[1];
+                first = false;
                 // CTA b takes tiles b, b + G, b + 2G, ... in order: every look-back
                 // waits on lower tiles only, and the lowest unfinished tile never
                 // waits on anything unfinished, so the pass always progresses
@@ -915,8 +919,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
                     return;
             }
         }
-        bk = sel ? A.bk[1] : A.bk[0];
-        bv = sel ? A.bv[1] : A.bv[0];
+        bk = first ? A.in_k : (sel ? A.bk[1] : A.bk[0]);  // no pass: every digit constant
+        bv = first ? A.in_v : (sel ? A.bv[1] : A.bv[0]);
     }
     const uint32_t G = gridDim.x;
 
@@ -2360,6 +2364,7 @@ void free_buffers(BatchBuffers &b) {
     b.q_cap = 0;
     b.qrec_cap = 0;
     b.qbound_cap = 0;
+    b.tab_shadow_valid = false;
 }
 
 gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
@@ -2432,6 +2437,7 @@ gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
         if (e != cudaSuccess)
             return cuda_fail(e, "cudaMallocHost(update tables)");
         b.gd = reinterpret_cast<GraphDesc *>(b.d_tab);
+        b.tab_shadow_valid = false;
         b.boff = reinterpret_cast<uint32_t *>(b.d_tab + sizeof(GraphDesc) * gc);
         b.toff = b.boff + gc + 1;
         b.qoff = b.toff + gc + 1;
@@ -2445,7 +2451,8 @@ gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
 }
 
 gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t k, BatchBuffers &buf, int sms,
-                        bool check_keys, size_t *tab_bytes, KernelLaunch *L, const uint32_t *abort) {
+                        bool check_keys, size_t *tab_bytes, KernelLaunch *L, const uint32_t *abort,
+                        const uint64_t *in_k, const uint8_t *in_v) {
     static_assert(sizeof(UpdateArgs) <= KernelLaunch::ARG_BYTES, "update arguments exceed the launch record");
     const uint64_t n = off[k];
     if (n >= (1ull << 31)) {
@@ -2563,6 +2570,8 @@ gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t
     A.boff = buf.boff;
     A.toff = buf.toff;
     A.n = (uint32_t)n;
+    A.in_k = in_k ? in_k : buf.bkeys[0];
+    A.in_v = in_v ? in_v : buf.bvals[0];
     for (int i = 0; i < 2; ++i) {
         A.bk[i] = buf.bkeys[i];
         A.bv[i] = buf.bvals[i];
@@ -2687,13 +2696,21 @@ bool update_needs_host(const unsigned char *stat, uint32_t k) {
 }
 
 gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32_t k, BatchBuffers &buf, int sms,
-                          cudaStream_t s, bool check_keys, bool profiling, cudaEvent_t *ev, gpma_profile *prof) {
+                          cudaStream_t s, bool check_keys, bool profiling, cudaEvent_t *ev, gpma_profile *prof,
+                          const uint64_t *in_k, const uint8_t *in_v) {
     if (off[k] == 0)
         return GPMA_OK;
     size_t tab_bytes = 0;
     KernelLaunch L;
-    GPMA_TRY(update_plan(graphs, off, k, buf, sms, check_keys, &tab_bytes, &L));
-    GPMA_CUDA(cudaMemcpyAsync(buf.d_tab, buf.h_tab, tab_bytes, cudaMemcpyHostToDevice, s));
+    GPMA_TRY(update_plan(graphs, off, k, buf, sms, check_keys, &tab_bytes, &L, nullptr, in_k, in_v));
+    // the tables (descriptors, batch and bucket offsets) are the same from
+    // one slide step to the next: an identical table is not uploaded again
+    if (!buf.tab_shadow_valid || buf.tab_shadow.size() != tab_bytes ||
+        memcmp(buf.tab_shadow.data(), buf.h_tab, tab_bytes) != 0) {
+        GPMA_CUDA(cudaMemcpyAsync(buf.d_tab, buf.h_tab, tab_bytes, cudaMemcpyHostToDevice, s));
+        buf.tab_shadow.assign(buf.h_tab, buf.h_tab + tab_bytes);
+        buf.tab_shadow_valid = true;
+    }
     GPMA_TRY(update_clear(buf, s));
     prof_mark(profiling, ev, 1, s);
     GPMA_CUDA(L.launch_cooperative(s));
@@ -2706,10 +2723,11 @@ gpma_status update_graphs(gpma_graph *const *graphs, const uint64_t *off, uint32
 }
 
 // Single-graph update of the n-key batch staged in g->buf.bkeys[0]/bvals[0].
-gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys) {
+gpma_status update_device(gpma_graph *g, uint64_t n, cudaStream_t s, bool check_keys, const uint64_t *in_k,
+                          const uint8_t *in_v) {
     const uint64_t off[2] = {0, n};
     gpma_graph *gs[1] = {g};
-    return update_graphs(gs, off, 1, g->buf, g->sms, s, check_keys, g->profiling, g->ev, &g->prof);
+    return update_graphs(gs, off, 1, g->buf, g->sms, s, check_keys, g->profiling, g->ev, &g->prof, in_k, in_v);
 }
 
 }  // namespace gpma
