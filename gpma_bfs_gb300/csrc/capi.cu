@@ -34,6 +34,16 @@ gpma_status cuda_fail(cudaError_t e, const char *what) {
     return e == cudaErrorMemoryAllocation ? GPMA_ERR_NOMEM : GPMA_ERR_CUDA;
 }
 
+// The device address of page-locked host memory, or null for anything else.
+const void *mapped_host_pointer(const void *p) {
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return attr.type == cudaMemoryTypeHost ? attr.devicePointer : nullptr;
+}
+
 bool is_device_pointer(const void *p) {
     cudaPointerAttributes attr;
     if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
@@ -390,6 +400,13 @@ gpma_status gpma_update(gpma_graph *g, const uint64_t *keys, const uint8_t *valu
     GPMA_TRY(ensure_buffers(g->buf, n, 1));
     if (is_device_pointer(keys) && is_device_pointer(values))
         return update_device(g, n, s, true, keys, values);  // the kernel reads the caller's batch in place
+    {
+        // page-locked host batches: the kernel reads them over the host link
+        // itself (the keys twice: ranks, then the scatter), no staging copy
+        const void *dk = mapped_host_pointer(keys), *dv = mapped_host_pointer(values);
+        if (dk && dv)
+            return update_device(g, n, s, true, static_cast<const uint64_t *>(dk), static_cast<const uint8_t *>(dv));
+    }
     GPMA_TRY(copy_in(g, g->buf.bkeys[0], keys, n * sizeof(uint64_t), s));
     GPMA_TRY(copy_in(g, g->buf.bvals[0], values, n, s));
     return update_device(g, n, s);
