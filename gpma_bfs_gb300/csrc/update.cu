@@ -473,7 +473,8 @@ __device__ __forceinline__ void store_slots(uint64_t *keys, uint8_t *vals, uint3
 
 template <uint32_t W>
 __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32_t r1, uint32_t level,
-                             const uint64_t *pk, const uint8_t *pv, unsigned char *smem, unsigned long long &acc) {
+                             const uint64_t *pk, const uint8_t *pv, unsigned char *smem, unsigned long long &acc,
+                             uint32_t part, uint32_t parts) {
     constexpr uint32_t G = W >= 128 ? 32 : (W >= 4 ? W / 4 : 1);  // lanes per window
     constexpr uint32_t GPW = 32 / G;                                // windows per warp
     constexpr uint32_t K = W / G;                                   // slots per lane
@@ -487,10 +488,11 @@ __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
     uint8_t *pend_v = reinterpret_cast<uint8_t *>(mk + W);
     uint8_t *cv = pend_v + W;
     uint8_t *mv = cv + W;
-    const uint32_t total_warps = gridDim.x * (BLOCK / 32);
+    // windows [r0, r1) over `parts` CTAs, this one being `part`
+    const uint32_t total_warps = parts * (BLOCK / 32);
     const uint32_t g_r0 = L.graph[r0];  // stands in for groups without a window
     // the next round's window descriptor is read while this round works
-    uint32_t wbase = r0 + (blockIdx.x * (BLOCK / 32) + warp) * GPW;
+    uint32_t wbase = r0 + (part * (BLOCK / 32) + warp) * GPW;
     uint32_t n_g = g_r0, n_node = 0, n_a = 0, n_b = 0;
     if (wbase + grp < r1) {
         n_g = L.graph[wbase + grp];
@@ -609,7 +611,7 @@ __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
 template <uint32_t W>
 __device__ void cta_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32_t r1, uint32_t level,
                             const uint64_t *pk, const uint8_t *pv, unsigned char *smem, uint32_t *tmp,
-                            unsigned long long &acc) {
+                            unsigned long long &acc, uint32_t part, uint32_t parts) {
     constexpr uint32_t K = W / BLOCK;
     uint64_t *sk = reinterpret_cast<uint64_t *>(smem);
     uint64_t *ck = sk + W;
@@ -618,7 +620,7 @@ __device__ void cta_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32_
     uint8_t *cv = sv + W;
     uint8_t *mv = cv + W;
     const uint32_t tid = threadIdx.x;
-    for (uint32_t w = r0 + blockIdx.x; w < r1; w += gridDim.x) {
+    for (uint32_t w = r0 + part; w < r1; w += parts) {
         const GraphDesc &D = A.gd[L.graph[w]];
         const uint32_t node = L.node[w], a = L.a[w], b = L.b[w];
         // the same condition in every thread: the whole CTA skips the window
@@ -811,11 +813,12 @@ __device__ bool grid_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
 template <uint32_t W>
 __device__ __forceinline__ void small_dispatch(const UpdateArgs &A, Windows L, uint32_t r0, uint32_t r1,
                                                uint32_t level, const uint64_t *pk, const uint8_t *pv,
-                                               unsigned char *smem, uint32_t *tmp, unsigned long long &acc) {
+                                               unsigned char *smem, uint32_t *tmp, unsigned long long &acc,
+                                               uint32_t part, uint32_t parts) {
     if constexpr (W <= WARP_WINDOW_MAX)
-        warp_windows<W>(A, L, r0, r1, level, pk, pv, smem, acc);
+        warp_windows<W>(A, L, r0, r1, level, pk, pv, smem, acc, part, parts);
     else
-        cta_windows<W>(A, L, r0, r1, level, pk, pv, smem, tmp, acc);
+        cta_windows<W>(A, L, r0, r1, level, pk, pv, smem, tmp, acc, part, parts);
 }
 
 // First window in [0, nw) whose graph has segment length >= s (windows are
@@ -831,6 +834,80 @@ __device__ __forceinline__ uint32_t first_window_of_seg(const UpdateArgs &A, con
             hi = mid;
     }
     return lo;
+}
+
+// Rejected windows of [lo, hi) that start a window of the next level (a
+// rejected right sibling joins its rejected left sibling) into cnt_h, and
+// their insertions into cnt_i, at blockIdx.x; root windows count in neither.
+// first_is_head: window lo counts as a start whatever its left neighbour
+// (whose flag may not be written yet); head_corrections removes those that
+// are not.
+__device__ __forceinline__ void count_rejected(const UpdateArgs &A, const Windows &L, uint32_t level, uint32_t lo,
+                                               uint32_t hi, bool first_is_head, uint32_t *cnt_h, uint32_t *cnt_i) {
+    uint32_t ch = 0, ci = 0;
+    constexpr int CU = 2;  // windows per thread per step, their fields loaded together
+    for (uint32_t w0 = lo + threadIdx.x; w0 < hi; w0 += CU * BLOCK) {
+        uint32_t f0[CU], fl[CU], g[CU], gl[CU], nd[CU], ndl[CU], wa[CU], wb[CU];
+#pragma unroll
+        for (int u = 0; u < CU; ++u) {
+            // the window's and its left neighbour's fields
+            const uint32_t w = w0 + u * BLOCK;
+            const bool ok = w < hi;
+            const bool left = ok && w > 0 && !(first_is_head && w == lo);
+            f0[u] = ok ? A.wflag[w] : 1u;
+            fl[u] = left ? A.wflag[w - 1] : 1u;
+            g[u] = ok ? L.graph[w] : 0u;
+            gl[u] = left ? L.graph[w - 1] : 0u;
+            nd[u] = ok ? L.node[w] : 0u;
+            ndl[u] = left ? L.node[w - 1] : 0u;
+            wa[u] = ok ? L.a[w] : 0u;
+            wb[u] = ok ? L.b[w] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < CU; ++u) {
+            if (f0[u])
+                continue;  // accepted (or past the range)
+            const GraphDesc &Dg = A.gd[g[u]];
+            if (level >= Dg.height)
+                continue;  // root window: to the remaining buffer
+            const uint32_t W = Dg.seg << level;
+            ci += wb[u] - wa[u];
+            const uint32_t par = nd[u] & ~W;
+            const bool merged = !fl[u] && gl[u] == g[u] && (ndl[u] & ~W) == par;  // fl = 1 without a left neighbour
+            ch += merged ? 0u : 1u;
+        }
+    }
+    const uint4 t = block_sum4(make_uint4(ch, ci, 0, 0));
+    if (threadIdx.x == 0) {
+        cnt_h[blockIdx.x] = t.x;
+        cnt_i[blockIdx.x] = t.y;
+    }
+}
+
+// One graph, counts taken with first_is_head: the CTAs c >= 1 whose first
+// window was counted as a start but joins its left neighbour (both rejected,
+// not root windows, one parent): how many precede this CTA, and in all.
+__device__ __forceinline__ void head_corrections(const UpdateArgs &A, const Windows &L, uint32_t nw, uint32_t level,
+                                                 uint32_t &before, uint32_t &all) {
+    const uint32_t per = (nw + gridDim.x - 1) / gridDim.x;
+    const GraphDesc &D = A.gd[0];
+    const uint32_t W = D.seg << level;
+    const bool root = level >= D.height;
+    uint32_t b = 0, t = 0;
+    for (uint32_t c = 1 + threadIdx.x; c < gridDim.x; c += BLOCK) {
+        const uint32_t w = c * per;
+        if (root || w >= nw)
+            continue;
+        const uint32_t f0 = A.wflag[w], fl = A.wflag[w - 1];
+        const uint32_t nd = L.node[w], ndl = L.node[w - 1];
+        if (!f0 && !fl && (nd & ~W) == (ndl & ~W)) {
+            ++t;
+            b += c < blockIdx.x ? 1u : 0u;
+        }
+    }
+    const uint4 r = block_sum4(make_uint4(b, t, 0, 0));
+    before = r.x;
+    all = r.y;
 }
 
 // Two register budgets of the same kernel: MINB resident CTAs per SM. Two
@@ -1203,6 +1280,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
     // range [wa, wb) of the current insertion buffer.
     uint32_t cur = 0, level = 0;
     for (; level <= A.max_height && nw > 0; ++level) {
+        // one graph, windows of at most CTA_WINDOW_MAX slots: each CTA
+        // dispatches a contiguous range of the windows and counts its rejected
+        // ones right away, so the level needs one grid barrier fewer
+        const bool fused = A.G == 1 && (A.gd[0].seg << level) <= CTA_WINDOW_MAX;
         Windows L;
         L.node = cur ? A.wnode[1] : A.wnode[0];
         L.graph = cur ? A.wgraph[1] : A.wgraph[0];
@@ -1221,20 +1302,31 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             }
             if (r0 >= r1)
                 continue;
-            const uint32_t W = s << level;
+            uint32_t W = s << level;
             const unsigned long long before = acc;
+            // windows over the grid; with the count fused into this phase,
+            // each CTA takes the contiguous range it counts (and copies) next
+            uint32_t d0 = r0, d1 = r1, part = blockIdx.x, parts = gridDim.x;
+            if (fused) {
+                cta_range(nw, d0, d1);
+                part = 0;
+                parts = 1;
+                if (d0 >= d1)
+                    W = 0;  // nothing for this CTA: no dispatch
+            }
             switch (W) {
-            case 2: small_dispatch<2>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
-            case 4: small_dispatch<4>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
-            case 8: small_dispatch<8>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
-            case 16: small_dispatch<16>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
-            case 32: small_dispatch<32>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
-            case 64: small_dispatch<64>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
-            case 128: small_dispatch<128>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
-            case 256: small_dispatch<256>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
-            case 512: small_dispatch<512>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
-            case 1024: small_dispatch<1024>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
-            case 2048: small_dispatch<2048>(A, L, r0, r1, level, pk, pv, smem, tmp, acc); break;
+            case 0: break;
+            case 2: small_dispatch<2>(A, L, d0, d1, level, pk, pv, smem, tmp, acc, part, parts); break;
+            case 4: small_dispatch<4>(A, L, d0, d1, level, pk, pv, smem, tmp, acc, part, parts); break;
+            case 8: small_dispatch<8>(A, L, d0, d1, level, pk, pv, smem, tmp, acc, part, parts); break;
+            case 16: small_dispatch<16>(A, L, d0, d1, level, pk, pv, smem, tmp, acc, part, parts); break;
+            case 32: small_dispatch<32>(A, L, d0, d1, level, pk, pv, smem, tmp, acc, part, parts); break;
+            case 64: small_dispatch<64>(A, L, d0, d1, level, pk, pv, smem, tmp, acc, part, parts); break;
+            case 128: small_dispatch<128>(A, L, d0, d1, level, pk, pv, smem, tmp, acc, part, parts); break;
+            case 256: small_dispatch<256>(A, L, d0, d1, level, pk, pv, smem, tmp, acc, part, parts); break;
+            case 512: small_dispatch<512>(A, L, d0, d1, level, pk, pv, smem, tmp, acc, part, parts); break;
+            case 1024: small_dispatch<1024>(A, L, d0, d1, level, pk, pv, smem, tmp, acc, part, parts); break;
+            case 2048: small_dispatch<2048>(A, L, d0, d1, level, pk, pv, smem, tmp, acc, part, parts); break;
             default:
                 if (!grid_windows(A, L, r0, r1, W, level, pk, pv, smem, tmp, acc))
                     return;
@@ -1244,6 +1336,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             // the CTA must be done with this run's staging first
             __syncthreads();
         }
+        cta_range(nw, lo, hi);
+        if (fused)  // the CTA's own range was dispatched (and flagged) by its own warps
+            count_rejected(A, L, level, lo, hi, true, CNT(scan_id), CNTI(scan_id));
         if (!grid_barrier(&st->bar, &st->err))
             return;
         // Next level. Rejected windows keep their insertions, which are
@@ -1260,50 +1355,19 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         uint32_t *nwb = nxt ? A.wb[1] : A.wb[0];
         uint64_t *nk = nxt ? A.ikeys[1] : A.ikeys[0];
         uint8_t *nv = nxt ? A.ivals[1] : A.ivals[0];
-        cta_range(nw, lo, hi);
-        {
-            uint32_t ch = 0, ci = 0;
-            constexpr int CU = 2;  // windows per thread per step, their fields loaded together
-            for (uint32_t w0 = lo + threadIdx.x; w0 < hi; w0 += CU * BLOCK) {
-                uint32_t f0[CU], fl[CU], g[CU], gl[CU], nd[CU], ndl[CU], wa[CU], wb[CU];
-#pragma unroll
-                for (int u = 0; u < CU; ++u) {
-                    // the window's and its left neighbour's fields
-                    const uint32_t w = w0 + u * BLOCK;
-                    const bool ok = w < hi;
-                    f0[u] = ok ? A.wflag[w] : 1u;
-                    fl[u] = ok && w > 0 ? A.wflag[w - 1] : 1u;
-                    g[u] = ok ? L.graph[w] : 0u;
-                    gl[u] = ok && w > 0 ? L.graph[w - 1] : 0u;
-                    nd[u] = ok ? L.node[w] : 0u;
-                    ndl[u] = ok && w > 0 ? L.node[w - 1] : 0u;
-                    wa[u] = ok ? L.a[w] : 0u;
-                    wb[u] = ok ? L.b[w] : 0u;
-                }
-#pragma unroll
-                for (int u = 0; u < CU; ++u) {
-                    if (f0[u])
-                        continue;  // accepted (or past the range)
-                    const GraphDesc &Dg = A.gd[g[u]];
-                    if (level >= Dg.height)
-                        continue;  // root window: to the remaining buffer
-                    const uint32_t W = Dg.seg << level;
-                    ci += wb[u] - wa[u];
-                    const uint32_t par = nd[u] & ~W;
-                    const bool merged = w0 + u * BLOCK > 0 && !fl[u] && gl[u] == g[u] && (ndl[u] & ~W) == par;
-                    ch += merged ? 0u : 1u;
-                }
-            }
-            const uint4 t = block_sum4(make_uint4(ch, ci, 0, 0));
-            if (threadIdx.x == 0) {
-                CNT(scan_id)[blockIdx.x] = t.x;
-                CNTI(scan_id)[blockIdx.x] = t.y;
-            }
+        if (!fused) {
+            count_rejected(A, L, level, lo, hi, false, CNT(scan_id), CNTI(scan_id));
+            if (!grid_barrier(&st->bar, &st->err))
+                return;
         }
-        if (!grid_barrier(&st->bar, &st->err))
-            return;
         uint32_t nw_next, base_i, total_i;
         cta_prefix2(CNT(scan_id), CNTI(scan_id), base, nw_next, base_i, total_i);
+        if (fused) {
+            uint32_t c_before, c_all;
+            head_corrections(A, L, nw, level, c_before, c_all);
+            base -= c_before;
+            nw_next -= c_all;
+        }
         if (nw_next == 0 && level < A.min_height) {
             // every window of this level was accepted and none can be a root
             // window: nothing to carry, no next level (counted as the loop's
