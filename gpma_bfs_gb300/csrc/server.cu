@@ -300,8 +300,8 @@ gpma_status gpma_server_create(const gpma_server_config *cfg, void *stream, gpma
     s->cfg = *cfg;
     s->plan_only = (cfg->flags & GPMA_SERVER_PLAN_ONLY) != 0;
     s->stream = (cudaStream_t)stream;
-    // each lane's round update buffers (about 110 bytes per key) are charged up front
-    s->fixed_bytes = 110ull * cfg->max_round_keys * lanes;
+    // each lane's round update buffers (about 120 bytes per key) are charged up front
+    s->fixed_bytes = 120ull * cfg->max_round_keys * lanes;
     if (s->fixed_bytes > cfg->hbm_budget_bytes) {
         delete s;
         set_error("gpma_server_create: round buffers for %llu keys exceed the budget",
@@ -962,6 +962,27 @@ gpma_status gpma_server_start(gpma_server *s) {
     int dev = -1;  // plan-only mode: no device
     if (!s->plan_only)
         GPMA_CUDA(cudaGetDevice(&dev));
+    if (!s->plan_only) {
+        // each lane's update buffers for a full round (max_round_keys keys, as
+        // charged to the budget) and its search state for every graph added so
+        // far, allocated now rather than by the first rounds that need them
+        // (an allocation inside a round stalls it and the other lanes)
+        std::vector<gpma_graph *> all;
+        for (Graph &G : s->graphs)
+            all.push_back(G.g);
+        const uint32_t k = (uint32_t)all.size();
+        std::vector<uint32_t> zero(k, 0u), one(k, 1u);
+        std::vector<const uint32_t *> srcs(k);
+        for (uint32_t i = 0; i < k; ++i)
+            srcs[i] = &zero[i];
+        for (Lane &L : s->lanes) {
+            GPMA_TRY(ensure_buffers(L.batch->buf, s->cfg.max_round_keys, std::max<uint32_t>(k, 1)));
+            if (k) {
+                BatchBfsPlan P;
+                GPMA_TRY(batch_bfs_plan(L.batch, all.data(), srcs.data(), one.data(), k, nullptr, &P));
+            }
+        }
+    }
     s->epoch = std::chrono::steady_clock::now();
     s->stopping = false;
     s->loop_status = GPMA_OK;

@@ -2478,6 +2478,23 @@ gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
         GPMA_TRY(dev_alloc(&b.wflag, cap));
         GPMA_TRY(dev_alloc(&b.wlive, cap));
         b.cap = cap;
+        // the bucket sort's buffers grow with the batch buffers, so a served
+        // round does not meet a first allocation later (a launch of n keys over
+        // k graphs uses at most n/16 + k buckets and n/1024 + k items)
+        const uint64_t gq = std::max<uint32_t>(graphs, std::max<uint32_t>(b.gcap, 1));
+        dev_free(b.qrec);
+        dev_free(b.qcnt);
+        dev_free(b.qinfo);
+        dev_free(b.qbound);
+        b.qrec_cap = b.q_cap = b.qbound_cap = 0;
+        GPMA_TRY(dev_alloc(&b.qrec, 2 * cap));
+        b.qrec_cap = cap;
+        GPMA_TRY(dev_alloc(&b.qcnt, cap / 16 + 2 * gq + 64));
+        GPMA_TRY(dev_alloc(&b.qinfo, cap / 16 + 2 * gq + 64));
+        b.q_cap = cap / 16 + 2 * gq + 64;
+        GPMA_TRY(dev_alloc(&b.qbound, cap / 1024 + gq + 64));
+        b.qbound_cap = cap / 1024 + gq + 64;
+        b.dirty = true;  // the new bucket counts are cleared before the next launch
     }
     if (graphs > b.gcap || !b.d_tab) {
         const uint32_t gc = std::max<uint32_t>(graphs, 1);
