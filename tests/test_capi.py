@@ -93,6 +93,7 @@ def test_null_arguments_rejected_without_gpu(built_lib):
     assert L.gpma_step_destroy(None) == 0
     assert L.gpma_batch_step_create(None, None, 0, ctypes.byref(out)) == 1
     assert L.gpma_batch_step_run(None, None, None, None, None, None, None, None) == 1
+    assert L.gpma_batch_step_run_many(None, 2, None, None, None, None, None, None, None) == 1
     assert L.gpma_batch_step_destroy(None) == 0
     assert L.gpma_validate(None, None, None) == 1
     assert L.gpma_partition_rows(None, None, 0, 10, 0, 1, None, None, None) == 1
@@ -183,3 +184,26 @@ def test_test_hooks_round_trip_and_reject_bad_values(built_lib):
     finally:
         G.set_test_hooks(**old)
     assert G.get_test_hooks()["update_stall"] == 0
+
+
+def test_update_sort_setting(built_lib):
+    """The batch-sort switch is host state: 0 (buckets) and 1 (digit passes)
+    are accepted, anything else is rejected and leaves the setting alone."""
+    import gpma_bfs_gb300 as G
+
+    old = G.get_tuning()
+    try:
+        assert old["update_sort"] == 0
+        G.set_tuning(update_sort=1)
+        assert G.get_tuning()["update_sort"] == 1
+        with pytest.raises(G.GPMAError):
+            G.set_tuning(update_sort=2)
+        assert G.get_tuning()["update_sort"] == 1
+    finally:
+        G.set_tuning(**old)
+
+
+def test_profile_reports_sort_fallbacks(built_lib):
+    import gpma_bfs_gb300 as G
+
+    assert "sort_fallbacks" in [n for n, _ in G._Profile._fields_]
