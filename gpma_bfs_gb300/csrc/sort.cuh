@@ -1,9 +1,10 @@
-// sort.cuh - stable LSD radix sort of the update batches of one or more
-// graphs (u64 key, u8 value), run as phases of the persistent update kernel.
+// sort.cuh - stable sort of the update batches of one or more graphs (u64
+// key, u8 value), run as phases of the persistent update kernel: a bucket
+// sort (below) and, for batches that crowd one bucket, LSD radix passes.
 //
 // Replaces thrust::sort_by_key of the batch (gpma.cuh:977), a stable radix
-// sort. Onesweep design, segmented by graph (graph g's batch occupies
-// [boff[g], boff[g+1]) and stays there):
+// sort. The digit passes are a onesweep design, segmented by graph (graph g's
+// batch occupies [boff[g], boff[g+1]) and stays there):
 //   1. one pass histograms all eight 8-bit digits of every graph's batch at
 //      once (and flags keys whose column is the reserved 0xFFFFFFFF);
 //   2. digits constant over every batch are skipped;

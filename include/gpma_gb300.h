@@ -445,7 +445,7 @@ typedef struct gpma_profile {
     uint64_t bfs_kernels;    /* launches of BFS traversal kernels */
     uint64_t kernel_launches;
     uint64_t bfs_edges;      /* edges scanned from reached nodes by multi-source BFS, summed over sources */
-    uint64_t sort_fallbacks; /* update launches whose bucket sort met a bucket of more than 3072 keys and
+    uint64_t sort_fallbacks; /* update launches whose bucket sort met a bucket of more than 1024 keys and
                                 sorted by digit passes instead */
 } gpma_profile;
 GPMA_API gpma_status gpma_set_profiling(gpma_graph *g, int enabled);
@@ -481,7 +481,7 @@ typedef struct gpma_tuning {
     uint32_t update_sort;          /* batch sort inside the update kernel: 0 buckets (equal slot ranges of the
                                       array, a key placed by its row's slots) ranked, scattered and sorted in
                                       shared memory, with the digit passes taken when one bucket holds more than
-                                      3072 keys; 1 digit passes always */
+                                      1024 keys; 1 digit passes always */
     uint32_t reserved[2];
 } gpma_tuning;
 GPMA_API gpma_status gpma_get_tuning(gpma_tuning *out);

@@ -85,7 +85,7 @@ def test_crowded_bucket_falls_back_to_digit_passes(sort_mode):
     G.update_gpma(g, k, v)
     o.update(k, v)
     # 12000 keys into three rows: their slots (a few dozen) lie in one or two
-    # buckets, which then hold far more than 3072 keys
+    # buckets, which then hold far more than 1024 keys
     k, v = _batch_with_repeats(rng, n, 12000, 1, rows=np.array([7, 8, 9]))
     G.update_gpma(g, k, v)
     o.update(k, v)
