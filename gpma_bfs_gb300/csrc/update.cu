@@ -3,7 +3,8 @@
 // Replaces update_gpma (gpma.cuh:968-1050). One persistent cooperative kernel
 // runs every step of the update of one or more independent graphs, with
 // bounded grid barriers instead of host round trips:
-//   S  stable radix sort of each graph's batch (sort.cuh, gpma.cuh:977);
+//   S  stable sort of each graph's batch (sort.cuh, gpma.cuh:977): a bucket
+//      sort, or radix digit passes for a batch that crowds one bucket;
 //   P1 locate: the reference's top-down search over segment first keys (its
 //      upper levels from a shared-memory copy when one graph is updated), then
 //      an equality scan of the leaf with 16-byte loads; hits store the
