@@ -158,7 +158,7 @@ struct BatchBuffers {
     uint32_t *wgraph[2] = {nullptr, nullptr};
     uint32_t *wa[2] = {nullptr, nullptr};
     uint32_t *wb[2] = {nullptr, nullptr};
-    uint32_t *wflag = nullptr;
+    uint32_t *wflag = nullptr;  // 2 * cap: one array per level parity
     uint32_t *wlive = nullptr;
     uint64_t *top = nullptr;    // one graph: its top-of-tree heads, gathered per launch for the locate cache
     // sort state
@@ -202,7 +202,7 @@ struct BatchBuffers {
     uint32_t *chunk_cnt = nullptr;
     uint64_t chunk_cap = 0;
     // persistent-kernel scratch
-    uint32_t *cta_cnt = nullptr;       // 4 * grid
+    uint32_t *cta_cnt = nullptr;       // 8 * grid: four count arrays, two window-range arrays
 };
 constexpr size_t STAT_GS_OFFSET = 128;
 static_assert(sizeof(DeviceStatus) <= STAT_GS_OFFSET, "status slot layout");

@@ -96,7 +96,7 @@ struct UpdateArgs {
     uint32_t *wgraph[2];
     uint32_t *wa[2];
     uint32_t *wb[2];
-    uint32_t *wflag;
+    uint32_t *wflag[2];  // window flags by level parity: a level may start before every CTA read the last
     uint32_t *wlive;
     uint32_t *chunk_cnt;
     uint32_t *cta_cnt;
@@ -118,6 +118,7 @@ struct UpdateArgs {
 // Current window list of a level.
 struct Windows {
     const uint32_t *node, *graph, *a, *b;
+    uint32_t *flag;  // per window: accepted (1) or rejected (0) at this level
 };
 
 __device__ __forceinline__ uint32_t graph_of(const UpdateArgs &A, uint32_t i) {
@@ -603,7 +604,7 @@ __device__ void warp_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
                 ++acc;
         }
         if (has && gl == 0)
-            A.wflag[w] = accept ? 1u : 0u;
+            L.flag[w] = accept ? 1u : 0u;
         __syncwarp();
     }
 }
@@ -707,7 +708,7 @@ __device__ void cta_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32_
                 ++acc;
         }
         if (tid == 0)
-            A.wflag[w] = accept ? 1u : 0u;
+            L.flag[w] = accept ? 1u : 0u;
         __syncthreads();
     }
 }
@@ -757,7 +758,7 @@ __device__ bool grid_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
         if (!in_bounds(&A.st->err, L.a[w] <= L.b[w] && L.b[w] <= A.n, BS_PENDING))
             accept = false;
         if (threadIdx.x == 0) {
-            A.wflag[w] = accept ? 1u : 0u;
+            L.flag[w] = accept ? 1u : 0u;
             A.wlive[w] = run;
             if (accept)
                 ++acc;
@@ -768,7 +769,7 @@ __device__ bool grid_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
     // B3: stable compaction of accepted windows into the graph's scratch arrays
     for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
         const uint32_t w = r0 + c / cpw, k = c % cpw;
-        if (!A.wflag[w])
+        if (!L.flag[w])
             continue;
         const GraphDesc &D = A.gd[L.graph[w]];
         const uint32_t node = L.node[w];
@@ -800,7 +801,7 @@ __device__ bool grid_windows(const UpdateArgs &A, Windows L, uint32_t r0, uint32
     uint8_t *mv = reinterpret_cast<uint8_t *>(mk + CHUNK);
     for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
         const uint32_t w = r0 + c / cpw, k = c % cpw;
-        if (!A.wflag[w])
+        if (!L.flag[w])
             continue;
         const GraphDesc &D = A.gd[L.graph[w]];
         const uint32_t node = L.node[w], a = L.a[w];
@@ -855,8 +856,8 @@ __device__ __forceinline__ void count_rejected(const UpdateArgs &A, const Window
             const uint32_t w = w0 + u * BLOCK;
             const bool ok = w < hi;
             const bool left = ok && w > 0 && !(first_is_head && w == lo);
-            f0[u] = ok ? A.wflag[w] : 1u;
-            fl[u] = left ? A.wflag[w - 1] : 1u;
+            f0[u] = ok ? L.flag[w] : 1u;
+            fl[u] = left ? L.flag[w - 1] : 1u;
             g[u] = ok ? L.graph[w] : 0u;
             gl[u] = left ? L.graph[w - 1] : 0u;
             nd[u] = ok ? L.node[w] : 0u;
@@ -888,18 +889,21 @@ __device__ __forceinline__ void count_rejected(const UpdateArgs &A, const Window
 // One graph, counts taken with first_is_head: the CTAs c >= 1 whose first
 // window was counted as a start but joins its left neighbour (both rejected,
 // not root windows, one parent): how many precede this CTA, and in all.
+// slices: each CTA's range [lo, hi) as (lo, hi) pairs, or null for the
+// ranges of cta_range.
 __device__ __forceinline__ void head_corrections(const UpdateArgs &A, const Windows &L, uint32_t nw, uint32_t level,
-                                                 uint32_t &before, uint32_t &all) {
+                                                 const uint32_t *slices, uint32_t &before, uint32_t &all) {
     const uint32_t per = (nw + gridDim.x - 1) / gridDim.x;
     const GraphDesc &D = A.gd[0];
     const uint32_t W = D.seg << level;
     const bool root = level >= D.height;
     uint32_t b = 0, t = 0;
     for (uint32_t c = 1 + threadIdx.x; c < gridDim.x; c += BLOCK) {
-        const uint32_t w = c * per;
-        if (root || w >= nw)
-            continue;
-        const uint32_t f0 = A.wflag[w], fl = A.wflag[w - 1];
+        const uint32_t w = slices ? __ldcg(slices + 2 * c) : c * per;
+        const uint32_t w_end = slices ? __ldcg(slices + 2 * c + 1) : min(nw, w + per);
+        if (root || w >= w_end || w == 0)
+            continue;  // an empty range, or nothing to its left
+        const uint32_t f0 = L.flag[w], fl = L.flag[w - 1];
         const uint32_t nd = L.node[w], ndl = L.node[w - 1];
         if (!f0 && !fl && (nd & ~W) == (ndl & ~W)) {
             ++t;
@@ -1005,6 +1009,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
     uint32_t scan_id = 0;
 #define CNT(id) ((id) ? A.cta_cnt + G : A.cta_cnt)
 #define CNTI(id) ((id) ? A.cta_cnt + 3 * G : A.cta_cnt + 2 * G)
+#define SLICES(p) (A.cta_cnt + 4 * G + 2 * (p) * G)  // per CTA (lo, hi) of its windows, by level parity
     unsigned long long acc = 0, acc_slots = 0;
     if (stamper)
         st->stamp[1] = globaltimer_ns();
@@ -1280,6 +1285,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
     // buffers selected by `cur`; each window's insertions are the contiguous
     // range [wa, wb) of the current insertion buffer.
     uint32_t cur = 0, level = 0;
+    // own: this level's windows [olo, ohi) of this CTA are the ones it wrote
+    // in the last level's carry pass, which ended without a grid barrier
+    bool own = false;
+    uint32_t olo = 0, ohi = 0;
     for (; level <= A.max_height && nw > 0; ++level) {
         // one graph, windows of at most CTA_WINDOW_MAX slots: each CTA
         // dispatches a contiguous range of the windows and counts its rejected
@@ -1290,6 +1299,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         L.graph = cur ? A.wgraph[1] : A.wgraph[0];
         L.a = cur ? A.wa[1] : A.wa[0];
         L.b = cur ? A.wb[1] : A.wb[0];
+        L.flag = A.wflag[level & 1];
         const uint64_t *pk = cur ? A.ikeys[1] : A.ikeys[0];
         const uint8_t *pv = cur ? A.ivals[1] : A.ivals[0];
         // one run of windows per segment length (a single run for one graph)
@@ -1309,7 +1319,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             // each CTA takes the contiguous range it counts (and copies) next
             uint32_t d0 = r0, d1 = r1, part = blockIdx.x, parts = gridDim.x;
             if (fused) {
-                cta_range(nw, d0, d1);
+                if (own) {
+                    d0 = olo;
+                    d1 = ohi;
+                } else {
+                    cta_range(nw, d0, d1);
+                }
                 part = 0;
                 parts = 1;
                 if (d0 >= d1)
@@ -1337,7 +1352,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             // the CTA must be done with this run's staging first
             __syncthreads();
         }
-        cta_range(nw, lo, hi);
+        if (own) {
+            lo = olo;
+            hi = ohi;
+        } else {
+            cta_range(nw, lo, hi);
+        }
         if (fused)  // the CTA's own range was dispatched (and flagged) by its own warps
             count_rejected(A, L, level, lo, hi, true, CNT(scan_id), CNTI(scan_id));
         if (!grid_barrier(&st->bar, &st->err))
@@ -1365,7 +1385,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         cta_prefix2(CNT(scan_id), CNTI(scan_id), base, nw_next, base_i, total_i);
         if (fused) {
             uint32_t c_before, c_all;
-            head_corrections(A, L, nw, level, c_before, c_all);
+            head_corrections(A, L, nw, level, own ? SLICES(level & 1) : nullptr, c_before, c_all);
             base -= c_before;
             nw_next -= c_all;
         }
@@ -1384,9 +1404,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
         // window) and the exclusive prefix of the counts, so the whole CTA
         // copies the concatenated ranges (a window of a million insertions is
         // not left to one warp)
+        // not left to one warp). A window whose left sibling ends the previous
+        // CTA's range has its insertions copied by that CTA, which writes the
+        // parent window: every next-level window's insertions come from the
+        // CTA that writes the window.
         uint32_t *l_src = reinterpret_cast<uint32_t *>(smem);
         uint32_t *l_pre = l_src + GROUP_ITEMS * BLOCK + 1;
         uint32_t *l_to = l_pre + GROUP_ITEMS * BLOCK + 1;  // destination offset | root << 31
+        const uint32_t next_lo = base;  // this CTA's first window of the next level
         for (uint32_t r0 = lo; r0 < hi; r0 += GROUP_ITEMS * BLOCK) {
             const uint32_t w0 = r0 + GROUP_ITEMS * threadIdx.x;
             // windows w0 - 1 .. w0 + GROUP_ITEMS: each needs both neighbours
@@ -1396,7 +1421,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             for (uint32_t q = 0; q < GROUP_ITEMS + 2; ++q) {
                 const uint32_t j = w0 + q - 1;
                 const bool ok = w0 + q >= 1 && j < nw;
-                fl[q] = ok ? A.wflag[j] : 1u;
+                fl[q] = ok ? L.flag[j] : 1u;
                 gg[q] = ok ? L.graph[j] : 0u;
                 nd[q] = ok ? L.node[j] : 0u;
                 wa[q] = ok ? L.a[j] : 0u;
@@ -1410,13 +1435,17 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
                 if (!rej)
                     continue;
                 const GraphDesc &Dg = A.gd[gg[q + 1]];
-                ++rsum;
-                asum += wb[q + 1] - wa[q + 1];
-                if (level >= Dg.height)
-                    continue;  // root window
-                csum += wb[q + 1] - wa[q + 1];
+                const bool root = level >= Dg.height;
                 const uint32_t W = Dg.seg << level;
-                const bool merged = j > 0 && !fl[q] && gg[q] == gg[q + 1] && (nd[q] & ~W) == (nd[q + 1] & ~W);
+                const bool merged =
+                    !root && j > 0 && !fl[q] && gg[q] == gg[q + 1] && (nd[q] & ~W) == (nd[q + 1] & ~W);
+                if (!(merged && j == lo)) {  // else the previous CTA copies it
+                    ++rsum;
+                    asum += wb[q + 1] - wa[q + 1];
+                }
+                if (root)
+                    continue;
+                csum += wb[q + 1] - wa[q + 1];
                 hsum += merged ? 0u : 1u;
             }
             uint32_t tot_i, tot_h, tot_r, tot_a;
@@ -1433,6 +1462,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
                 const uint32_t g = gg[q + 1];
                 const GraphDesc &Dg = A.gd[g];
                 const uint32_t c = wb[q + 1] - wa[q + 1];
+                const uint32_t W = Dg.seg << level;
+                const uint32_t par = nd[q + 1] & ~W;
+                const bool merged = level < Dg.height && j > 0 && !fl[q] && gg[q] == g && (nd[q] & ~W) == par;
+                if (merged && j == lo) {
+                    nb += c;  // copied by the previous CTA
+                    continue;
+                }
                 l_src[li] = wa[q + 1];
                 l_pre[li] = pre;
                 pre += c;
@@ -1446,9 +1482,6 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
                 }
                 l_to[li] = nb;
                 ++li;
-                const uint32_t W = Dg.seg << level;
-                const uint32_t par = nd[q + 1] & ~W;
-                const bool merged = j > 0 && !fl[q] && gg[q] == g && (nd[q] & ~W) == par;
                 if (!merged) {
                     const bool right = j + 1 < nw && !fl[q + 2] && gg[q + 2] == g && (nd[q + 2] & ~W) == par;
                     nwn[e] = par;
@@ -1483,9 +1516,41 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
             base += tot_h;
             base_i += tot_i;
         }
+        if (hi > lo && hi < nw) {
+            // the last window's right sibling, rejected, begins the next
+            // CTA's range: its insertions follow this CTA's
+            const uint32_t j = hi - 1;
+            const uint32_t g = L.graph[j];
+            const GraphDesc &Dg = A.gd[g];
+            const uint32_t W = Dg.seg << level;
+            if (level < Dg.height && !L.flag[j] && !L.flag[hi] && L.graph[hi] == g &&
+                (L.node[j] & ~W) == (L.node[hi] & ~W)) {
+                const uint32_t a = L.a[hi], c = L.b[hi] - a;
+                for (uint32_t k = threadIdx.x; k < c; k += BLOCK) {
+                    nk[base_i + k] = pk[a + k];
+                    nv[base_i + k] = pv[a + k];
+                }
+            }
+            __syncthreads();
+        }
         scan_id ^= 1;
-        if (!grid_barrier(&st->bar, &st->err))
+        // The next level goes on without a grid barrier when it too is fused:
+        // each CTA then takes the windows it just wrote, whose insertions it
+        // copied itself, and the slots they cover were last written before
+        // this level's barrier. The window flags alternate by level, so a CTA
+        // flagging the next level's windows does not overwrite ones a slower
+        // CTA still reads here.
+        own = fused && nw_next > 0 && level + 1 <= A.max_height && (A.gd[0].seg << (level + 1)) <= CTA_WINDOW_MAX;
+        if (own) {
+            olo = next_lo;
+            ohi = base;
+            if (threadIdx.x == 0) {
+                SLICES((level + 1) & 1)[2 * blockIdx.x] = olo;
+                SLICES((level + 1) & 1)[2 * blockIdx.x + 1] = ohi;
+            }
+        } else if (!grid_barrier(&st->bar, &st->err)) {
             return;
+        }
         nw = nw_next;
         cur = nxt;
     }
@@ -2476,7 +2541,7 @@ gpma_status ensure_buffers(BatchBuffers &b, uint64_t n, uint32_t graphs) {
         GPMA_TRY(dev_alloc(&b.rvals, cap));
         GPMA_TRY(dev_alloc(&b.ileaf, cap));
         GPMA_TRY(dev_alloc(&b.igraph, cap));
-        GPMA_TRY(dev_alloc(&b.wflag, cap));
+        GPMA_TRY(dev_alloc(&b.wflag, 2 * cap));  // one array per level parity
         GPMA_TRY(dev_alloc(&b.wlive, cap));
         b.cap = cap;
         // the bucket sort's buffers grow with the batch buffers, so a served
@@ -2549,7 +2614,7 @@ gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t
     }
     GPMA_TRY(ensure_buffers(buf, n, k));
     if (!buf.cta_cnt)
-        GPMA_TRY(dev_alloc(&buf.cta_cnt, 4ull * sms * MAX_BLOCKS_PER_SM));  // any tuned grid
+        GPMA_TRY(dev_alloc(&buf.cta_cnt, 8ull * sms * MAX_BLOCKS_PER_SM));  // any tuned grid
     // per-graph tables in the pinned staging copy: descriptors, batch offsets,
     // sort tile offsets (the previous launch's upload finished: it synchronised)
     GraphDesc *h_gd = reinterpret_cast<GraphDesc *>(buf.h_tab);
@@ -2684,7 +2749,8 @@ gpma_status update_plan(gpma_graph *const *graphs, const uint64_t *off, uint32_t
     A.rvals = buf.rvals;
     A.ileaf = buf.ileaf;
     A.igraph = buf.igraph;
-    A.wflag = buf.wflag;
+    A.wflag[0] = buf.wflag;
+    A.wflag[1] = buf.wflag + buf.cap;
     A.wlive = buf.wlive;
     A.chunk_cnt = buf.chunk_cnt;
     A.cta_cnt = buf.cta_cnt;
