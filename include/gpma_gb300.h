@@ -114,10 +114,9 @@ GPMA_API gpma_status gpma_bfs_multi(gpma_graph *g, const uint32_t *srcs, uint32_
  * Limits: row_num <= 2,097,152 (GPMA_ERR_CAPACITY beyond); levels must be
  * device memory of row_num entries (GPMA_ERR_INVALID otherwise); reached is an
  * optional host pointer. The first call on a device looks up the array's
- * device address with that device current; make that first call before any
- * stream capture. All calls share the one array and it keeps the last call's
- * contents, so calls whose work overlaps on the GPU (other threads, other
- * streams) race: serialise them. */
+ * device address with that device current. All calls share the one array
+ * and it keeps the last call's contents, so calls whose work overlaps on the
+ * GPU (other threads, other streams) race: serialise them. */
 GPMA_API gpma_status gpma_bfs_noalloc(gpma_graph *g, uint32_t src, uint32_t *levels, uint64_t *reached,
                                       void *stream);
 
