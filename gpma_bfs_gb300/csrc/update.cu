@@ -307,6 +307,31 @@ __device__ __forceinline__ uint4 block_sum4(uint4 x) {
     return r;
 }
 
+// Four exclusive scans over the CTA in one shared-memory round (every thread
+// gets its four prefixes and the four totals).
+__device__ __forceinline__ uint4 block_excl_scan4(uint4 x, uint4 &total) {
+    __shared__ uint4 s_scan[BLOCK / 32 + 1];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint4 inc = make_uint4(warp_incl_scan(x.x), warp_incl_scan(x.y), warp_incl_scan(x.z), warp_incl_scan(x.w));
+    if (lane == 31)
+        s_scan[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const uint4 v = lane < BLOCK / 32 ? s_scan[lane] : make_uint4(0, 0, 0, 0);
+        const uint4 vi =
+            make_uint4(warp_incl_scan(v.x), warp_incl_scan(v.y), warp_incl_scan(v.z), warp_incl_scan(v.w));
+        if (lane < BLOCK / 32)
+            s_scan[lane] = make_uint4(vi.x - v.x, vi.y - v.y, vi.z - v.z, vi.w - v.w);
+        if (lane == BLOCK / 32 - 1)
+            s_scan[BLOCK / 32] = vi;
+    }
+    __syncthreads();
+    const uint4 pre = s_scan[warp];
+    total = s_scan[BLOCK / 32];
+    __syncthreads();  // the next call may overwrite s_scan
+    return make_uint4(pre.x + inc.x - x.x, pre.y + inc.y - x.y, pre.z + inc.z - x.z, pre.w + inc.w - x.w);
+}
+
 // Sum of ca[0..blockIdx.x) and of ca[0..gridDim.x), and the same of cb (or
 // zeros without cb): per-CTA counts written before the last grid barrier. A
 // thread's loads are all issued before the first is used.
@@ -842,7 +867,7 @@ __device__ __forceinline__ uint32_t first_window_of_seg(const UpdateArgs &A, con
 // rejected right sibling joins its rejected left sibling) into cnt_h, and
 // their insertions into cnt_i, at blockIdx.x; root windows count in neither.
 // first_is_head: window lo counts as a start whatever its left neighbour
-// (whose flag may not be written yet); head_corrections removes those that
+// (whose flag may not be written yet); level_prefix removes those that
 // are not.
 __device__ __forceinline__ void count_rejected(const UpdateArgs &A, const Windows &L, uint32_t level, uint32_t lo,
                                                uint32_t hi, bool first_is_head, uint32_t *cnt_h, uint32_t *cnt_i) {
@@ -886,33 +911,63 @@ __device__ __forceinline__ void count_rejected(const UpdateArgs &A, const Window
     }
 }
 
-// One graph, counts taken with first_is_head: the CTAs c >= 1 whose first
-// window was counted as a start but joins its left neighbour (both rejected,
-// not root windows, one parent): how many precede this CTA, and in all.
-// slices: each CTA's range [lo, hi) as (lo, hi) pairs, or null for the
-// ranges of cta_range.
-__device__ __forceinline__ void head_corrections(const UpdateArgs &A, const Windows &L, uint32_t nw, uint32_t level,
-                                                 const uint32_t *slices, uint32_t &before, uint32_t &all) {
+// The level's prefix sums over the per-CTA counts of count_rejected (written
+// before the last grid barrier): this CTA's first next-level window (base_h)
+// and insertion (base_i), and the totals. fused: one graph, counts taken with
+// first_is_head; a CTA c >= 1 whose first window was counted as a start but
+// joins its left neighbour (both rejected, one parent, not root windows) has
+// that start taken off here, its fields read in the same round as the counts.
+// slices: each CTA's range as (lo, hi) pairs, or null for cta_range's.
+__device__ __forceinline__ void level_prefix(const UpdateArgs &A, const Windows &L, uint32_t nw, uint32_t level,
+                                             bool fused, const uint32_t *slices, const uint32_t *cnt_h,
+                                             const uint32_t *cnt_i, uint32_t &base_h, uint32_t &total_h,
+                                             uint32_t &base_i, uint32_t &total_i) {
     const uint32_t per = (nw + gridDim.x - 1) / gridDim.x;
     const GraphDesc &D = A.gd[0];
     const uint32_t W = D.seg << level;
-    const bool root = level >= D.height;
-    uint32_t b = 0, t = 0;
-    for (uint32_t c = 1 + threadIdx.x; c < gridDim.x; c += BLOCK) {
-        const uint32_t w = slices ? __ldcg(slices + 2 * c) : c * per;
-        const uint32_t w_end = slices ? __ldcg(slices + 2 * c + 1) : min(nw, w + per);
-        if (root || w >= w_end || w == 0)
-            continue;  // an empty range, or nothing to its left
-        const uint32_t f0 = L.flag[w], fl = L.flag[w - 1];
-        const uint32_t nd = L.node[w], ndl = L.node[w - 1];
-        if (!f0 && !fl && (nd & ~W) == (ndl & ~W)) {
-            ++t;
-            b += c < blockIdx.x ? 1u : 0u;
+    const bool starts = fused && level < D.height;  // else no correction
+    constexpr int CU = 2;  // CTAs per thread per step
+    uint4 s = make_uint4(0, 0, 0, 0);
+    for (uint32_t j0 = 0; j0 < gridDim.x; j0 += CU * BLOCK) {
+        uint32_t vh[CU], vi[CU], w[CU], w_end[CU];
+#pragma unroll
+        for (int u = 0; u < CU; ++u) {
+            const uint32_t c = j0 + u * BLOCK + threadIdx.x;
+            const bool in = c < gridDim.x;
+            vh[u] = in ? __ldcg(cnt_h + c) : 0u;
+            vi[u] = in ? __ldcg(cnt_i + c) : 0u;
+            w[u] = 0;
+            w_end[u] = 0;
+            if (starts && in && c >= 1) {
+                w[u] = slices ? __ldcg(slices + 2 * c) : c * per;
+                w_end[u] = slices ? __ldcg(slices + 2 * c + 1) : min(nw, c * per + per);
+            }
+        }
+        uint32_t f0[CU], fl[CU], nd[CU], ndl[CU];
+#pragma unroll
+        for (int u = 0; u < CU; ++u) {
+            const bool chk = w[u] < w_end[u] && w[u] > 0;  // a non-empty range with a window to its left
+            f0[u] = chk ? L.flag[w[u]] : 1u;
+            fl[u] = chk ? L.flag[w[u] - 1] : 1u;
+            nd[u] = chk ? L.node[w[u]] : 0u;
+            ndl[u] = chk ? L.node[w[u] - 1] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < CU; ++u) {
+            const uint32_t c = j0 + u * BLOCK + threadIdx.x;
+            const uint32_t h = vh[u] - ((!f0[u] && !fl[u] && (nd[u] & ~W) == (ndl[u] & ~W)) ? 1u : 0u);
+            const bool before = c < blockIdx.x;
+            s.x += before ? h : 0u;
+            s.y += h;
+            s.z += before ? vi[u] : 0u;
+            s.w += vi[u];
         }
     }
-    const uint4 r = block_sum4(make_uint4(b, t, 0, 0));
-    before = r.x;
-    all = r.y;
+    s = block_sum4(s);
+    base_h = s.x;
+    total_h = s.y;
+    base_i = s.z;
+    total_i = s.w;
 }
 
 // Two register budgets of the same kernel: MINB resident CTAs per SM. Two
@@ -1382,13 +1437,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
                 return;
         }
         uint32_t nw_next, base_i, total_i;
-        cta_prefix2(CNT(scan_id), CNTI(scan_id), base, nw_next, base_i, total_i);
-        if (fused) {
-            uint32_t c_before, c_all;
-            head_corrections(A, L, nw, level, own ? SLICES(level & 1) : nullptr, c_before, c_all);
-            base -= c_before;
-            nw_next -= c_all;
-        }
+        level_prefix(A, L, nw, level, fused, own ? SLICES(level & 1) : nullptr, CNT(scan_id), CNTI(scan_id), base,
+                     nw_next, base_i, total_i);
         if (nw_next == 0 && level < A.min_height) {
             // every window of this level was accepted and none can be a root
             // window: nothing to carry, no next level (counted as the loop's
@@ -1448,11 +1498,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) update_kernel(UpdateArgs A) {
                 csum += wb[q + 1] - wa[q + 1];
                 hsum += merged ? 0u : 1u;
             }
-            uint32_t tot_i, tot_h, tot_r, tot_a;
-            uint32_t nb = base_i + block_excl_scan(csum, &tot_i, tmp);
-            uint32_t e = base + block_excl_scan(hsum, &tot_h, tmp);
-            uint32_t li = block_excl_scan(rsum, &tot_r, tmp);
-            uint32_t pre = block_excl_scan(asum, &tot_a, tmp);
+            uint4 tot;
+            const uint4 ex = block_excl_scan4(make_uint4(csum, hsum, rsum, asum), tot);
+            const uint32_t tot_i = tot.x, tot_h = tot.y, tot_r = tot.z, tot_a = tot.w;
+            uint32_t nb = base_i + ex.x;
+            uint32_t e = base + ex.y;
+            uint32_t li = ex.z;
+            uint32_t pre = ex.w;
 #pragma unroll
             for (uint32_t q = 0; q < GROUP_ITEMS; ++q) {
                 const uint32_t j = w0 + q;
