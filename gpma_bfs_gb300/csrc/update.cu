@@ -23,7 +23,10 @@
 //      Windows are ordered by graph and graphs by segment length, so the list
 //      splits into one contiguous run per segment length and each run has one
 //      window width: up to 256 slots per warp group, up to 2048 per CTA in
-//      shared memory, wider ones chunk by chunk over the whole grid.
+//      shared memory, wider ones chunk by chunk over the whole grid. For one
+//      graph, a level of windows up to 2048 slots costs one grid barrier:
+//      each CTA dispatches, counts and carries a contiguous range of the
+//      windows and goes on with the next-level windows it wrote itself.
 // The host reads the status blocks once. Only the root resize (:1034-1044)
 // and the >= 5M-insertion rebuild (:936-966) run host-driven, per graph.
 #include "gpma_internal.cuh"
